@@ -1,0 +1,84 @@
+"""ctypes binding of the C ABI declared in ``include/petgem_gb300.h``.
+
+The shared library is the only implementation: if it is missing or fails to
+load, every entry point raises; there is no CPU fallback.
+"""
+import ctypes
+import os
+import threading
+
+from . import _build
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_INT = ctypes.c_int
+_SZ = ctypes.c_size_t
+_D = ctypes.c_double
+
+# name -> (restype, argtypes); mirrors include/petgem_gb300.h
+SIGNATURES = {
+    "pg_abi_version": (_INT, []),
+    "pg_last_error": (ctypes.c_char_p, []),
+    "pg_table_doubles": (_I64, [_INT]),
+    "pg_tuples_workspace_bytes": (_SZ, [_I64]),
+    "pg_orientation_tuples": (_INT, [_P, _P, _I64, _P, _P, _P, _P, _SZ, _P]),
+    "pg_tuple_tables": (_INT, [_P, _I64, _INT, _P, _P]),
+    "pg_elemental_matrices": (_INT, [_P, _P, _P, _P, _P, _I64, _INT, _P, _P, _P, _P]),
+}
+
+STATUS = {
+    0: "PG_OK", -1: "PG_ERR_ARG", -2: "PG_ERR_CUDA", -3: "PG_ERR_WORKSPACE", -4: "PG_ERR_UNSUPPORTED",
+    -5: "PG_ERR_DEGENERATE", -6: "PG_ERR_NOT_FOUND", -7: "PG_ERR_NOT_CONVERGED", -8: "PG_ERR_BREAKDOWN",
+    -9: "PG_ERR_NONFINITE",
+}
+
+
+class PetgemError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, name, status, msg):
+        self.status = status
+        super().__init__(f"{name} -> {STATUS.get(status, status)}: {msg}")
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) and return the ctypes library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing and _build.needs_build():
+            _build.build()
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise ImportError(f"petgem_gb300 native library not found at {path}; run petgem_gb300._build.build()")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def call(name, *args):
+    """Call a status-returning entry point; raise PetgemError on failure."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != 0:
+        msg = lib.pg_last_error()
+        raise PetgemError(name, st, msg.decode() if msg else "")
+    return st
+
+
+def query(name, *args):
+    """Call a size/value query entry point and return its result."""
+    return getattr(load(), name)(*args)

@@ -1,0 +1,119 @@
+"""Seeded synthetic meshes and models for the benchmark workloads.
+
+No public dataset is involved: every workload is a box split into n^3 cubes,
+each cube into 6 Kuhn tetrahedra, with analytic or seeded conductivities.
+All tetrahedra are generated with positive orientation, because petgem
+scales M and K by the signed det(J) (petgem/hvfem.py:265,313-314).
+"""
+import itertools
+
+import numpy as np
+
+
+def kuhn_box(n, lo=(-1000.0, -1000.0, -1000.0), hi=(1000.0, 1000.0, 1000.0)):
+    """Nodes (x fastest) and positively oriented Kuhn tets, cube by cube."""
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    ax = [np.linspace(lo[d], hi[d], n + 1) for d in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    nodes = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    k, j, i = [a.ravel() for a in np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")]
+
+    def vid(di, dj, dk):
+        return (i + di) + (n + 1) * ((j + dj) + (n + 1) * (k + dk))
+
+    tets = []
+    for perm in itertools.permutations(range(3)):
+        step = np.zeros(3, dtype=np.int64)
+        corner = [vid(0, 0, 0)]
+        for a in perm[:2]:
+            step[a] = 1
+            corner.append(vid(*step))
+        corner.append(vid(1, 1, 1))
+        inv = sum(1 for x in range(3) for y in range(x + 1, 3) if perm[x] > perm[y])
+        if inv % 2:                      # odd permutation -> negative volume
+            corner[1], corner[2] = corner[2], corner[1]
+        tets.append(np.stack(corner, axis=1))
+    tets = np.stack(tets, axis=1).reshape(-1, 4)     # cube-major: 6 tets per cube
+    return nodes, tets.astype(np.int64)
+
+
+def signed_volumes(nodes, tets):
+    c = nodes[tets]
+    return np.linalg.det(c[:, 1:] - c[:, :1]) / 6.0
+
+
+def jitter_interior(nodes, n, frac, seed, lo, hi):
+    """Move interior nodes by U(-frac*h, frac*h) per axis; boundary nodes fixed."""
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    h = (hi - lo) / n
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(-1.0, 1.0, size=nodes.shape) * frac * h
+    eps = 1e-9 * h
+    interior = np.all((nodes > lo + eps) & (nodes < hi - eps), axis=1)
+    out = nodes.copy()
+    out[interior] += d[interior]
+    return out
+
+
+class Model:
+    """A forward-modelling workload: mesh, conductivity, source, receivers."""
+
+    def __init__(self, name, nodes, tets, sigma, p, source, receivers, physical=None):
+        self.name = name
+        self.nodes = nodes
+        self.tets = tets
+        self.sigma = sigma            # (T, 2) horizontal, vertical
+        self.p = p
+        self.source = source          # dict: frequency, position, azimuth, dip, current, length
+        self.receivers = receivers    # (R, 3)
+        self.physical = physical
+
+
+def _hed(x=0.0, y=0.0, z=50.0, f=1.0):
+    return {"frequency": f, "position": [x, y, z], "azimuth": 0.0, "dip": 0.0, "current": 1.0, "length": 1.0}
+
+
+def csem_two_layer(n, p, block=True, f=1.0):
+    """Seawater 3.3 S/m above z=0, sediment 1.0 S/m below, optional 0.01 S/m
+    400x400x100 m block centred at (0,0,-300); x-HED at (0,0,50); 20
+    receivers on z=0, x in [-800, 800]."""
+    nodes, tets = kuhn_box(n)
+    cen = nodes[tets].mean(axis=1)
+    s = np.where(cen[:, 2] > 0.0, 3.3, 1.0)
+    if block:
+        blk = (np.abs(cen[:, 0]) <= 200.0) & (np.abs(cen[:, 1]) <= 200.0) & (cen[:, 2] >= -350.0) & (cen[:, 2] <= -250.0)
+        s[blk] = 0.01
+    sigma = np.stack([s, s], axis=1)
+    rx = np.stack([np.linspace(-800.0, 800.0, 20), np.zeros(20), np.zeros(20)], axis=1)
+    return Model(f"csem_two_layer_n{n}_p{p}", nodes, tets, sigma, p, _hed(f=f), rx)
+
+
+def config0():
+    """Plain FP64 CSEM, p=1, 16^3 cubes x 6 tets (24,576 tets)."""
+    m = csem_two_layer(16, 1, block=True)
+    m.name = "csem_p1_16cubed"
+    return m
+
+
+def config1(n=32):
+    """Mixed-precision CSEM, p=2, 32^3 cubes x 6 tets (196,608 tets); interior
+    nodes jittered by U(+-0.15h) (seed 0); per-element sigma log-uniform in
+    [0.01, 3.3] S/m (seed 1); HED at (0,0,50) 1 Hz; 10x10 receivers on z=0
+    spanning [-800, 800]^2."""
+    lo, hi = (-1000.0,) * 3, (1000.0,) * 3
+    nodes, tets = kuhn_box(n, lo, hi)
+    nodes = jitter_interior(nodes, n, 0.15, 0, lo, hi)
+    rng = np.random.default_rng(1)
+    s = 10.0 ** rng.uniform(np.log10(0.01), np.log10(3.3), size=len(tets))
+    sigma = np.stack([s, s], axis=1)
+    g = np.linspace(-800.0, 800.0, 10)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    rx = np.stack([X.ravel(), Y.ravel(), np.zeros(100)], axis=1)
+    return Model(f"csem_p2_{n}cubed_jitter", nodes, tets, sigma, 2, _hed(), rx)
+
+
+def config2_sources():
+    """64 x-directed HEDs at z = 50 m, x evenly spaced in [-1600, 1600]."""
+    return [_hed(x=float(x)) for x in np.linspace(-1600.0, 1600.0, 64)]
