@@ -1,0 +1,462 @@
+// CSR sparsity pattern and deterministic value assembly of
+//   A = sum_e P_e^T (K_e - i omega mu M_e) P_e      (petgem/solver.py:182-235)
+// plus PEC rows/columns (solver.py:552-577).
+//
+// Pattern.  petgem inserts every element's dense nd x nd block into a PETSc
+// AIJ matrix, so row r's columns are the union of the DOFs of the elements
+// containing r, sorted.  DOFs are numbered entity by entity (edges, faces,
+// volumes), so all rows of one entity share one column list, made of whole
+// DOF blocks of the entities adjacent to it.  The builder therefore works on
+// entity pairs: keys (a, b) for every pair of entities of every element
+// (nl^2 per element, nl = 6/10/11 entities with DOFs for p = 1/2/>=3) are
+// radix-sorted; each distinct key is one dense na x nb block of A, and the
+// sorted run of equal keys lists, in ascending element order, every element
+// contributing to that block.
+//
+// Values.  Each block is summed over its member elements in that fixed
+// order (no atomics): bitwise reproducible and independent of the launch
+// shape.  Two value paths exist: from materialised elemental matrices, and a
+// fused path that evaluates each contribution from the element's 12
+// geometry coefficients and its orientation tuple's moment tables, so the
+// elemental matrices are never written to memory.
+#include "pg_common.cuh"
+#include "pg_sort.cuh"
+
+namespace {
+
+#define GRID_STRIDE(i, n) \
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+struct Ent {
+  int64_t nE, nF, T;
+  int p, nl, de, df, dv;
+  __host__ __device__ Ent(int64_t nE_, int64_t nF_, int64_t T_, int p_) : nE(nE_), nF(nF_), T(T_), p(p_) {
+    de = p;
+    df = p * (p - 1);
+    dv = p * (p - 1) * (p - 2) / 2;
+    nl = p == 1 ? 6 : (p == 2 ? 10 : 11);
+  }
+  __host__ __device__ int64_t count() const { return nE + nF + T; }
+  // global entity id of local entity l of element e
+  __device__ int64_t ent(const int32_t* elemsE, const int32_t* elemsF, int64_t e, int l) const {
+    if (l < 6) return elemsE[6 * e + l];
+    if (l < 10) return nE + elemsF[4 * e + (l - 6)];
+    return nE + nF + e;
+  }
+  __host__ __device__ int nd_ent(int64_t a) const { return a < nE ? de : (a < nE + nF ? df : dv); }
+  __host__ __device__ int64_t first_dof(int64_t a) const {
+    if (a < nE) return a * de;
+    if (a < nE + nF) return nE * de + (a - nE) * df;
+    return nE * de + nF * df + (a - nE - nF) * dv;
+  }
+  // local DOF offset of local entity l inside the element's nd DOFs
+  __host__ __device__ int local_off(int l) const {
+    if (l < 6) return l * de;
+    if (l < 10) return 6 * de + (l - 6) * df;
+    return 6 * de + 4 * df;
+  }
+  __host__ __device__ int64_t ndofs() const { return nE * de + nF * df + T * dv; }
+  // entity of global DOF r
+  __device__ int64_t ent_of_dof(int64_t r) const {
+    if (r < nE * de) return r / de;
+    r -= nE * de;
+    if (r < nF * df) return nE + r / df;
+    r -= nF * df;
+    return nE + nF + r / dv;
+  }
+};
+
+__global__ void k_pair_keys(const int32_t* elemsE, const int32_t* elemsF, Ent E, uint64_t* keys, int32_t* vals) {
+  const int nl2 = E.nl * E.nl;
+  const uint64_t n_ent = (uint64_t)E.count();
+  GRID_STRIDE(i, E.T * nl2) {
+    const int64_t e = i / nl2;
+    const int r = (int)(i % nl2);
+    const int la = r / E.nl, lb = r % E.nl;
+    const uint64_t a = (uint64_t)E.ent(elemsE, elemsF, e, la);
+    const uint64_t b = (uint64_t)E.ent(elemsE, elemsF, e, lb);
+    keys[i] = a * n_ent + b;
+    vals[i] = (int32_t)i;
+  }
+}
+
+__global__ void k_flags(const uint64_t* keys, int64_t n, int32_t* flags) {
+  GRID_STRIDE(i, n) flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+// per sorted position: pair id; per pair: start, a, b, nb
+__global__ void k_pairs(const uint64_t* keys, const int32_t* excl, int64_t n, Ent E, int32_t* pair_start,
+                        int64_t* pair_a, int32_t* pair_nb) {
+  const uint64_t n_ent = (uint64_t)E.count();
+  GRID_STRIDE(i, n) {
+    if (i == 0 || keys[i] != keys[i - 1]) {
+      const int32_t g = excl[i];
+      pair_start[g] = (int32_t)i;
+      pair_a[g] = (int64_t)(keys[i] / n_ent);
+      pair_nb[g] = E.nd_ent((int64_t)(keys[i] % n_ent));
+    }
+  }
+}
+
+__global__ void k_pair_tail(const int32_t* n_pairs, int64_t M, int32_t* pair_start, int64_t* counts) {
+  pair_start[*n_pairs] = (int32_t)M;
+  counts[0] = *n_pairs;
+}
+
+// ent_first[a] = first pair of entity a
+__global__ void k_ent_first(const int64_t* pair_a, const int32_t* n_pairs, int32_t* ent_first) {
+  const int64_t np = *n_pairs;
+  GRID_STRIDE(g, np) {
+    if (g == 0 || pair_a[g] != pair_a[g - 1]) ent_first[pair_a[g]] = (int32_t)g;
+  }
+}
+
+// colstart[g] = X[g] - X[ent_first[a]];  row length of a = X[last]+nb[last]-X[first]
+__global__ void k_colstart(const int64_t* pair_a, const int32_t* X, const int32_t* pair_nb, const int32_t* ent_first,
+                           const int32_t* n_pairs, int32_t* colstart, int32_t* ent_len) {
+  const int64_t np = *n_pairs;
+  GRID_STRIDE(g, np) {
+    const int64_t a = pair_a[g];
+    const int32_t x0 = X[ent_first[a]];
+    colstart[g] = X[g] - x0;
+    if (g == np - 1 || pair_a[g + 1] != a) ent_len[a] = X[g] + pair_nb[g] - x0;
+  }
+}
+
+__global__ void k_rowlen(Ent E, const int32_t* ent_len, int64_t N, int64_t* rowptr) {
+  GRID_STRIDE(r, N) rowptr[r] = ent_len[E.ent_of_dof(r)];
+}
+
+__global__ void k_zero_i32(int32_t* a, int64_t n) { GRID_STRIDE(i, n) a[i] = 0; }
+
+// one warp per pair: fill the block's column indices
+__global__ void k_columns(const int32_t* members, const int32_t* pair_start, const int32_t* colstart, int64_t n_pairs,
+                          const int32_t* elemsE, const int32_t* elemsF, Ent E, const int64_t* rowptr, int32_t* col) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nl2 = E.nl * E.nl;
+  for (int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; g < n_pairs; g += warps) {
+    const int32_t m = members[pair_start[g]];
+    const int64_t e = m / nl2;
+    const int r = m % nl2;
+    const int64_t a = E.ent(elemsE, elemsF, e, r / E.nl), b = E.ent(elemsE, elemsF, e, r % E.nl);
+    const int na = E.nd_ent(a), nb = E.nd_ent(b);
+    const int64_t fa = E.first_dof(a), fb = E.first_dof(b);
+    const int cs = colstart[g];
+    for (int t = lane; t < na * nb; t += 32) {
+      const int i = t / nb, j = t % nb;
+      col[rowptr[fa + i] + cs + j] = (int32_t)(fb + j);
+    }
+  }
+}
+
+// values from materialised M, K: warp per pair, lanes over block entries
+__global__ void k_values_mk(const double* __restrict__ Mm, const double* __restrict__ Km,
+                            const int32_t* __restrict__ members, const int32_t* __restrict__ pair_start,
+                            const int32_t* __restrict__ colstart, int64_t n_pairs, const int32_t* elemsE,
+                            const int32_t* elemsF, Ent E, int nd, const int64_t* __restrict__ rowptr, double omu,
+                            double2* __restrict__ vals) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nl2 = E.nl * E.nl;
+  const int64_t nd2 = (int64_t)nd * nd;
+  for (int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; g < n_pairs; g += warps) {
+    const int32_t s0 = pair_start[g], s1 = pair_start[g + 1];
+    const int32_t m0 = members[s0];
+    const int64_t e0 = m0 / nl2;
+    const int r0 = m0 % nl2;
+    const int64_t a = E.ent(elemsE, elemsF, e0, r0 / E.nl), b = E.ent(elemsE, elemsF, e0, r0 % E.nl);
+    const int na = E.nd_ent(a), nb = E.nd_ent(b);
+    const int64_t fa = E.first_dof(a);
+    const int cs = colstart[g];
+    for (int t = lane; t < na * nb; t += 32) {
+      const int i = t / nb, j = t % nb;
+      double re = 0.0, im = 0.0;
+      for (int32_t s = s0; s < s1; ++s) {
+        const int32_t m = members[s];
+        const int64_t e = m / nl2;
+        const int r = m % nl2;
+        const int64_t off = e * nd2 + (int64_t)(E.local_off(r / E.nl) + i) * nd + E.local_off(r % E.nl) + j;
+        re += Km[off];
+        im += Mm[off];
+      }
+      vals[rowptr[fa + i] + cs + j] = make_double2(re, -omu * im);
+    }
+  }
+}
+
+// per-element coefficients for the fused path: [cK(6) | -omega mu det S (6)]
+__global__ void k_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t T, double omu,
+                               double* coef, int32_t* status) {
+  GRID_STRIDE(e, T) {
+    double x[4][3];
+    for (int v = 0; v < 4; ++v) {
+      const int64_t n = elemsN[4 * e + v];
+      x[v][0] = nodes[3 * n];
+      x[v][1] = nodes[3 * n + 1];
+      x[v][2] = nodes[3 * n + 2];
+    }
+    double J[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) J[r][c] = x[r + 1][c] - x[0][c];
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    double* cf = coef + 12 * e;
+    if (!(det != 0.0) || !isfinite(det)) {
+      *status = PG_ERR_DEGENERATE;
+      for (int t = 0; t < 12; ++t) cf[t] = 0.0;
+      continue;
+    }
+    const double id = 1.0 / det;
+    double inv[3][3];
+    inv[0][0] = c00 * id;
+    inv[1][0] = c01 * id;
+    inv[2][0] = c02 * id;
+    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    const double D[3] = {sigma[2 * e], sigma[2 * e], sigma[2 * e + 1]};
+    const int pa[6] = {0, 1, 2, 0, 0, 1};
+    const int pb[6] = {0, 1, 2, 1, 2, 2};
+    for (int t = 0; t < 6; ++t) {
+      double s = 0.0, g = 0.0;
+      for (int c = 0; c < 3; ++c) {
+        s += inv[c][pa[t]] * D[c] * inv[c][pb[t]];
+        g += J[pa[t]][c] * J[pb[t]][c];
+      }
+      cf[t] = g * id;
+      cf[6 + t] = -omu * (det * s);
+    }
+  }
+}
+
+__device__ __forceinline__ int packed_index(int j, int k, int nd) {
+  if (k < j) { int t = j; j = k; k = t; }
+  return j * nd - (j * (j - 1)) / 2 + (k - j);
+}
+
+// fused values: warp per pair; each member contributes 12 FMAs per entry
+__global__ void k_values_fused(const double* __restrict__ coef, const int32_t* __restrict__ tuple_of_elem,
+                               const double* __restrict__ tables, const int32_t* __restrict__ members,
+                               const int32_t* __restrict__ pair_start, const int32_t* __restrict__ colstart,
+                               int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, Ent E, int nd,
+                               const int64_t* __restrict__ rowptr, double2* __restrict__ vals) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nl2 = E.nl * E.nl;
+  const int64_t NT = (int64_t)nd * (nd + 1) / 2;
+  for (int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; g < n_pairs; g += warps) {
+    const int32_t s0 = pair_start[g], s1 = pair_start[g + 1];
+    const int32_t m0 = members[s0];
+    const int64_t e0 = m0 / nl2;
+    const int r0 = m0 % nl2;
+    const int64_t a = E.ent(elemsE, elemsF, e0, r0 / E.nl), b = E.ent(elemsE, elemsF, e0, r0 % E.nl);
+    const int na = E.nd_ent(a), nb = E.nd_ent(b);
+    const int64_t fa = E.first_dof(a);
+    const int cs = colstart[g];
+    for (int t = lane; t < na * nb; t += 32) {
+      const int i = t / nb, j = t % nb;
+      double re = 0.0, im = 0.0;
+      for (int32_t s = s0; s < s1; ++s) {
+        const int32_t m = members[s];
+        const int64_t e = m / nl2;
+        const int r = m % nl2;
+        const int jl = E.local_off(r / E.nl) + i, kl = E.local_off(r % E.nl) + j;
+        const double* tb = tables + (int64_t)tuple_of_elem[e] * 12 * NT + packed_index(jl, kl, nd);
+        const double* cf = coef + 12 * e;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          re = fma(cf[q], __ldg(tb + (6 + q) * NT), re);
+          im = fma(cf[6 + q], __ldg(tb + q * NT), im);
+        }
+      }
+      vals[rowptr[fa + i] + cs + j] = make_double2(re, im);
+    }
+  }
+}
+
+__global__ void k_mark_bnd(const int32_t* bnd, int64_t nb, uint8_t* flag, double2* b) {
+  GRID_STRIDE(i, nb) {
+    flag[bnd[i]] = 1;
+    if (b) b[bnd[i]] = make_double2(0.0, 0.0);
+  }
+}
+
+// zeroRowsColumns(rows, diag=1): warp per row
+__global__ void k_pec(const int64_t* rowptr, const int32_t* col, double2* vals, int64_t N, const uint8_t* flag) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < N; r += warps) {
+    const bool rb = flag[r] != 0;
+    for (int64_t k = rowptr[r] + lane; k < rowptr[r + 1]; k += 32) {
+      const int32_t c = col[k];
+      if (rb) vals[k] = make_double2(c == r ? 1.0 : 0.0, 0.0);
+      else if (flag[c]) vals[k] = make_double2(0.0, 0.0);
+    }
+  }
+}
+
+unsigned warp_grid(int64_t items) {
+  int64_t blocks = (items + 7) / 8;  // 8 warps per 256-thread block
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks < 1) blocks = 1;
+  return (unsigned)blocks;
+}
+
+}  // namespace
+
+extern "C" int pg_pattern_local_entities(int p) { return p == 1 ? 6 : (p == 2 ? 10 : 11); }
+
+extern "C" size_t pg_pattern_workspace_bytes(int64_t n_elems, int64_t nE, int64_t nF, int p) {
+  const int nl = pg_pattern_local_entities(p);
+  const int64_t M = n_elems * nl * nl;
+  const int64_t n_ent = nE + nF + n_elems;
+  return pg_align256(sizeof(uint64_t) * M) + pg_align256(sizeof(int32_t) * M) /*excl*/ +
+         pg_align256(sizeof(int64_t) * M) /*pair_a*/ + pg_align256(sizeof(int32_t) * M) * 2 /*nb, X*/ +
+         pg_align256(sizeof(int32_t) * n_ent) * 2 + pg::sort_workspace_bytes(M) + pg::scan_workspace_bytes(M) +
+         4096;
+}
+
+extern "C" int pg_pattern_build(const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE,
+                                int64_t nF, int p, int32_t* members, int32_t* pair_start, int32_t* pair_colstart,
+                                int64_t* rowptr, int64_t* counts, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+  if (p < 1 || p > 6) {
+    pg_set_error("pg_pattern_build: order must be 1..6");
+    return PG_ERR_UNSUPPORTED;
+  }
+  Ent E(nE, nF, n_elems, p);
+  const int64_t M = n_elems * E.nl * E.nl;
+  const int64_t N = E.ndofs();
+  if (n_elems < 1 || nE < 1 || nF < 1 || !elemsE || !elemsF || !members || !pair_start || !pair_colstart || !rowptr ||
+      !counts || M >= (1ll << 31) || N >= (1ll << 31)) {
+    pg_set_error("pg_pattern_build: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (!workspace || workspace_bytes < pg_pattern_workspace_bytes(n_elems, nE, nF, p)) {
+    pg_set_error("pg_pattern_build: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  cudaStream_t s = pg_stream(stream);
+  PgArena ar(workspace, workspace_bytes);
+  uint64_t* keys = ar.take<uint64_t>(M);
+  int32_t* excl = ar.take<int32_t>(M);
+  int64_t* pair_a = ar.take<int64_t>(M);
+  int32_t* pair_nb = ar.take<int32_t>(M);
+  int32_t* X = ar.take<int32_t>(M);
+  const int64_t n_ent = E.count();
+  int32_t* ent_first = ar.take<int32_t>(n_ent);
+  int32_t* ent_len = ar.take<int32_t>(n_ent);
+  const size_t sort_b = pg::sort_workspace_bytes(M);
+  void* sort_ws = ar.take<char>(sort_b);
+  const size_t scan_b = pg::scan_workspace_bytes(M);
+  void* scan_ws = ar.take<char>(scan_b);
+  int32_t* tot = ar.take<int32_t>(8);
+  if (!keys || !excl || !pair_a || !pair_nb || !X || !ent_first || !ent_len || !sort_ws || !scan_ws || !tot)
+    return PG_ERR_WORKSPACE;
+  const unsigned gM = pg_blocks(M, 256);
+  int st;
+  k_pair_keys<<<gM, 256, 0, s>>>(elemsE, elemsF, E, keys, members);
+  st = pg::sort_pairs(keys, members, M, pg::bits_for((uint64_t)n_ent * (uint64_t)n_ent - 1), sort_ws, sort_b, s);
+  if (st) { pg_set_error("pg_pattern_build: sort failed"); return st; }
+  k_flags<<<gM, 256, 0, s>>>(keys, M, excl);
+  st = pg::scan_exclusive_i32(excl, excl, M, tot, scan_ws, scan_b, s);
+  if (st) return st;
+  k_pairs<<<gM, 256, 0, s>>>(keys, excl, M, E, pair_start, pair_a, pair_nb);
+  k_pair_tail<<<1, 1, 0, s>>>(tot, M, pair_start, counts);
+  // X = exclusive scan of nb over pairs (length n_pairs <= M; the tail beyond n_pairs is unused)
+  // n_pairs is only known on the device: scan over the M-capacity prefix with zero padding.
+  k_zero_i32<<<gM, 256, 0, s>>>(X, M);
+  // copy nb into X's input (X reused as output of the scan)
+  st = pg::scan_exclusive_i32(pair_nb, X, M, nullptr, scan_ws, scan_b, s);
+  if (st) return st;
+  k_ent_first<<<gM, 256, 0, s>>>(pair_a, tot, ent_first);
+  k_zero_i32<<<pg_blocks(n_ent, 256), 256, 0, s>>>(ent_len, n_ent);
+  k_colstart<<<gM, 256, 0, s>>>(pair_a, X, pair_nb, ent_first, tot, pair_colstart, ent_len);
+  k_rowlen<<<pg_blocks(N, 256), 256, 0, s>>>(E, ent_len, N, rowptr);
+  st = pg::scan_exclusive_i64(rowptr, rowptr, N + 1, counts + 1, scan_ws, scan_b, s);
+  if (st) return st;
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_pattern_columns(const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
+                                  int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems,
+                                  int64_t nE, int64_t nF, int p, const int64_t* rowptr, int32_t* col, void* stream) {
+  if (p < 1 || p > 6 || n_pairs < 1 || !members || !pair_start || !pair_colstart || !rowptr || !col) {
+    pg_set_error("pg_pattern_columns: bad argument");
+    return PG_ERR_ARG;
+  }
+  Ent E(nE, nF, n_elems, p);
+  k_columns<<<warp_grid(n_pairs), 256, 0, pg_stream(stream)>>>(members, pair_start, pair_colstart, n_pairs, elemsE,
+                                                               elemsF, E, rowptr, col);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_assemble_values(const double* M, const double* K, const int32_t* members, const int32_t* pair_start,
+                                  const int32_t* pair_colstart, int64_t n_pairs, const int32_t* elemsE,
+                                  const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p,
+                                  const int64_t* rowptr, double omega_mu, double* vals, void* stream) {
+  if (p < 1 || p > 6 || n_pairs < 1 || !M || !K || !members || !pair_start || !pair_colstart || !rowptr || !vals) {
+    pg_set_error("pg_assemble_values: bad argument");
+    return PG_ERR_ARG;
+  }
+  Ent E(nE, nF, n_elems, p);
+  k_values_mk<<<warp_grid(n_pairs), 256, 0, pg_stream(stream)>>>(M, K, members, pair_start, pair_colstart, n_pairs,
+                                                                 elemsE, elemsF, E, pg_nd_elem(p), rowptr, omega_mu,
+                                                                 reinterpret_cast<double2*>(vals));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_element_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma,
+                                       int64_t n_elems, double omega_mu, double* coef, int32_t* status,
+                                       void* stream) {
+  if (n_elems < 1 || !nodes || !elemsN || !sigma || !coef || !status) {
+    pg_set_error("pg_element_coefficients: bad argument");
+    return PG_ERR_ARG;
+  }
+  k_coefficients<<<pg_blocks(n_elems, 256), 256, 0, pg_stream(stream)>>>(nodes, elemsN, sigma, n_elems, omega_mu,
+                                                                        coef, status);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_assemble_fused(const double* coef, const int32_t* tuple_of_elem, const double* tables,
+                                 const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
+                                 int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems,
+                                 int64_t nE, int64_t nF, int p, const int64_t* rowptr, double* vals, void* stream) {
+  if (p < 1 || p > 6 || n_pairs < 1 || !coef || !tuple_of_elem || !tables || !members || !pair_start ||
+      !pair_colstart || !rowptr || !vals) {
+    pg_set_error("pg_assemble_fused: bad argument");
+    return PG_ERR_ARG;
+  }
+  Ent E(nE, nF, n_elems, p);
+  k_values_fused<<<warp_grid(n_pairs), 256, 0, pg_stream(stream)>>>(coef, tuple_of_elem, tables, members, pair_start,
+                                                                    pair_colstart, n_pairs, elemsE, elemsF, E,
+                                                                    pg_nd_elem(p), rowptr,
+                                                                    reinterpret_cast<double2*>(vals));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_apply_pec(const int64_t* rowptr, const int32_t* col, double* vals, int64_t n_dofs,
+                            const int32_t* bnd, int64_t n_bnd, double* b, uint8_t* flag_ws, void* stream) {
+  if (n_dofs < 1 || !rowptr || !col || !vals || !flag_ws || (n_bnd > 0 && !bnd)) {
+    pg_set_error("pg_apply_pec: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  PG_CUDA_TRY(cudaMemsetAsync(flag_ws, 0, (size_t)n_dofs, s));
+  if (n_bnd > 0)
+    k_mark_bnd<<<pg_blocks(n_bnd, 256), 256, 0, s>>>(bnd, n_bnd, flag_ws, reinterpret_cast<double2*>(b));
+  k_pec<<<warp_grid(n_dofs), 256, 0, s>>>(rowptr, col, reinterpret_cast<double2*>(vals), n_dofs, flag_ws);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

@@ -1,0 +1,32 @@
+// Device primitives shared by the topology and pattern builders: a stable
+// LSD radix sort of (uint64 key, int32 value) pairs and exclusive scans.
+// Both are deterministic (no floating point, no order-dependent atomics).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pg {
+
+// Workspace bytes for sort_pairs on n items (ping-pong buffers included).
+size_t sort_workspace_bytes(int64_t n);
+
+// Stable sort of keys[0..n) (uint64) carrying vals (int32); sorts the low
+// `key_bits` bits.  Results end in keys/vals (in place).  n < 2^31.
+int sort_pairs(uint64_t* keys, int32_t* vals, int64_t n, int key_bits, void* ws, size_t ws_bytes,
+               cudaStream_t s);
+
+// Exclusive scans (out may alias in).  `total` (device, may be null)
+// receives the sum.  Workspace: scan_workspace_bytes(n).
+size_t scan_workspace_bytes(int64_t n);
+int scan_exclusive_i32(const int32_t* in, int32_t* out, int64_t n, int32_t* total, void* ws, size_t ws_bytes,
+                       cudaStream_t s);
+int scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* total, void* ws, size_t ws_bytes,
+                       cudaStream_t s);
+
+inline int bits_for(uint64_t maxval) {
+  int b = 0;
+  while (b < 64 && (maxval >> b) != 0) ++b;
+  return b < 1 ? 1 : b;
+}
+
+}  // namespace pg
