@@ -87,6 +87,169 @@ int pg_elemental_matrices(const double* nodes, const int32_t* elemsN, const doub
                           const int32_t* tuple_of_elem, const double* tables, int64_t n_elems,
                           int p, double* M, double* K, int32_t* status, void* stream);
 
+
+/* ------------------------------------------------------------------------
+ * Mesh topology, DOF numbering, orientation, PEC boundary (bit-exact)
+ * --------------------------------------------------------------------- */
+
+/* Workspace for pg_topology. */
+size_t pg_topology_workspace_bytes(int64_t n_elems);
+
+/* Edges and faces of a tetrahedral mesh, numbered exactly as petgem:
+ * replaces petgem/mesh.py:18 computeEdges, mesh.py:56 computeFaces and
+ * mesh.py:92 computeFacesEdges (with vectors.py:15 deleteDuplicateRows and
+ * vectors.py:81 invConnectivity).
+ * In: elemsN int32 [T*4] (0-based node ids < n_nodes <= 2^21).
+ * Out: elemsE [T*6]; elemsF [T*4]; edgesNodes [cap 6T * 2] (sorted pair);
+ * facesN [cap 4T * 3] (vertex order of the first occurrence); facesE
+ * [cap 4T * 3]; face_nelem [cap 4T] (elements sharing each face: 1 on the
+ * boundary); counts int64 [2] = (nEdges, nFaces); status int32 [1] set to
+ * PG_ERR_ARG if a node id is out of range (caller zeroes it). */
+int pg_topology(const int32_t* elemsN, int64_t n_elems, int64_t n_nodes, int32_t* elemsE, int32_t* elemsF,
+                int32_t* edgesNodes, int32_t* facesN, int32_t* facesE, int32_t* face_nelem, int64_t* counts,
+                int32_t* status, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Element-to-DOF map: replaces petgem/hvfem.py:15 computeConnectivityDOFS
+ * (its dof_edges/dof_faces/dof_volume are the closed forms p*e+j,
+ * nE*p + f*p(p-1) + j, nE*p + nF*p(p-1) + e*p(p-1)(p-2)/2 + j).
+ * Out: dofs int32 [T * p(p+2)(p+3)/2]. */
+int pg_connectivity_dofs(const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF,
+                         int p, int32_t* dofs, void* stream);
+
+/* Edge flags and face codes of every element: replaces
+ * petgem/hvfem.py:122 computeElementOrientation.  Out: eo int8 [T*6],
+ * fo int8 [T*4]. */
+int pg_element_orientation(const int32_t* elemsN, const int32_t* elemsE, const int32_t* edgesNodes,
+                           const int32_t* elemsF, const int32_t* facesE, int64_t n_elems, int8_t* eo, int8_t* fo,
+                           void* stream);
+
+/* Workspace for pg_boundary_dofs. */
+size_t pg_boundary_workspace_bytes(int64_t nE, int64_t nF);
+
+/* PEC (Dirichlet) DOF list in petgem's order: edge DOFs of boundary edges
+ * (ascending edge id) then face DOFs of boundary faces (ascending face id).
+ * Replaces petgem/mesh.py:149 computeBoundaryFaces, mesh.py:224
+ * computeBoundaryEdges, mesh.py:280 computeBoundaries.
+ * Out: bnd int32 [cap nE*p + nF*p(p-1)], n_bnd int64 [1]. */
+int pg_boundary_dofs(const int32_t* face_nelem, const int32_t* facesE, int64_t nE, int64_t nF, int p, int32_t* bnd,
+                     int64_t* n_bnd, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * CSR pattern and value assembly (replaces petgem/parallel.py:150
+ * createParallelMatrix + the Mat.setValues(ADD_VALUES)/assemblyBegin/End
+ * loop of petgem/solver.py:182-235)
+ * --------------------------------------------------------------------- */
+
+/* Entities with DOFs per element: 6 (p=1), 10 (p=2), 11 (p>=3). */
+int pg_pattern_local_entities(int p);
+
+size_t pg_pattern_workspace_bytes(int64_t n_elems, int64_t nE, int64_t nF, int p);
+
+/* Phase 1.  With nl = pg_pattern_local_entities(p), M = T*nl*nl:
+ * Out: members int32 [M] (element-entity pair codes e*nl*nl + la*nl + lb,
+ * grouped by global entity pair, ascending element inside a group);
+ * pair_start int32 [cap M+1]; pair_colstart int32 [cap M]; rowptr int64
+ * [N+1] with N = nE*p + nF*p(p-1) + T*p(p-1)(p-2)/2; counts int64 [2] =
+ * (n_pairs, nnz).  Columns of every row are sorted ascending, as PETSc AIJ. */
+int pg_pattern_build(const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p,
+                     int32_t* members, int32_t* pair_start, int32_t* pair_colstart, int64_t* rowptr,
+                     int64_t* counts, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Phase 2: column indices col int32 [nnz]. */
+int pg_pattern_columns(const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
+                       int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE,
+                       int64_t nF, int p, const int64_t* rowptr, int32_t* col, void* stream);
+
+/* vals complex128 [nnz] = sum_e (K_e - i omega_mu M_e) from materialised
+ * elemental matrices (pg_elemental_matrices), summed per entry in ascending
+ * element order (deterministic). */
+int pg_assemble_values(const double* M, const double* K, const int32_t* members, const int32_t* pair_start,
+                       const int32_t* pair_colstart, int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF,
+                       int64_t n_elems, int64_t nE, int64_t nF, int p, const int64_t* rowptr, double omega_mu,
+                       double* vals, void* stream);
+
+/* Per-element geometry coefficients for the fused path: coef f64 [T*12] =
+ * (J J^T / det, -omega_mu * det * invJ^T diag(sh,sh,sv) invJ), 6 symmetric
+ * entries each.  status int32 [1] <- PG_ERR_DEGENERATE on det(J) == 0. */
+int pg_element_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t n_elems,
+                            double omega_mu, double* coef, int32_t* status, void* stream);
+
+/* Fused elemental + assembly: vals complex128 [nnz] without materialising
+ * elemental matrices (12 FMAs per contribution from coef and tables). */
+int pg_assemble_fused(const double* coef, const int32_t* tuple_of_elem, const double* tables, const int32_t* members,
+                      const int32_t* pair_start, const int32_t* pair_colstart, int64_t n_pairs,
+                      const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p,
+                      const int64_t* rowptr, double* vals, void* stream);
+
+/* PETSc MatZeroRowsColumns(rows, diag=1) and b[rows] = 0
+ * (petgem/solver.py:552-577).  b may be NULL.  flag_ws uint8 [n_dofs]. */
+int pg_apply_pec(const int64_t* rowptr, const int32_t* col, double* vals, int64_t n_dofs, const int32_t* bnd,
+                 int64_t n_bnd, double* b, uint8_t* flag_ws, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Points: location, point-dipole source, receiver interpolation
+ * --------------------------------------------------------------------- */
+
+/* First (lowest-index) element containing each point within barycentric
+ * tolerance tol, -1 if none: the brute-force find_simplex(tol=1e-12) rule of
+ * petgem/preprocessing.py:414-425 and postprocessing.py:532-539.
+ * pts f64 [R*3]; elem_out int32 [R]. */
+int pg_locate_points(const double* nodes, const int32_t* elemsN, int64_t n_elems, const double* pts, int64_t n_pts,
+                     double tol, int32_t* elem_out, void* stream);
+
+/* b[dofs_e] += (scale_re + i scale_im) * (field . N_e(position)) for the
+ * element *elem (device int32): the total-field point dipole of
+ * petgem/solver.py:247-316 (scale = i omega mu).  position_host and
+ * field_host are HOST double[3].  status <- PG_ERR_NOT_FOUND if *elem < 0. */
+int pg_source_rhs(const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo, const int32_t* dofs,
+                  int p, const int32_t* elem, const double* position_host, const double* field_host,
+                  double scale_re, double scale_im, double* b, int32_t* status, void* stream);
+
+/* Receiver fields (petgem/postprocessing.py:479 fieldInterpolator):
+ * fields complex128 [R*6] = (Ex,Ey,Ez,Hx,Hy,Hz), H = curl E / (i omega_mu);
+ * NaN for receivers with elem < 0. */
+int pg_gather_fields(const double* x, const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo,
+                     const int32_t* dofs, int p, const double* pts, const int32_t* elem, int64_t n_pts,
+                     double omega_mu, double* fields, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Krylov (replaces the PETSc KSP of petgem/solver.py:584-594)
+ * --------------------------------------------------------------------- */
+
+/* y = A x, CSR with int64 row pointers; nrhs in {1,2,4,8,16,32}, vectors
+ * stored row-major with the RHS index fastest. */
+int pg_spmv_z(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n_rows, const double* x,
+              double* y, int nrhs, void* stream);
+int pg_spmv_c(const int64_t* rowptr, const int32_t* col, const float* vals, int64_t n_rows, const float* x, float* y,
+              int nrhs, void* stream);
+
+typedef struct pg_gmres_opts {
+  int restart;    /* GMRES(m), 1..64 (PETSc default 30) */
+  int max_it;     /* cap on Arnoldi steps */
+  double rtol;    /* stop when ||b - A x|| <= rtol ||b|| (true residual, FP64) */
+  int precision;  /* 0: complex128 Arnoldi; 1: complex64 Arnoldi + complex128 refinement */
+  int reorth;     /* 1: classical Gram-Schmidt applied twice (CGS2) */
+} pg_gmres_opts;
+
+typedef struct pg_gmres_result {
+  int64_t iterations; /* Arnoldi steps (max over RHS) */
+  int64_t restarts;   /* cycles (= FP64 refinement steps in mixed precision) */
+  double relres;      /* max over RHS of the final true relative residual */
+  int status;
+} pg_gmres_result;
+
+void pg_gmres_default_opts(pg_gmres_opts* opts);
+size_t pg_gmres_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_gmres_opts* opts);
+
+/* Right-Jacobi-preconditioned restarted GMRES on A x = b with nrhs RHS
+ * (b, x: complex128 [n*nrhs]; x holds the initial guess).  Synchronises the
+ * stream once per restart.  result and relres_per_rhs are HOST pointers
+ * (may be NULL).  Returns PG_OK, PG_ERR_NOT_CONVERGED (x holds the last
+ * iterate), or an error. */
+int pg_gmres(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz, const double* b,
+             double* x, int nrhs, const pg_gmres_opts* opts, pg_gmres_result* result, double* relres_per_rhs,
+             void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

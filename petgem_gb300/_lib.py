@@ -15,6 +15,22 @@ _INT = ctypes.c_int
 _SZ = ctypes.c_size_t
 _D = ctypes.c_double
 
+
+class GmresOpts(ctypes.Structure):
+    """pg_gmres_opts (include/petgem_gb300.h)."""
+    _fields_ = [("restart", ctypes.c_int), ("max_it", ctypes.c_int), ("rtol", ctypes.c_double),
+                ("precision", ctypes.c_int), ("reorth", ctypes.c_int)]
+
+
+class GmresResult(ctypes.Structure):
+    """pg_gmres_result (include/petgem_gb300.h)."""
+    _fields_ = [("iterations", ctypes.c_int64), ("restarts", ctypes.c_int64), ("relres", ctypes.c_double),
+                ("status", ctypes.c_int)]
+
+
+_PO = ctypes.POINTER(GmresOpts)
+_PR = ctypes.POINTER(GmresResult)
+
 # name -> (restype, argtypes); mirrors include/petgem_gb300.h
 SIGNATURES = {
     "pg_abi_version": (_INT, []),
@@ -24,6 +40,28 @@ SIGNATURES = {
     "pg_orientation_tuples": (_INT, [_P, _P, _I64, _P, _P, _P, _P, _SZ, _P]),
     "pg_tuple_tables": (_INT, [_P, _I64, _INT, _P, _P]),
     "pg_elemental_matrices": (_INT, [_P, _P, _P, _P, _P, _I64, _INT, _P, _P, _P, _P]),
+    "pg_topology_workspace_bytes": (_SZ, [_I64]),
+    "pg_topology": (_INT, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "pg_connectivity_dofs": (_INT, [_P, _P, _I64, _I64, _I64, _INT, _P, _P]),
+    "pg_element_orientation": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _P]),
+    "pg_boundary_workspace_bytes": (_SZ, [_I64, _I64]),
+    "pg_boundary_dofs": (_INT, [_P, _P, _I64, _I64, _INT, _P, _P, _P, _SZ, _P]),
+    "pg_pattern_local_entities": (_INT, [_INT]),
+    "pg_pattern_workspace_bytes": (_SZ, [_I64, _I64, _I64, _INT]),
+    "pg_pattern_build": (_INT, [_P, _P, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "pg_pattern_columns": (_INT, [_P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P]),
+    "pg_assemble_values": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _D, _P, _P]),
+    "pg_element_coefficients": (_INT, [_P, _P, _P, _I64, _D, _P, _P, _P]),
+    "pg_assemble_fused": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P]),
+    "pg_apply_pec": (_INT, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P]),
+    "pg_locate_points": (_INT, [_P, _P, _I64, _P, _I64, _D, _P, _P]),
+    "pg_source_rhs": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _P, _D, _D, _P, _P, _P]),
+    "pg_gather_fields": (_INT, [_P, _P, _P, _P, _P, _P, _INT, _P, _P, _I64, _D, _P, _P]),
+    "pg_spmv_z": (_INT, [_P, _P, _P, _I64, _P, _P, _INT, _P]),
+    "pg_spmv_c": (_INT, [_P, _P, _P, _I64, _P, _P, _INT, _P]),
+    "pg_gmres_default_opts": (None, [_PO]),
+    "pg_gmres_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PO]),
+    "pg_gmres": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PO, _PR, _P, _P, _SZ, _P]),
 }
 
 STATUS = {

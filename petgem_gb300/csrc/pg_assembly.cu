@@ -123,8 +123,9 @@ __global__ void k_colstart(const int64_t* pair_a, const int32_t* X, const int32_
   }
 }
 
+// row lengths into rowptr[0..N) and 0 into rowptr[N], ready for the exclusive scan
 __global__ void k_rowlen(Ent E, const int32_t* ent_len, int64_t N, int64_t* rowptr) {
-  GRID_STRIDE(r, N) rowptr[r] = ent_len[E.ent_of_dof(r)];
+  GRID_STRIDE(r, N + 1) rowptr[r] = r < N ? ent_len[E.ent_of_dof(r)] : 0;
 }
 
 __global__ void k_zero_i32(int32_t* a, int64_t n) { GRID_STRIDE(i, n) a[i] = 0; }
@@ -378,7 +379,7 @@ extern "C" int pg_pattern_build(const int32_t* elemsE, const int32_t* elemsF, in
   k_ent_first<<<gM, 256, 0, s>>>(pair_a, tot, ent_first);
   k_zero_i32<<<pg_blocks(n_ent, 256), 256, 0, s>>>(ent_len, n_ent);
   k_colstart<<<gM, 256, 0, s>>>(pair_a, X, pair_nb, ent_first, tot, pair_colstart, ent_len);
-  k_rowlen<<<pg_blocks(N, 256), 256, 0, s>>>(E, ent_len, N, rowptr);
+  k_rowlen<<<pg_blocks(N + 1, 256), 256, 0, s>>>(E, ent_len, N, rowptr);
   st = pg::scan_exclusive_i64(rowptr, rowptr, N + 1, counts + 1, scan_ws, scan_b, s);
   if (st) return st;
   PG_LAUNCH_CHECK();

@@ -1,0 +1,732 @@
+// Restarted GMRES for petgem's complex system A x = b (petgem/solver.py:584-594,
+// PETSc KSP with -ksp_type gmres -pc_type jacobi), for one or several
+// right-hand sides at once.
+//
+// Structure (same code for both precisions, templated on the Arnoldi scalar):
+//   loop over restarts:
+//     r = b - A x                    complex128 CSR SpMV/SpMM with the original A
+//     stop when ||r|| <= rtol ||b|| for every RHS (true residual, FP64)
+//     one Arnoldi cycle of m steps on  Ahat = A D^-1  (right Jacobi), in the
+//     Arnoldi precision: complex128 ("fp64") or complex64 ("mixed")
+//     x += D^-1 V y                  FP64 update
+// In the mixed form every restart is an FP64 iterative-refinement step around
+// a complex64 GMRES(m) cycle; in the plain form both parts are complex128.
+//
+// Orthogonalisation is classical Gram-Schmidt (PETSc's default), optionally
+// repeated once (CGS2).  Basis vectors are stored unnormalised with a scale
+// alpha_i = 1/||v~_i|| that is folded into the small Hessenberg scalars, so
+// no kernel rewrites a vector only to normalise it.  All reductions are
+// two-stage with a fixed order: results are bitwise reproducible.  Within a
+// cycle the host does not synchronise: a one-block kernel applies the Givens
+// rotations, tracks the residual estimate and switches the remaining launches
+// of the cycle off once every RHS is below its target.
+//
+// Vectors with k right-hand sides are stored row-major, RHS fastest:
+// v[row * k + rhs].  k must be 1, 2, 4, 8, 16 or 32.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "pg_common.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxM = 64;    // restart length limit
+constexpr int kMaxK = 32;    // RHS per block limit
+
+// ---------------------------------------------------------------- complex helpers
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // c + a*b
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float2 cconjfma(float2 a, float2 b, float2 c) {  // c + conj(a)*b
+  return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double2 cconjfma(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+template <typename C> struct Real;
+template <> struct Real<float2> { typedef float T; };
+template <> struct Real<double2> { typedef double T; };
+template <typename C> __device__ __forceinline__ C czero();
+template <> __device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+template <typename C> __device__ __forceinline__ C cfrom(double2 v);
+template <> __device__ __forceinline__ float2 cfrom<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+template <> __device__ __forceinline__ double2 cfrom<double2>(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_d(double2 v) { return v; }
+__device__ __forceinline__ double2 dadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 dsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 dscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ double dabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double2 dconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 ddiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+template <typename T> __device__ __forceinline__ T shfl_xor(T v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float2 shfl_xor(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ __forceinline__ double2 shfl_xor(double2 v, int m) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// ---------------------------------------------------------------- per-RHS cycle state
+struct RhsState {
+  double2 H[kMaxM * (kMaxM + 1)];  // column j: H[j*(m+1) + i]
+  double2 g[kMaxM + 1];
+  double2 sn[kMaxM];
+  double cs[kMaxM];
+  double alpha[kMaxM + 1];         // 1 / ||v~_i||
+  double2 y[kMaxM];
+  double target;                   // absolute residual target for this RHS
+  double res_est;                  // current Arnoldi residual estimate
+  double rnorm;                    // ||r|| at cycle start
+  int active;                      // still iterating in this cycle
+  int kdone;                       // Arnoldi steps completed in this cycle
+  int breakdown;
+  int pad;
+};
+
+struct Ctl {
+  int any_active;  // some RHS still iterating in this cycle
+  int nonfinite;
+};
+
+// ---------------------------------------------------------------- SpMV / SpMM
+// y = A x for k = 1, G lanes per row.  Optionally y = b - A x (resid).
+template <typename C, int G>
+__global__ void __launch_bounds__(kThreads) k_spmv1(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                    const C* __restrict__ val, int64_t n, const C* __restrict__ x,
+                                                    C* __restrict__ y, const C* __restrict__ bsub, const Ctl* ctl) {
+  if (ctl && !ctl->any_active) return;
+  // The row loop is warp-uniform (all 32 lanes run the same trip count) so
+  // the full-mask shuffles below are always executed by the whole warp.
+  const int lane = threadIdx.x % G;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  for (int64_t rw = warp_base; rw < n; rw += groups) {
+    const int64_t r = rw + (gid - warp_base);
+    const bool valid = r < n;
+    C acc = czero<C>();
+    if (valid) {
+      const int64_t e = rowptr[r + 1];
+      for (int64_t q = rowptr[r] + lane; q < e; q += G) acc = cfma(val[q], x[col[q]], acc);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) acc = cadd(acc, shfl_xor(acc, off));
+    if (valid && lane == 0) {
+      if (bsub) {
+        C bb = bsub[r];
+        acc.x = bb.x - acc.x;
+        acc.y = bb.y - acc.y;
+      }
+      y[r] = acc;
+    }
+  }
+}
+
+// k > 1: thread (row, rhs); rows of a block stride by kThreads / K
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_spmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                   const C* __restrict__ val, int64_t n, const C* __restrict__ x,
+                                                   C* __restrict__ y, const C* __restrict__ bsub, const Ctl* ctl) {
+  if (ctl && !ctl->any_active) return;
+  const int rhs = threadIdx.x % K;
+  const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / K;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; r < n; r += rows_per_pass) {
+    C acc = czero<C>();
+    const int64_t e = rowptr[r + 1];
+    for (int64_t q = rowptr[r]; q < e; ++q) acc = cfma(val[q], x[(int64_t)col[q] * K + rhs], acc);
+    if (bsub) {
+      C bb = bsub[r * K + rhs];
+      acc.x = bb.x - acc.x;
+      acc.y = bb.y - acc.y;
+    }
+    y[r * K + rhs] = acc;
+  }
+}
+
+// ---------------------------------------------------------------- reductions
+// Block-reduce per-thread values that all belong to rhs = tid % K; writes
+// out[rhs] for this block (double2).  Fixed order => deterministic.
+template <int K>
+__device__ void block_reduce_rhs(double2 v, double2* smem, double2* out) {
+  // warp stage: lanes with equal (lane % K) combine
+#pragma unroll
+  for (int off = 16; off >= K; off >>= 1) v = dadd(v, shfl_xor(v, off));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K) smem[warp * K + lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int w = 0; w < kThreads / 32; ++w) s = dadd(s, smem[w * K + threadIdx.x]);
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// partial[b][i][rhs] = sum over this block's rows of conj(v~_i) . w~   for i <= j
+// Basis vectors are processed 8 at a time (accumulators stay in registers).
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_dots(const C* __restrict__ V, int64_t stride, const C* __restrict__ w,
+                                                   int64_t n, int j, double2* partial, const Ctl* ctl) {
+  if (!ctl->any_active) return;
+  constexpr int GB = 8;
+  __shared__ double2 smem[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double2* out = partial + (int64_t)blockIdx.x * (kMaxM + 1) * K;
+  for (int i0 = 0; i0 <= j; i0 += GB) {
+    C acc[GB];
+#pragma unroll
+    for (int t = 0; t < GB; ++t) acc[t] = czero<C>();
+    for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+      const C we = w[e];
+#pragma unroll
+      for (int t = 0; t < GB; ++t)
+        if (i0 + t <= j) acc[t] = cconjfma(V[(int64_t)(i0 + t) * stride + e], we, acc[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < GB; ++t)
+      if (i0 + t <= j) block_reduce_rhs<K>(to_d(acc[t]), smem, out + (i0 + t) * K);
+  }
+}
+
+// sums of |w|^2 per rhs for this block
+template <typename C, int K>
+__device__ void norm_partial(double2 v, double2* smem, double2* out) {
+  block_reduce_rhs<K>(v, smem, out);
+}
+
+// h_ij = alpha_i * alpha_j * sum_b partial ; coef[i][rhs] = h_ij * alpha_i (as C)
+// `accumulate` adds into the existing column (second CGS pass, alpha_j := 1).
+template <typename C, int K>
+__global__ void k_dots_final(const double2* partial, int nblocks, int j, int m, RhsState* st, C* coef, int second,
+                             const Ctl* ctl) {
+  if (!ctl->any_active) return;
+  for (int t = threadIdx.x; t < (j + 1) * K; t += blockDim.x) {  // t = i * K + rhs
+    const int i = t / K, rhs = t % K;
+    RhsState& S = st[rhs];
+    double2 s = make_double2(0.0, 0.0);
+    for (int b = 0; b < nblocks; ++b) s = dadd(s, partial[((int64_t)b * (kMaxM + 1) + i) * K + rhs]);
+    const double aj = second ? 1.0 : S.alpha[j];
+    const double2 h = dscale(S.alpha[i] * aj, s);
+    if (S.active) {
+      if (second) S.H[j * (m + 1) + i] = dadd(S.H[j * (m + 1) + i], h);
+      else S.H[j * (m + 1) + i] = h;
+    }
+    coef[i * K + rhs] = cfrom<C>(dscale(S.alpha[i], h));
+  }
+}
+
+// w~ <- a_j w~ - sum_i coef_i v~_i ; partial norms of the result
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_update(const C* __restrict__ V, int64_t stride, C* __restrict__ w,
+                                                     int64_t n, int j, const C* __restrict__ coef,
+                                                     const RhsState* st, int second, double2* partial,
+                                                     const Ctl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[(kThreads / 32) * kMaxK];
+  __shared__ C cf[kMaxM * kMaxK];
+  __shared__ typename Real<C>::T aj[kMaxK];
+  for (int t = threadIdx.x; t < (j + 1) * K; t += kThreads) cf[t] = coef[t];
+  if (threadIdx.x < K) aj[threadIdx.x] = second ? 1 : (typename Real<C>::T)st[threadIdx.x].alpha[j];
+  __syncthreads();
+  const int rhs = threadIdx.x % K;
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double nrm = 0.0;
+  typename Real<C>::T nrm_f = 0;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    C v = w[e];
+    v.x *= aj[rhs];
+    v.y *= aj[rhs];
+#pragma unroll
+    for (int i = 0; i < kMaxM; ++i)
+      if (i <= j) {
+        const C c = cf[i * K + rhs];
+        const C b = V[(int64_t)i * stride + e];
+        v.x -= c.x * b.x - c.y * b.y;
+        v.y -= c.x * b.y + c.y * b.x;
+      }
+    w[e] = v;
+    nrm_f += v.x * v.x + v.y * v.y;
+  }
+  nrm = (double)nrm_f;
+  block_reduce_rhs<K>(make_double2(nrm, 0.0), smem, partial + (int64_t)blockIdx.x * K);
+}
+
+// Finish step j: h_{j+1,j} = ||w||, Givens, residual estimate, activity.
+template <int K>
+__global__ void k_givens(const double2* partial, int nblocks, int j, int m, RhsState* st, Ctl* ctl, int last) {
+  if (!ctl->any_active) return;
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  const int rhs = threadIdx.x;
+  if (rhs < K) {
+    RhsState& S = st[rhs];
+    if (S.active) {
+      double ss = 0.0;
+      for (int b = 0; b < nblocks; ++b) ss += partial[(int64_t)b * K + rhs].x;
+      const double hn = sqrt(ss);
+      double2* Hc = S.H + j * (m + 1);
+      Hc[j + 1] = make_double2(hn, 0.0);
+      if (!isfinite(hn)) ctl->nonfinite = 1;
+      S.alpha[j + 1] = hn > 0.0 ? 1.0 / hn : 0.0;
+      // apply previous rotations to column j
+      for (int i = 0; i < j; ++i) {
+        const double2 a = Hc[i], b = Hc[i + 1];
+        const double c = S.cs[i];
+        const double2 s = S.sn[i];
+        Hc[i] = dadd(dscale(c, a), cmul(s, b));
+        Hc[i + 1] = dsub(dscale(c, b), cmul(dconj(s), a));
+      }
+      // new rotation zeroing H[j+1][j]
+      const double2 a = Hc[j], b = Hc[j + 1];
+      const double na = sqrt(dabs2(a)), nb = sqrt(dabs2(b));
+      double c;
+      double2 s;
+      if (nb == 0.0) {
+        c = 1.0;
+        s = make_double2(0.0, 0.0);
+      } else if (na == 0.0) {
+        c = 0.0;
+        s = make_double2(1.0, 0.0);
+      } else {
+        const double r = sqrt(na * na + nb * nb);
+        c = na / r;
+        const double2 ph = dscale(1.0 / na, a);  // a/|a|
+        s = dscale(1.0 / r, cmul(ph, dconj(b)));
+      }
+      S.cs[j] = c;
+      S.sn[j] = s;
+      Hc[j] = dadd(dscale(c, a), cmul(s, b));
+      Hc[j + 1] = make_double2(0.0, 0.0);
+      const double2 gj = S.g[j];
+      S.g[j] = dscale(c, gj);
+      S.g[j + 1] = dscale(-1.0, cmul(dconj(s), gj));
+      S.res_est = sqrt(dabs2(S.g[j + 1]));
+      S.kdone = j + 1;
+      const bool lucky = !(hn > 1e-300 * (S.rnorm > 0 ? S.rnorm : 1.0));
+      if (lucky) S.breakdown = 1;
+      if (S.res_est <= S.target || lucky || last || !isfinite(S.res_est)) S.active = 0;
+    }
+    if (S.active) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ctl->any_active = any;
+}
+
+// y = H^-1 g (upper triangular, kdone x kdone); coef_i = y_i alpha_i
+template <int K>
+__global__ void k_backsolve(RhsState* st, int m, double2* ycoef) {
+  const int rhs = threadIdx.x;
+  if (rhs >= K) return;
+  RhsState& S = st[rhs];
+  const int k = S.kdone;
+  for (int i = k - 1; i >= 0; --i) {
+    double2 s = S.g[i];
+    for (int l = i + 1; l < k; ++l) s = dsub(s, cmul(S.H[l * (m + 1) + i], S.y[l]));
+    const double2 d = S.H[i * (m + 1) + i];
+    S.y[i] = (d.x == 0.0 && d.y == 0.0) ? make_double2(0.0, 0.0) : ddiv(s, d);
+  }
+  for (int i = 0; i < kMaxM; ++i) ycoef[i * K + rhs] = i < k ? dscale(S.alpha[i], S.y[i]) : make_double2(0.0, 0.0);
+}
+
+// x += D^-1 sum_i ycoef_i v~_i   (FP64 accumulation)
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_update_x(const C* __restrict__ V, int64_t stride, int kmax, int64_t n,
+                                                       const double2* __restrict__ ycoef, const double2* __restrict__ dinv,
+                                                       double2* __restrict__ x) {
+  __shared__ double2 yc[kMaxM * kMaxK];
+  for (int t = threadIdx.x; t < kmax * K; t += kThreads) yc[t] = ycoef[t];
+  __syncthreads();
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads) {
+    const int rhs = (int)(e % K);
+    double2 s = make_double2(0.0, 0.0);
+    for (int i = 0; i < kmax; ++i) {
+      const double2 c = yc[i * K + rhs];
+      if (c.x != 0.0 || c.y != 0.0) s = cfma(c, to_d(V[(int64_t)i * stride + e]), s);
+    }
+    x[e] = dadd(x[e], cmul(dinv[e / K], s));
+  }
+}
+
+// v~_0 = r / ||r|| (cast to C); per-RHS norms partials first
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_norm2(const double2* __restrict__ r, int64_t n, double2* partial) {
+  __shared__ double2 smem[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double s = 0.0;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) s += dabs2(r[e]);
+  block_reduce_rhs<K>(make_double2(s, 0.0), smem, partial + (int64_t)blockIdx.x * K);
+}
+
+template <int K>
+__global__ void k_norm_final(const double2* partial, int nblocks, double* out) {
+  const int rhs = threadIdx.x;
+  if (rhs >= K) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += partial[(int64_t)b * K + rhs].x;
+  out[rhs] = sqrt(s);
+}
+
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_start(const double2* __restrict__ r, int64_t n, const double* rnorm,
+                                                    C* __restrict__ v0) {
+  __shared__ double inv[kMaxK];
+  if (threadIdx.x < K) inv[threadIdx.x] = rnorm[threadIdx.x] > 0 ? 1.0 / rnorm[threadIdx.x] : 0.0;
+  __syncthreads();
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    v0[e] = cfrom<C>(dscale(inv[e % K], r[e]));
+}
+
+template <int K>
+__global__ void k_cycle_init(RhsState* st, const double* rnorm, const double* target, const int* want, Ctl* ctl) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  const int rhs = threadIdx.x;
+  if (rhs < K) {
+    RhsState& S = st[rhs];
+    S.rnorm = rnorm[rhs];
+    S.target = target[rhs];
+    S.alpha[0] = 1.0;
+    S.g[0] = make_double2(rnorm[rhs], 0.0);
+    S.res_est = rnorm[rhs];
+    S.kdone = 0;
+    S.breakdown = 0;
+    S.active = want[rhs] && rnorm[rhs] > 0.0;
+    if (S.active) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any;
+    ctl->nonfinite = 0;
+  }
+}
+
+// Ahat = A D^-1 in the Arnoldi precision; dinv = 1 / diag(A)
+__global__ void k_diag_inv(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n, double2* dinv,
+                           int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 d = make_double2(0.0, 0.0);
+    for (int64_t q = rowptr[r]; q < rowptr[r + 1]; ++q)
+      if (col[q] == r) d = val[q];
+    if (d.x == 0.0 && d.y == 0.0) {
+      *status = PG_ERR_BREAKDOWN;
+      dinv[r] = make_double2(1.0, 0.0);
+    } else {
+      dinv[r] = ddiv(make_double2(1.0, 0.0), d);
+    }
+  }
+}
+
+template <typename C>
+__global__ void k_scale_cols(const int32_t* col, const double2* val, int64_t nnz, const double2* dinv, C* out) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+    out[q] = cfrom<C>(cmul(val[q], dinv[col[q]]));
+}
+
+// ---------------------------------------------------------------- host driver
+struct Plan {
+  int64_t n, nnz;
+  int k, m;
+  int prec;           // 0 fp64 Arnoldi, 1 fp32 Arnoldi
+  int nb;             // reduction blocks
+  size_t csize;       // sizeof Arnoldi complex
+};
+
+size_t ws_layout(const Plan& P, size_t* off /* 14 */) {
+  size_t o = 0;
+  auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
+  put(0, P.nnz * P.csize);                                   // Ahat
+  put(1, sizeof(double2) * P.n);                             // dinv
+  put(2, P.csize * (size_t)(P.m + 1) * P.n * P.k);           // V
+  put(3, sizeof(double2) * P.n * P.k);                       // r
+  put(4, sizeof(double2) * (size_t)P.nb * (kMaxM + 1) * P.k);  // dot partials
+  put(5, sizeof(double2) * (size_t)P.nb * P.k);              // norm partials
+  put(6, sizeof(RhsState) * P.k);                            // state
+  put(7, sizeof(Ctl));                                       // ctl
+  put(8, P.csize * kMaxM * P.k);                             // coef
+  put(9, sizeof(double2) * kMaxM * P.k);                     // ycoef
+  put(10, sizeof(double) * P.k);                             // rnorm
+  put(11, sizeof(double) * P.k);                             // target
+  put(12, sizeof(int) * P.k);                                // want
+  put(13, sizeof(int));                                      // status
+  return o;
+}
+
+int pick_blocks(int64_t n, int k) {
+  int64_t nb = (n * k + 4095) / 4096;
+  if (nb > 152 * 4) nb = 152 * 4;
+  if (nb < 1) nb = 1;
+  return (int)nb;
+}
+
+template <typename C>
+void launch_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const C* val, const C* x, C* y,
+                 const C* bsub, const Ctl* ctl, int64_t nnz_per_row, cudaStream_t s) {
+  const unsigned grid = 152 * 16;
+  switch (P.k) {
+    case 1:
+      if (nnz_per_row > 48) k_spmv1<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl);
+      else if (nnz_per_row > 20) k_spmv1<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl);
+      else k_spmv1<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl);
+      break;
+    case 2: k_spmm<C, 2><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+    case 4: k_spmm<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+    case 8: k_spmm<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+    case 16: k_spmm<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+    case 32: k_spmm<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+  }
+}
+
+#define PG_KSWITCH(KVAR, CALL)              \
+  switch (KVAR) {                           \
+    case 1: { constexpr int K = 1; CALL; } break;   \
+    case 2: { constexpr int K = 2; CALL; } break;   \
+    case 4: { constexpr int K = 4; CALL; } break;   \
+    case 8: { constexpr int K = 8; CALL; } break;   \
+    case 16: { constexpr int K = 16; CALL; } break; \
+    case 32: { constexpr int K = 32; CALL; } break; \
+  }
+
+template <typename C>
+int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
+              const pg_gmres_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
+  size_t off[14];
+  ws_layout(P, off);
+  C* Ahat = reinterpret_cast<C*>(ws + off[0]);
+  double2* dinv = reinterpret_cast<double2*>(ws + off[1]);
+  C* V = reinterpret_cast<C*>(ws + off[2]);
+  double2* r = reinterpret_cast<double2*>(ws + off[3]);
+  double2* dpart = reinterpret_cast<double2*>(ws + off[4]);
+  double2* npart = reinterpret_cast<double2*>(ws + off[5]);
+  RhsState* st = reinterpret_cast<RhsState*>(ws + off[6]);
+  Ctl* ctl = reinterpret_cast<Ctl*>(ws + off[7]);
+  C* coef = reinterpret_cast<C*>(ws + off[8]);
+  double2* ycoef = reinterpret_cast<double2*>(ws + off[9]);
+  double* rnorm = reinterpret_cast<double*>(ws + off[10]);
+  double* target = reinterpret_cast<double*>(ws + off[11]);
+  int* want = reinterpret_cast<int*>(ws + off[12]);
+  int* dstatus = reinterpret_cast<int*>(ws + off[13]);
+  const int k = P.k, m = P.m, nb = P.nb;
+  const int64_t stride = P.n * k;
+  const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
+
+  PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  k_diag_inv<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, dinv, dstatus);
+  k_scale_cols<C><<<pg_blocks(P.nnz, 256), 256, 0, s>>>(col, A, P.nnz, dinv, Ahat);
+  PG_LAUNCH_CHECK();
+
+  // ||b|| per RHS
+  std::vector<double> bnorm(k), rn(k), tgt(k);
+  std::vector<int> wnt(k);
+  PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, npart), k_norm_final<K><<<1, 32, 0, s>>>(npart, nb, rnorm)));
+  PG_LAUNCH_CHECK();
+  PG_CUDA_TRY(cudaMemcpyAsync(bnorm.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  int hstatus = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hstatus) {
+    pg_set_error("pg_gmres: zero diagonal entry (Jacobi preconditioner undefined)");
+    return PG_ERR_BREAKDOWN;
+  }
+  for (int i = 0; i < k; ++i) {
+    if (!isfinite(bnorm[i])) {
+      pg_set_error("pg_gmres: non-finite right-hand side");
+      return PG_ERR_NONFINITE;
+    }
+  }
+  int64_t its = 0, restarts = 0;
+  int status = PG_OK;
+  // PG_KSP_MONITOR=1 prints the true residual at every restart (like PETSc -ksp_monitor_true_residual)
+  const char* mon_env = getenv("PG_KSP_MONITOR");
+  const bool monitor = mon_env && mon_env[0] && mon_env[0] != '0';
+  if (monitor)
+    for (int i = 0; i < k; ++i) fprintf(stderr, "pg_gmres: rhs %d ||b|| = %.6e\n", i, bnorm[i]);
+  const int64_t max_it = o->max_it > 0 ? o->max_it : 10000;
+  for (;;) {
+    // r = b - A x (FP64), ||r||
+    launch_spmv<double2>(P, rowptr, col, A, x, r, b, nullptr, npr, s);
+    PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r, P.n, npart), k_norm_final<K><<<1, 32, 0, s>>>(npart, nb, rnorm)));
+    PG_LAUNCH_CHECK();
+    PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    bool all = true;
+    if (monitor)
+      for (int i = 0; i < k; ++i)
+        fprintf(stderr, "pg_gmres: restart %lld its %lld rhs %d true ||r||/||b|| = %.6e\n", (long long)restarts,
+                (long long)its, i, bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0);
+    for (int i = 0; i < k; ++i) {
+      if (!isfinite(rn[i])) {
+        pg_set_error("pg_gmres: non-finite residual");
+        status = PG_ERR_NONFINITE;
+      }
+      const double tb = o->rtol * bnorm[i];
+      const bool ok = rn[i] <= tb || bnorm[i] == 0.0;
+      wnt[i] = ok ? 0 : 1;
+      // inner target: aim slightly below the outer target (estimate vs true residual)
+      tgt[i] = tb * 0.5;
+      if (!ok) all = false;
+    }
+    if (status) break;
+    if (all) break;
+    if (its >= max_it) {
+      status = PG_ERR_NOT_CONVERGED;
+      break;
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    PG_KSWITCH(k, (k_start<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(r, P.n, rnorm, V),
+                   k_cycle_init<K><<<1, 32, 0, s>>>(st, rnorm, target, want, ctl)));
+    int steps = (int)((max_it - its) < m ? (max_it - its) : m);
+    for (int j = 0; j < steps; ++j) {
+      C* vj = V + (int64_t)j * stride;
+      C* w = V + (int64_t)(j + 1) * stride;
+      launch_spmv<C>(P, rowptr, col, Ahat, vj, w, nullptr, ctl, npr, s);
+      const int passes = o->reorth ? 2 : 1;
+      for (int pass = 0; pass < passes; ++pass) {
+        PG_KSWITCH(k, (k_dots<C, K><<<nb, kThreads, 0, s>>>(V, stride, w, P.n, j, dpart, ctl),
+                       k_dots_final<C, K><<<1, 1024, 0, s>>>(dpart, nb, j, m, st, coef, pass, ctl),
+                       k_update<C, K><<<nb, kThreads, 0, s>>>(V, stride, w, P.n, j, coef, st, pass, npart, ctl)));
+      }
+      PG_KSWITCH(k, (k_givens<K><<<1, 32, 0, s>>>(npart, nb, j, m, st, ctl, j == steps - 1)));
+    }
+    PG_LAUNCH_CHECK();
+    PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
+                   k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n, ycoef,
+                                                                                      dinv, x)));
+    // iterations actually used this cycle (max over RHS)
+    std::vector<int> hs(k);
+    for (int i = 0; i < k; ++i)
+      PG_CUDA_TRY(cudaMemcpyAsync(&hs[i], &st[i].kdone, sizeof(int), cudaMemcpyDeviceToHost, s));
+    Ctl hctl;
+    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    int used = 0;
+    for (int i = 0; i < k; ++i) used = hs[i] > used ? hs[i] : used;
+    its += used > 0 ? used : 1;
+    ++restarts;
+    if (hctl.nonfinite) {
+      pg_set_error("pg_gmres: non-finite Arnoldi norm");
+      status = PG_ERR_NONFINITE;
+      break;
+    }
+  }
+  double worst = 0.0;
+  for (int i = 0; i < k; ++i) {
+    const double rr = bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0;
+    if (relres_out) relres_out[i] = rr;
+    worst = rr > worst ? rr : worst;
+  }
+  if (res) {
+    res->iterations = its;
+    res->restarts = restarts;
+    res->relres = worst;
+    res->status = status;
+  }
+  if (status == PG_ERR_NOT_CONVERGED) pg_set_error("pg_gmres: max_it reached before rtol");
+  return status;
+}
+
+bool valid_k(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32; }
+
+}  // namespace
+
+extern "C" void pg_gmres_default_opts(pg_gmres_opts* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->restart = 30;
+  o->max_it = 10000;
+  o->rtol = 1e-8;
+  o->precision = 0;
+  o->reorth = 0;
+}
+
+extern "C" size_t pg_gmres_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_gmres_opts* opts) {
+  if (!opts || n < 1 || !valid_k(nrhs)) return 0;
+  Plan P{n, nnz, nrhs, opts->restart, opts->precision, pick_blocks(n, nrhs),
+         opts->precision ? sizeof(float2) : sizeof(double2)};
+  size_t off[14];
+  return ws_layout(P, off) + 256;
+}
+
+extern "C" int pg_gmres(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
+                        const double* b, double* x, int nrhs, const pg_gmres_opts* opts, pg_gmres_result* result,
+                        double* relres_per_rhs, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!opts || !rowptr || !col || !vals || !b || !x || n < 1 || nnz < n || !valid_k(nrhs)) {
+    pg_set_error("pg_gmres: bad argument (nrhs must be 1, 2, 4, 8, 16 or 32)");
+    return PG_ERR_ARG;
+  }
+  if (opts->restart < 1 || opts->restart > kMaxM || !(opts->rtol > 0.0) ||
+      (opts->precision != 0 && opts->precision != 1)) {
+    pg_set_error("pg_gmres: restart must be 1..64, rtol > 0, precision 0 or 1");
+    return PG_ERR_ARG;
+  }
+  const size_t need = pg_gmres_workspace_bytes(n, nnz, nrhs, opts);
+  if (!workspace || workspace_bytes < need) {
+    pg_set_error("pg_gmres: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  char* ws = reinterpret_cast<char*>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+  Plan P{n, nnz, nrhs, opts->restart, opts->precision, pick_blocks(n, nrhs),
+         opts->precision ? sizeof(float2) : sizeof(double2)};
+  cudaStream_t s = pg_stream(stream);
+  const double2* A = reinterpret_cast<const double2*>(vals);
+  const double2* bb = reinterpret_cast<const double2*>(b);
+  double2* xx = reinterpret_cast<double2*>(x);
+  if (P.prec == 0) return run_gmres<double2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
+  return run_gmres<float2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
+}
+
+extern "C" int pg_spmv_z(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n_rows, const double* x,
+                         double* y, int nrhs, void* stream) {
+  if (!rowptr || !col || !vals || !x || !y || n_rows < 1 || !valid_k(nrhs)) {
+    pg_set_error("pg_spmv_z: bad argument");
+    return PG_ERR_ARG;
+  }
+  Plan P{n_rows, 0, nrhs, 1, 0, 1, sizeof(double2)};
+  launch_spmv<double2>(P, rowptr, col, reinterpret_cast<const double2*>(vals), reinterpret_cast<const double2*>(x),
+                       reinterpret_cast<double2*>(y), nullptr, nullptr, 43, pg_stream(stream));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_spmv_c(const int64_t* rowptr, const int32_t* col, const float* vals, int64_t n_rows, const float* x,
+                         float* y, int nrhs, void* stream) {
+  if (!rowptr || !col || !vals || !x || !y || n_rows < 1 || !valid_k(nrhs)) {
+    pg_set_error("pg_spmv_c: bad argument");
+    return PG_ERR_ARG;
+  }
+  Plan P{n_rows, 0, nrhs, 1, 1, 1, sizeof(float2)};
+  launch_spmv<float2>(P, rowptr, col, reinterpret_cast<const float2*>(vals), reinterpret_cast<const float2*>(x),
+                      reinterpret_cast<float2*>(y), nullptr, nullptr, 43, pg_stream(stream));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

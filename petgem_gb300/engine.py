@@ -1,0 +1,296 @@
+"""Device-resident forward-modelling engine (one GPU).
+
+``DeviceMesh`` holds a tetrahedral mesh on the GPU together with everything
+derived from it once per mesh (topology, DOF numbering, orientation tuples and
+their moment tables, the CSR pattern and the PEC DOF list).  Per model
+(conductivity, frequency, source) it assembles A and b, solves, and
+interpolates the receivers.  Every computation runs in libpetgem_gb300.so;
+torch only provides device memory and the current stream.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+
+MU0 = 4.0 * math.pi * 1e-7     # petgem/solver.py:174
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+
+def _s():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ws(nbytes, dev):
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=dev)
+
+
+def ndof_elem(p):
+    return p * (p + 2) * (p + 3) // 2
+
+
+def source_field(src):
+    """Dipole moment vector after azimuth/dip rotation (petgem/hvfem.py:2303-2344,
+    solver.py:255-266): rot(azimuth) rot(dip) (I L e_x)."""
+    a = math.radians(src["azimuth"])
+    b = math.radians(src["dip"])
+    IL = float(src["current"]) * float(src["length"])
+    # M1 (x-y) @ M2 (x-z) @ e_x
+    v = np.array([math.cos(a) * math.cos(b), math.sin(a) * math.cos(b), math.sin(b)])
+    return v * IL
+
+
+class SolveInfo:
+    def __init__(self, iterations, restarts, relres, status, relres_per_rhs, seconds=None):
+        self.iterations = iterations
+        self.restarts = restarts
+        self.relres = relres
+        self.status = status
+        self.relres_per_rhs = relres_per_rhs
+        self.seconds = seconds
+
+    def __repr__(self):
+        return (f"SolveInfo(iterations={self.iterations}, restarts={self.restarts}, relres={self.relres:.3e}, "
+                f"status={self.status})")
+
+
+class DeviceMesh:
+    """Mesh, topology, DOF map, orientation tables and CSR pattern on one GPU."""
+
+    def __init__(self, nodes, elemsN, p, device="cuda:0", pattern=True):
+        if not 1 <= p <= 6:
+            raise ValueError("basis order must be 1..6 (petgem/common.py:210-216)")
+        self.device = torch.device(device)
+        self.p = int(p)
+        dev = self.device
+        self.nodes = torch.as_tensor(np.ascontiguousarray(nodes, dtype=np.float64), device=dev).contiguous()
+        self.elemsN = torch.as_tensor(np.ascontiguousarray(elemsN), device=dev).to(torch.int32).contiguous()
+        self.T = int(self.elemsN.shape[0])
+        self.n_nodes = int(self.nodes.shape[0])
+        self._topology()
+        self._dofs_orientation()
+        self._tables()
+        self._boundary()
+        self.rowptr = self.col = None
+        if pattern:
+            self._pattern()
+
+    # ---------------------------------------------------------------- per-mesh setup
+    def _topology(self):
+        dev, T = self.device, self.T
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.elemsE = torch.empty((T, 6), **i32)
+        self.elemsF = torch.empty((T, 4), **i32)
+        edgesNodes = torch.empty((6 * T, 2), **i32)
+        facesN = torch.empty((4 * T, 3), **i32)
+        facesE = torch.empty((4 * T, 3), **i32)
+        face_nelem = torch.empty(4 * T, **i32)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        status = torch.zeros(1, **i32)
+        ws = _ws(_lib.query("pg_topology_workspace_bytes", T), dev)
+        _lib.call("pg_topology", _p(self.elemsN), T, self.n_nodes, _p(self.elemsE), _p(self.elemsF), _p(edgesNodes),
+                  _p(facesN), _p(facesE), _p(face_nelem), _p(counts), _p(status), _p(ws), ws.numel(), _s())
+        c = counts.cpu().tolist()
+        if int(status.item()) != 0:
+            raise _lib.PetgemError("pg_topology", int(status.item()), "node index out of range in elemsN")
+        self.nE, self.nF = int(c[0]), int(c[1])
+        self.edgesNodes = edgesNodes[:self.nE].contiguous()
+        self.facesN = facesN[:self.nF].contiguous()
+        self.facesE = facesE[:self.nF].contiguous()
+        self.face_nelem = face_nelem[:self.nF].contiguous()
+
+    def _dofs_orientation(self):
+        dev, T, p = self.device, self.T, self.p
+        self.nd = ndof_elem(p)
+        self.dofs = torch.empty((T, self.nd), dtype=torch.int32, device=dev)
+        _lib.call("pg_connectivity_dofs", _p(self.elemsE), _p(self.elemsF), T, self.nE, self.nF, p, _p(self.dofs), _s())
+        self.N = self.nE * p + self.nF * p * (p - 1) + T * (p * (p - 1) * (p - 2) // 2)
+        self.eo = torch.empty((T, 6), dtype=torch.int8, device=dev)
+        self.fo = torch.empty((T, 4), dtype=torch.int8, device=dev)
+        _lib.call("pg_element_orientation", _p(self.elemsN), _p(self.elemsE), _p(self.edgesNodes), _p(self.elemsF),
+                  _p(self.facesE), T, _p(self.eo), _p(self.fo), _s())
+
+    def _tables(self):
+        dev, T = self.device, self.T
+        self.tuple_of_elem = torch.empty(T, dtype=torch.int32, device=dev)
+        codes = torch.empty(min(T, 64 * 1296), dtype=torch.int32, device=dev)
+        n = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = _ws(_lib.query("pg_tuples_workspace_bytes", T), dev)
+        _lib.call("pg_orientation_tuples", _p(self.eo), _p(self.fo), T, _p(self.tuple_of_elem), _p(codes), _p(n),
+                  _p(ws), ws.numel(), _s())
+        U = int(n.item())
+        self.codes = codes[:U].contiguous()
+        per = _lib.query("pg_table_doubles", self.p)
+        self.tables = torch.empty(U * per, dtype=torch.float64, device=dev)
+        _lib.call("pg_tuple_tables", _p(self.codes), U, self.p, _p(self.tables), _s())
+        self.n_tuples = U
+
+    def _boundary(self):
+        dev, p = self.device, self.p
+        cap = self.nE * p + self.nF * p * (p - 1)
+        bnd = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+        nb = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = _ws(_lib.query("pg_boundary_workspace_bytes", self.nE, self.nF), dev)
+        _lib.call("pg_boundary_dofs", _p(self.face_nelem), _p(self.facesE), self.nE, self.nF, p, _p(bnd), _p(nb),
+                  _p(ws), ws.numel(), _s())
+        self.bnd = bnd[:int(nb.item())].contiguous()
+        self.pec_flags = torch.empty(self.N, dtype=torch.uint8, device=dev)
+
+    def _pattern(self):
+        dev, T, p = self.device, self.T, self.p
+        nl = _lib.query("pg_pattern_local_entities", p)
+        M = T * nl * nl
+        self.members = torch.empty(M, dtype=torch.int32, device=dev)
+        pair_start = torch.empty(M + 1, dtype=torch.int32, device=dev)
+        pair_colstart = torch.empty(M, dtype=torch.int32, device=dev)
+        self.rowptr = torch.empty(self.N + 1, dtype=torch.int64, device=dev)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        ws = _ws(_lib.query("pg_pattern_workspace_bytes", T, self.nE, self.nF, p), dev)
+        _lib.call("pg_pattern_build", _p(self.elemsE), _p(self.elemsF), T, self.nE, self.nF, p, _p(self.members),
+                  _p(pair_start), _p(pair_colstart), _p(self.rowptr), _p(counts), _p(ws), ws.numel(), _s())
+        del ws
+        c = counts.cpu().tolist()
+        self.n_pairs, self.nnz = int(c[0]), int(c[1])
+        self.pair_start = pair_start[:self.n_pairs + 1].contiguous()
+        self.pair_colstart = pair_colstart[:self.n_pairs].contiguous()
+        del pair_start, pair_colstart
+        self.col = torch.empty(self.nnz, dtype=torch.int32, device=dev)
+        _lib.call("pg_pattern_columns", _p(self.members), _p(self.pair_start), _p(self.pair_colstart), self.n_pairs,
+                  _p(self.elemsE), _p(self.elemsF), T, self.nE, self.nF, p, _p(self.rowptr), _p(self.col), _s())
+
+    # ---------------------------------------------------------------- per-model work
+    def sigma_tensor(self, sigma):
+        s = torch.as_tensor(np.ascontiguousarray(sigma, dtype=np.float64), device=self.device)
+        if s.ndim == 1:
+            s = torch.stack([s, s], dim=1)
+        return s.contiguous()
+
+    def elemental_matrices(self, sigma):
+        """Batched elemental (M, K) f64 [T, nd, nd] (petgem/hvfem.py:223)."""
+        s = self.sigma_tensor(sigma) if not torch.is_tensor(sigma) else sigma
+        M = torch.empty((self.T, self.nd, self.nd), dtype=torch.float64, device=self.device)
+        K = torch.empty_like(M)
+        st = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _lib.call("pg_elemental_matrices", _p(self.nodes), _p(self.elemsN), _p(s), _p(self.tuple_of_elem),
+                  _p(self.tables), self.T, self.p, _p(M), _p(K), _p(st), _s())
+        if int(st.item()) != 0:
+            raise _lib.PetgemError("pg_elemental_matrices", int(st.item()), "degenerate element")
+        return M, K
+
+    def element_coefficients(self, sigma, frequency, out=None, check=True):
+        s = self.sigma_tensor(sigma) if not torch.is_tensor(sigma) else sigma
+        omu = 2.0 * math.pi * float(frequency) * MU0
+        coef = out if out is not None else torch.empty((self.T, 12), dtype=torch.float64, device=self.device)
+        st = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _lib.call("pg_element_coefficients", _p(self.nodes), _p(self.elemsN), _p(s), self.T, omu, _p(coef), _p(st),
+                  _s())
+        if check and int(st.item()) != 0:
+            raise _lib.PetgemError("pg_element_coefficients", int(st.item()), "degenerate element")
+        return coef
+
+    def assemble(self, sigma, frequency, fused=True, out=None, coef=None):
+        """A values (complex128 [nnz]) before PEC: sum_e K_e - i omega mu M_e."""
+        if self.col is None:
+            self._pattern()
+        vals = out if out is not None else torch.empty(self.nnz, dtype=torch.complex128, device=self.device)
+        if fused:
+            if coef is None:
+                coef = self.element_coefficients(sigma, frequency)
+            _lib.call("pg_assemble_fused", _p(coef), _p(self.tuple_of_elem), _p(self.tables), _p(self.members),
+                      _p(self.pair_start), _p(self.pair_colstart), self.n_pairs, _p(self.elemsE), _p(self.elemsF),
+                      self.T, self.nE, self.nF, self.p, _p(self.rowptr), _p(vals), _s())
+        else:
+            M, K = self.elemental_matrices(sigma)
+            omu = 2.0 * math.pi * float(frequency) * MU0
+            _lib.call("pg_assemble_values", _p(M), _p(K), _p(self.members), _p(self.pair_start),
+                      _p(self.pair_colstart), self.n_pairs, _p(self.elemsE), _p(self.elemsF), self.T, self.nE, self.nF,
+                      self.p, _p(self.rowptr), omu, _p(vals), _s())
+        return vals
+
+    def locate(self, pts, tol=1e-12):
+        pts_t = torch.as_tensor(np.ascontiguousarray(np.atleast_2d(pts), dtype=np.float64), device=self.device)
+        out = torch.empty(pts_t.shape[0], dtype=torch.int32, device=self.device)
+        _lib.call("pg_locate_points", _p(self.nodes), _p(self.elemsN), self.T, _p(pts_t), pts_t.shape[0], tol,
+                  _p(out), _s())
+        return pts_t, out
+
+    def locate_source(self, src):
+        """Element containing the source point (petgem/preprocessing.py:414-425), device int32 [1]."""
+        _, elem = self.locate(np.asarray(src["position"], dtype=np.float64))
+        return elem
+
+    def source_rhs(self, src, elem, b, status=None):
+        """b += i omega mu (field . N_e(position)) on the device (no host sync)."""
+        pos = np.asarray(src["position"], dtype=np.float64)
+        field = source_field(src)
+        omu = 2.0 * math.pi * float(src["frequency"]) * MU0
+        st = status if status is not None else torch.zeros(1, dtype=torch.int32, device=self.device)
+        pos_c = (ctypes.c_double * 3)(*pos.tolist())
+        fld_c = (ctypes.c_double * 3)(*field.tolist())
+        _lib.call("pg_source_rhs", _p(self.nodes), _p(self.elemsN), _p(self.eo), _p(self.fo), _p(self.dofs), self.p,
+                  _p(elem), ctypes.cast(pos_c, ctypes.c_void_p), ctypes.cast(fld_c, ctypes.c_void_p), 0.0, omu,
+                  _p(b), _p(st), _s())
+        return st
+
+    def source_vector(self, src, b=None):
+        """Point-dipole RHS (petgem/solver.py:247-316); returns (b, source element)."""
+        if b is None:
+            b = torch.zeros(self.N, dtype=torch.complex128, device=self.device)
+        elem = self.locate_source(src)
+        st = self.source_rhs(src, elem, b)
+        s = int(st.item())
+        if s != 0:
+            raise _lib.PetgemError("pg_source_rhs", s, "source not located in the computational domain")
+        return b, int(elem.item())
+
+    def apply_pec(self, vals, b=None):
+        """zeroRowsColumns(boundaries, diag=1) and b[boundaries] = 0 (solver.py:552-577)."""
+        _lib.call("pg_apply_pec", _p(self.rowptr), _p(self.col), _p(vals), self.N, _p(self.bnd), self.bnd.numel(),
+                  _p(b), _p(self.pec_flags), _s())
+        return vals, b
+
+    def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
+              raise_on_fail=True):
+        """Right-Jacobi GMRES; b complex128 [N] or [N, k] (k in 1,2,4,8,16,32)."""
+        nrhs = 1 if b.ndim == 1 else int(b.shape[1])
+        x = torch.zeros_like(b) if x0 is None else x0.clone()
+        o = _lib.GmresOpts()
+        _lib.load().pg_gmres_default_opts(ctypes.byref(o))
+        o.restart, o.max_it, o.rtol = int(restart), int(max_it), float(rtol)
+        o.precision = {"fp64": 0, "mixed": 1}[precision]
+        o.reorth = 1 if reorth else 0
+        res = _lib.GmresResult()
+        rr = (ctypes.c_double * nrhs)()
+        nbytes = _lib.query("pg_gmres_workspace_bytes", self.N, self.nnz, nrhs, ctypes.byref(o))
+        ws = _ws(nbytes + 256, self.device)
+        st = _lib.load().pg_gmres(_p(self.rowptr), _p(self.col), _p(vals), self.N, self.nnz, _p(b.contiguous()), _p(x),
+                                  nrhs, ctypes.byref(o), ctypes.byref(res), ctypes.cast(rr, ctypes.c_void_p), _p(ws),
+                                  ws.numel(), _s())
+        info = SolveInfo(int(res.iterations), int(res.restarts), float(res.relres), int(st), list(rr))
+        if st != 0 and (raise_on_fail or st != -7):
+            msg = _lib.load().pg_last_error()
+            raise _lib.PetgemError("pg_gmres", st, msg.decode() if msg else "")
+        return x, info
+
+    def receiver_fields(self, x, receivers, frequency):
+        """(fields complex128 [R', 6], kept mask) like petgem fieldInterpolator
+        (postprocessing.py:479-616): receivers outside the mesh are dropped."""
+        pts_t, elem = self.locate(receivers)
+        R = pts_t.shape[0]
+        F = torch.empty((R, 6), dtype=torch.complex128, device=self.device)
+        omu = 2.0 * math.pi * float(frequency) * MU0
+        _lib.call("pg_gather_fields", _p(x.contiguous()), _p(self.nodes), _p(self.elemsN), _p(self.eo), _p(self.fo),
+                  _p(self.dofs), self.p, _p(pts_t), _p(elem), R, omu, _p(F), _s())
+        keep = (elem >= 0)
+        return F[keep], keep
+
+    def spmv(self, vals, x):
+        y = torch.empty_like(x)
+        nrhs = 1 if x.ndim == 1 else int(x.shape[1])
+        _lib.call("pg_spmv_z", _p(self.rowptr), _p(self.col), _p(vals), self.N, _p(x.contiguous()), _p(y), nrhs, _s())
+        return y

@@ -1,0 +1,177 @@
+"""GPU pipeline parity: topology / DOF maps / PEC DOFs bit-exact against the
+reference's golden hashes; CSR pattern bit-exact and values within 1e-12 of
+the oracle; source RHS within 1e-12 of the reference; solves to a 1e-8 true
+relative residual with receiver fields within 1e-6 of the reference's
+fieldInterpolator applied to a direct solution."""
+import json
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from oracle import fem, topology
+from tests.helpers import load, load_test_mesh, rel_norm, sha, topology_json
+
+pytestmark = pytest.mark.gpu
+
+ELEM_TOL = 1e-12      # elemental / assembled values, normwise relative
+FIELD_TOL = 1e-6      # receiver E/H at a 1e-8 relative residual
+
+
+def _mesh(pts, tets, p, pattern=True):
+    from petgem_gb300.engine import DeviceMesh
+    return DeviceMesh(pts, tets, p, pattern=pattern)
+
+
+@pytest.mark.parametrize("case", ["test_mesh", "kuhn3"])
+def test_topology_dofs_boundary_bit_exact(case):
+    ref = topology_json()[case]
+    if case == "test_mesh":
+        pts, tets, _ = load_test_mesh()
+    else:
+        from petgem_gb300 import synthetic
+        pts, tets = synthetic.kuhn_box(3)
+    for p in (1, 2, 3):
+        m = _mesh(pts, tets, p, pattern=False)
+        assert (m.nE, m.nF) == (ref["nEdges"], ref["nFaces"])
+        got = {"elemsE": m.elemsE, "elemsF": m.elemsF, "edgesNodes": m.edgesNodes, "facesN": m.facesN,
+               "facesE": m.facesE, "eo": m.eo, "fo": m.fo}
+        for k, v in got.items():
+            assert sha(v.cpu().numpy()) == ref["sha"][k], (p, k)
+        assert m.N == ref[f"p{p}"]["total_num_dofs"]
+        assert sha(m.dofs.cpu().numpy()) == ref[f"p{p}"]["dofs_sha"]
+        assert sha(m.bnd.cpu().numpy()) == ref[f"p{p}"]["boundary_sha"]
+    if case == "test_mesh":
+        # petgem tests/test_mesh.py:31-36
+        assert m.elemsE[0].tolist() == [10591, 10600, 10831, 10832, 10601, 11465]
+        assert m.elemsF[0].tolist() == [17369, 17370, 17400, 17977]
+
+
+def _oracle_A(pts, tets, sigma, p, freq):
+    t = {}
+    elemsE, edgesN = topology.compute_edges(tets)
+    elemsF, facesN = topology.compute_faces(tets)
+    facesE = topology.compute_faces_edges(elemsF, elemsE, facesN.shape[0])
+    eo, fo = topology.element_orientation(tets, elemsE, edgesN, elemsF, facesE)
+    dofs, de, df, dv, nd = topology.compute_connectivity_dofs(elemsE, elemsF, p)
+    M, K = fem.element_matrices_batch(pts[tets], eo, fo, sigma, p)
+    return fem.assemble(M, K, dofs, nd, freq)
+
+
+def _csr(m, vals):
+    return sp.csr_matrix((vals.cpu().numpy(), m.col.cpu().numpy(), m.rowptr.cpu().numpy()), shape=(m.N, m.N))
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+@pytest.mark.parametrize("fused", [True, False])
+def test_assembly_vs_reference_golden(p, fused):
+    g = load("system_n2.npz")
+    pts, tets, sigma = g["points"], g["tets"], g["sigma"]
+    src = json.loads(str(g["src"]))
+    m = _mesh(pts, tets, p)
+    vals = m.assemble(sigma, src["frequency"], fused=fused)
+    A = _csr(m, vals)
+    assert np.array_equal(A.indptr, g[f"p{p}_indptr"]) and np.array_equal(A.indices, g[f"p{p}_indices"])
+    assert rel_norm(A.data, g[f"p{p}_data"]) < ELEM_TOL
+    b, se = m.source_vector(src)
+    assert se == int(g[f"p{p}_src_elem"])
+    assert rel_norm(b.cpu().numpy(), g[f"p{p}_b"]) < ELEM_TOL
+    assert np.array_equal(m.bnd.cpu().numpy(), g[f"p{p}_bnd"])
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_assembly_test_mesh_vs_oracle_and_deterministic(p):
+    pts, tets, phys = load_test_mesh()
+    rng = np.random.default_rng(3)
+    s = 10.0 ** rng.uniform(-2, 0.5, len(tets))
+    sigma = np.stack([s, s * rng.uniform(0.5, 1.0, len(tets))], 1)
+    m = _mesh(pts, tets, p)
+    v1 = m.assemble(sigma, 2.0, fused=True)
+    v2 = m.assemble(sigma, 2.0, fused=True)
+    assert torch.equal(v1, v2)                       # bitwise reproducible
+    v3 = m.assemble(sigma, 2.0, fused=False)
+    A = _csr(m, v1)
+    Ao = _oracle_A(pts, tets, sigma, p, 2.0)
+    assert np.array_equal(A.indptr, Ao.indptr) and np.array_equal(A.indices, Ao.indices)
+    assert rel_norm(A.data, Ao.data) < ELEM_TOL
+    assert rel_norm(v3.cpu().numpy(), Ao.data) < ELEM_TOL
+
+
+def test_pec_matches_oracle():
+    g = load("system_n2.npz")
+    pts, tets, sigma = g["points"], g["tets"], g["sigma"]
+    src = json.loads(str(g["src"]))
+    p = 2
+    m = _mesh(pts, tets, p)
+    vals = m.assemble(sigma, src["frequency"])
+    b, _ = m.source_vector(src)
+    m.apply_pec(vals, b)
+    Ar = sp.csr_matrix((g["p2_data"], g["p2_indices"], g["p2_indptr"]), shape=(m.N, m.N))
+    Ao, bo = fem.apply_pec(Ar, g["p2_b"], g["p2_bnd"])
+    A = _csr(m, vals)
+    assert abs(A - Ao).max() <= ELEM_TOL * abs(Ao).max()
+    assert rel_norm(b.cpu().numpy(), bo) < ELEM_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_and_receivers_vs_reference(precision):
+    g = load("pipeline_n3.npz")
+    pts, tets, sigma = g["points"], g["tets"], g["sigma"]
+    src = json.loads(str(g["src"]))
+    m = _mesh(pts, tets, 2)
+    vals = m.assemble(sigma, src["frequency"])
+    b, se = m.source_vector(src)
+    assert se == int(g["src_elem"])
+    m.apply_pec(vals, b)
+    assert rel_norm(b.cpu().numpy(), g["b"]) < ELEM_TOL
+    x, info = m.solve(vals, b, rtol=1e-10, precision=precision)
+    assert info.relres <= 1e-10
+    A = _csr(m, vals)
+    xn = x.cpu().numpy()
+    assert np.linalg.norm(A @ xn - b.cpu().numpy()) <= 1e-10 * np.linalg.norm(b.cpu().numpy()) * 1.01
+    F, keep = m.receiver_fields(x, g["receivers"], src["frequency"])
+    assert keep.cpu().numpy().tolist() == [True] * 7 + [False]     # the receiver outside is dropped
+    assert rel_norm(F.cpu().numpy(), g["fields"]) < FIELD_TOL
+
+
+def test_multi_rhs_matches_single():
+    from petgem_gb300 import synthetic
+    mdl = synthetic.csem_two_layer(4, 2, block=False)
+    m = _mesh(mdl.nodes, mdl.tets, 2)
+    vals = m.assemble(mdl.sigma, 1.0)
+    m.apply_pec(vals, None)
+    bs = []
+    for x0 in (-600.0, -200.0, 200.0, 600.0):
+        src = dict(mdl.source, position=[x0, 10.0, 50.0])
+        b, _ = m.source_vector(src)
+        m.apply_pec(vals.clone(), b)                     # zero the PEC entries of b
+        bs.append(b)
+    B = torch.stack(bs, 1).contiguous()
+    for prec in ("fp64", "mixed"):
+        X, info = m.solve(vals, B, rtol=1e-9, precision=prec)
+        assert max(info.relres_per_rhs) <= 1e-9
+        for k in range(4):
+            xk, _ = m.solve(vals, bs[k], rtol=1e-11)
+            assert rel_norm(X[:, k].cpu().numpy(), xk.cpu().numpy()) < 1e-6
+
+
+def test_gmres_maxit_status_is_returned():
+    from petgem_gb300 import _lib, synthetic
+    mdl = synthetic.csem_two_layer(4, 2, block=False)
+    m = _mesh(mdl.nodes, mdl.tets, 2)
+    vals = m.assemble(mdl.sigma, 1.0)
+    b, _ = m.source_vector(mdl.source)
+    m.apply_pec(vals, b)
+    x, info = m.solve(vals, b, rtol=1e-14, max_it=5, raise_on_fail=False)
+    assert info.status == -7 and info.iterations <= 30
+    with pytest.raises(_lib.PetgemError):
+        m.solve(vals, b, rtol=1e-14, max_it=5)
+
+
+def test_source_outside_mesh_raises():
+    from petgem_gb300 import _lib, synthetic
+    mdl = synthetic.csem_two_layer(2, 1, block=False)
+    m = _mesh(mdl.nodes, mdl.tets, 1)
+    with pytest.raises(_lib.PetgemError):
+        m.source_vector(dict(mdl.source, position=[5000.0, 0.0, 0.0]))
