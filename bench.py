@@ -1,0 +1,413 @@
+#!/usr/bin/env python3
+"""Benchmark of the petgem forward-modelling hot path on GB300.
+
+Workload (configuration the metric is quoted on): mixed-precision CSEM,
+Nedelec p=2 on a box [-1000,1000]^3 m split into 32^3 cubes x 6 Kuhn
+tetrahedra (196,608 tets, 1,276,096 DOFs, 54,751,616 stored entries),
+interior nodes jittered by U(+-0.15h) (seed 0), per-element conductivity
+log-uniform in [0.01, 3.3] S/m (seed 1), x-directed HED at (0,0,50) m, 1 Hz.
+Seeded synthetic inputs with these shapes stand in for any dataset.
+
+One step = one pass of the assembly over the whole mesh with inputs
+resident in HBM: element geometry coefficients -> fused elemental
+matrices + deterministic CSR value assembly -> point-dipole RHS -> PEC.
+`value` is Melem/s = elements / step time (the metric's "p=2 Melem/s
+assembled"); the pattern build (once per mesh) is reported separately.
+The "ms/RHS to 1e-8 residual, FP64 vs mixed-precision batched" half of the
+metric is measured in `solve` (true FP64 residual <= 1e-8 ||b||).
+
+`--impl reference` times the reference's algorithm on the host CPU (the
+numpy oracle port of petgem's hvfem elemental matrices + COO assembly), on
+bounded samples of the same workload, with all host cores.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "p=2 Melem/s assembled; ms/RHS to 1e-8 residual, FP64 vs mixed-prec batched"
+WORKLOAD = "csem_p2_32cubed_jittered_logsigma (196,608 tets, 1,276,096 DOFs)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=32, help="cubes per axis (32 = the metric's configuration)")
+    ap.add_argument("--solve", default="all", choices=["all", "none"])
+    ap.add_argument("--max-it", type=int, default=40000)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of a baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--solve-iters", type=int, default=0,
+                    help="profiling mode: run each solver form for exactly this many iterations")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- CPU (oracle) leg
+def _cpu_worker(args):
+    """Elemental matrices + COO->CSR assembly of a slice of elements with the
+    oracle (numpy restatement of petgem/hvfem.py:223-316, solver.py:182-235)."""
+    coords, eo, fo, sigma, dofs, p, N = args
+    from oracle import fem
+    M, K = fem.element_matrices_batch(coords, eo, fo, sigma, p)
+    A = fem.assemble(M, K, dofs, N, 1.0)
+    return A.nnz
+
+
+def cpu_assembly_rate(model, seconds, cores):
+    """Melem/s of the oracle assembly on a bounded sample; returns (rate, sample_elems, wall)."""
+    from oracle import topology
+    tets = model.tets
+    eE, eN = topology.compute_edges(tets)
+    eF, fN = topology.compute_faces(tets)
+    fE = topology.compute_faces_edges(eF, eE, fN.shape[0])
+    eo, fo = topology.element_orientation(tets, eE, eN, eF, fE)
+    dofs, _, _, _, N = topology.compute_connectivity_dofs(eE, eF, model.p)
+    coords = model.nodes[tets]
+
+    def job(idx):
+        return (coords[idx], eo[idx], fo[idx], model.sigma[idx], dofs[idx], model.p, N)
+
+    # calibrate on one core
+    t = time.time()
+    _cpu_worker(job(np.arange(64)))
+    per_elem = (time.time() - t) / 64
+    n_el = int(min(len(tets), max(cores * 64, seconds * cores / max(per_elem, 1e-6))))
+    idx = np.arange(n_el)
+    parts = np.array_split(idx, cores * 4)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_cpu_worker, [job(parts[0][:8])] * cores)     # warm the workers
+        t = time.time()
+        pool.map(_cpu_worker, [job(pp) for pp in parts])
+        wall = time.time() - t
+    return n_el / wall / 1e6, n_el, wall
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"pg_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [ln.split(",") for ln in open(self.path).read().strip().splitlines() if ln.strip()]
+        except Exception:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- GPU leg
+def fp64_peak(torch, lib):
+    import ctypes
+    out = torch.empty(152 * 16 * 256, dtype=torch.float64, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    blocks, iters = 152 * 16, 2048
+    for _ in range(2):
+        lib.pg_fp64_probe(ctypes.c_void_p(out.data_ptr()), blocks, iters, s)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        lib.pg_fp64_probe(ctypes.c_void_p(out.data_ptr()), blocks, iters, s)
+    e1.record()
+    torch.cuda.synchronize()
+    return 5 * lib.pg_fp64_probe_flops(blocks, iters) / (e0.elapsed_time(e1) * 1e-3) / 1e12
+
+
+def read_traffic(name):
+    """dram bytes per launch recorded in a committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from petgem_gb300 import _lib, synthetic
+    from petgem_gb300.engine import DeviceMesh
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    lib = _lib.load()
+    model = synthetic.config1(args.n)
+    freq = model.source["frequency"]
+
+    t0 = time.time()
+    mesh = DeviceMesh(model.nodes, model.tets, model.p, device=f"cuda:{local_rank}")
+    torch.cuda.synchronize()
+    setup_ms = (time.time() - t0) * 1e3
+    T = mesh.T
+    sigma = mesh.sigma_tensor(model.sigma)
+    coef = torch.empty((T, 12), dtype=torch.float64, device="cuda")
+    vals = torch.empty(mesh.nnz, dtype=torch.complex128, device="cuda")
+    b = torch.zeros(mesh.N, dtype=torch.complex128, device="cuda")
+    src_elem = mesh.locate_source(model.source)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    launches_per_step = 5   # coefficients, fused assembly, source, PEC mark, PEC rows
+
+    def step():
+        mesh.element_coefficients(sigma, freq, out=coef, check=False)
+        mesh.assemble(sigma, freq, out=vals, coef=coef)
+        b.zero_()
+        mesh.source_rhs(model.source, src_elem, b, status=status)
+        mesh.apply_pec(vals, b)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if status.item() != 0:
+        raise RuntimeError("source RHS failed")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    ms_max = ms
+    if dist is not None:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    ms_per_step = ms_max / args.steps
+    value = world * T / (ms_per_step * 1e-3) / 1e6
+
+    # dominant kernel: fused assembly, timed alone on the launching stream
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record()
+    for _ in range(args.steps):
+        mesh.assemble(sigma, freq, out=vals, coef=coef)
+    k1.record()
+    torch.cuda.synchronize()
+    k_ms = k0.elapsed_time(k1) / args.steps
+    nd = mesh.nd
+    flops = T * (nd * (nd + 1) // 2) * 12 * 2          # 12 FMA per unique elemental entry
+    peak64 = fp64_peak(torch, lib)
+    achieved = flops / (k_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": "k_values_sym (fused elemental + CSR assembly)",
+                "achieved": round(achieved, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
+                "frac": round(achieved / peak64, 4), "peak_source": "measured live (FP64 FMA probe)",
+                "traffic": read_traffic("assembly_cfg1_ncu.md"),
+                "algorithmic_flops_per_launch": flops, "ms_per_launch": round(k_ms, 4),
+                "algorithmic_bytes_per_launch": int(mesh.nnz * 16 + mesh.items.numel() * 8 + T * (12 * 8 + 4) +
+                                                    mesh.members.numel() * 4)}
+
+    # end to end: host buffers in (pinned), A values and b back to the host
+    nodes_h = torch.from_numpy(np.ascontiguousarray(model.nodes)).pin_memory()
+    sigma_h = torch.from_numpy(np.ascontiguousarray(model.sigma)).pin_memory()
+    vals_h = torch.empty(mesh.nnz, dtype=torch.complex128).pin_memory()
+    b_h = torch.empty(mesh.N, dtype=torch.complex128).pin_memory()
+
+    def e2e_step():
+        mesh.nodes.copy_(nodes_h, non_blocking=True)
+        sigma.copy_(sigma_h, non_blocking=True)
+        step()
+        vals_h.copy_(vals, non_blocking=True)
+        b_h.copy_(b, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e = {"value": round(world * T / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Melem/s",
+           "h2d_bytes_per_step": int(nodes_h.numel() * 8 + sigma_h.numel() * 8),
+           "d2h_bytes_per_step": int(vals_h.numel() * 16 + b_h.numel() * 16), "ms_per_step": round(e2e_ms, 3)}
+
+    solve = None
+    if args.solve_iters > 0 and rank == 0:
+        solve = profile_solves(args, torch, mesh, vals, b)
+    elif args.solve == "all" and rank == 0:
+        solve = run_solves(args, torch, mesh, model, vals, b)
+
+    line = None
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Melem/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+                "higher_is_better": True, "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded Kuhn-cube mesh, jittered; log-uniform sigma)",
+                "config": {"workload": WORKLOAD, "p": 2, "tets": T, "dofs": mesh.N, "nnz": mesh.nnz,
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "l2": "working set per step > 1 GB (A values alone 876 MB) > 129 MB L2",
+                           "pattern_setup_ms": round(setup_ms, 1), "orientation_tuples": mesh.n_tuples},
+                "roofline": roofline, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
+                "clocks": clk.summary(), "solve": solve}
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return line
+
+
+def run_solves(args, torch, mesh, model, vals, b):
+    """ms/RHS to a 1e-8 true relative residual for the plain FP64 form and the
+    mixed-precision batched form (COCG with Jacobi scaling; restarted GMRES(30)
+    per iteration cost as the PETSc-default reference point)."""
+    from petgem_gb300 import synthetic
+    out = {"criterion": "||b - A x|| <= 1e-8 ||b|| (FP64 true residual)"}
+
+    def timed(ksp, prec, rhs, max_it):
+        torch.cuda.synchronize()
+        t = time.time()
+        x, info = mesh.solve(vals, rhs, rtol=1e-8, precision=prec, max_it=max_it, raise_on_fail=False, ksp=ksp)
+        torch.cuda.synchronize()
+        dt = time.time() - t
+        k = 1 if rhs.ndim == 1 else rhs.shape[1]
+        return x, {"ksp": ksp, "precision": prec, "nrhs": k, "seconds": round(dt, 3),
+                   "ms_per_rhs": round(dt * 1e3 / k, 2), "iterations": info.iterations,
+                   "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4),
+                   "relres": info.relres, "converged": info.status == 0}
+
+    srcs = synthetic.config2_sources()[:args.nrhs]
+    B = torch.zeros((mesh.N, len(srcs)), dtype=torch.complex128, device="cuda")
+    for k, s in enumerate(srcs):
+        bk = torch.zeros(mesh.N, dtype=torch.complex128, device="cuda")
+        mesh.source_rhs(s, mesh.locate_source(s), bk)
+        B[:, k] = bk
+    B[mesh.bnd.long(), :] = 0
+    x64, r64 = timed("cocg", "fp64", b, args.max_it)
+    xmx, rmx = timed("cocg", "mixed", b, args.max_it)
+    Xb, rb = timed("cocg", "mixed", B.contiguous(), args.max_it)
+    _, rg = timed("gmres", "mixed", b, 300)
+    # receiver-field error of each form against a tight FP64 solve
+    xt, _ = mesh.solve(vals, b, rtol=1e-11, precision="fp64", max_it=4 * args.max_it, raise_on_fail=False, ksp="cocg")
+    Ft, _ = mesh.receiver_fields(xt, model.receivers, model.source["frequency"])
+    for x, r in ((x64, r64), (xmx, rmx)):
+        F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
+        r["receiver_rel_err_vs_fp64_1e-11"] = float(torch.linalg.norm(F - Ft) / torch.linalg.norm(Ft))
+    out["fp64"] = r64
+    out["mixed"] = rmx
+    out["mixed_batched"] = rb
+    out["gmres30_mixed_300its"] = rg
+    out["speedup_mixed_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rb["ms_per_rhs"], 1e-9), 2)
+    return out
+
+
+def profile_solves(args, torch, mesh, vals, b):
+    """Fixed iteration counts of every solver form (for kernel launch lists)."""
+    out = {}
+    B = torch.stack([b] * args.nrhs, 1).contiguous()
+    for name, ksp, prec, rhs in (("cocg_fp64", "cocg", "fp64", b), ("cocg_mixed", "cocg", "mixed", b),
+                                 ("cocg_mixed_batched", "cocg", "mixed", B), ("gmres_mixed", "gmres", "mixed", b),
+                                 ("gmres_fp64", "gmres", "fp64", b)):
+        torch.cuda.synchronize()
+        t = time.time()
+        _, info = mesh.solve(vals, rhs, rtol=1e-30, precision=prec, max_it=args.solve_iters, raise_on_fail=False,
+                             ksp=ksp, check_every=args.solve_iters)
+        torch.cuda.synchronize()
+        dt = time.time() - t
+        out[name] = {"iterations": info.iterations, "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4)}
+    return out
+
+
+def run_reference(args, rank):
+    """The reference's algorithm (oracle port) on the host CPU, bounded samples."""
+    if rank != 0:
+        return None
+    from petgem_gb300 import synthetic
+    model = synthetic.config1(args.n)
+    cores = os.cpu_count() or 1
+    rates = []
+    samples = []
+    for _ in range(max(args.steps, 1)):
+        rate, n_el, wall = cpu_assembly_rate(model, args.cpu_seconds / 4, cores)
+        rates.append(rate)
+        samples.append(n_el)
+    v = float(np.median(rates))
+    sample = (f"oracle elemental matrices + COO/CSR assembly of the first {samples[0]} of {len(model.tets)} "
+              f"elements per step, {cores} processes")
+    return {"metric": METRIC, "value": round(v, 6), "unit": "Melem/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD, "p": 2},
+            "cpu_baseline": {"value": round(v, 6), "unit": "Melem/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(v, 6), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    line = run_gpu(args, rank, world, local_rank)
+    if rank == 0 and line is not None:
+        if not args.no_cpu_baseline:
+            from petgem_gb300 import synthetic
+            cores = os.cpu_count() or 1
+            rate, n_el, wall = cpu_assembly_rate(synthetic.config1(args.n), args.cpu_seconds, cores)
+            line["cpu_baseline"] = {"value": round(rate, 6), "unit": "Melem/s", "cores": cores, "kind": "port",
+                                    "sample": f"oracle assembly of {n_el} elements of the same mesh, "
+                                              f"{cores} processes, {wall:.1f} s"}
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -46,6 +46,12 @@ int pg_abi_version(void);
 /* Message for the last failing call on the calling thread. */
 const char* pg_last_error(void);
 
+/* Measurement helper, no petgem counterpart: FP64 FMA throughput probe
+ * (8 independent FMA chains per thread, 256 threads per block).
+ * out: f64 [blocks * 256]; pg_fp64_probe_flops gives the flops of one launch. */
+int pg_fp64_probe(double* out, int blocks, int iters, void* stream);
+int64_t pg_fp64_probe_flops(int blocks, int iters);
+
 /* ------------------------------------------------------------------------
  * Reference-space integration tables
  * --------------------------------------------------------------------- */
@@ -174,12 +180,27 @@ int pg_assemble_values(const double* M, const double* K, const int32_t* members,
 int pg_element_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t n_elems,
                             double omega_mu, double* coef, int32_t* status, void* stream);
 
+size_t pg_pattern_items_workspace_bytes(int64_t n_pairs);
+
+/* Work list of the symmetric fused assembly: for every entity pair (a, b)
+ * with a <= b, one item per entry of its upper block (all na*nb entries when
+ * a < b, the na(na+1)/2 upper entries when a == b), encoded (pair << 12) |
+ * entry; pair_partner[g] = index of the transposed pair (b, a).
+ * Out: pair_partner int32 [n_pairs]; items int64 [cap nnz]; n_items int64 [1]. */
+int pg_pattern_items(const int32_t* members, const int32_t* pair_start, int64_t n_pairs, const int32_t* elemsE,
+                     const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, int32_t* pair_partner,
+                     int64_t* items, int64_t* n_items, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Fused elemental + assembly: vals complex128 [nnz] without materialising
- * elemental matrices (12 FMAs per contribution from coef and tables). */
+ * elemental matrices.  Each item sums 12 FMAs per member element (element
+ * coefficients x orientation-tuple tables) in ascending element order and
+ * writes the value to its slot and to the transposed slot, so A comes out
+ * exactly symmetric and bitwise reproducible. */
 int pg_assemble_fused(const double* coef, const int32_t* tuple_of_elem, const double* tables, const int32_t* members,
-                      const int32_t* pair_start, const int32_t* pair_colstart, int64_t n_pairs,
-                      const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p,
-                      const int64_t* rowptr, double* vals, void* stream);
+                      const int32_t* pair_start, const int32_t* pair_colstart, const int32_t* pair_partner,
+                      const int64_t* items, int64_t n_items, int64_t n_pairs, const int32_t* elemsE,
+                      const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, const int64_t* rowptr,
+                      double* vals, void* stream);
 
 /* PETSc MatZeroRowsColumns(rows, diag=1) and b[rows] = 0
  * (petgem/solver.py:552-577).  b may be NULL.  flag_ws uint8 [n_dofs]. */
@@ -249,6 +270,26 @@ size_t pg_gmres_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_gmres
 int pg_gmres(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz, const double* b,
              double* x, int nrhs, const pg_gmres_opts* opts, pg_gmres_result* result, double* relres_per_rhs,
              void* workspace, size_t workspace_bytes, void* stream);
+
+/* COCG (conjugate orthogonal CG) for the complex-symmetric A with symmetric
+ * Jacobi scaling; an additional KSP type beside GMRES for the same system
+ * (petgem configures PETSc's KSP from the options file, solver.py:588).
+ * precision 0: complex128 recurrence; 1: complex64 recurrence with complex128
+ * reliable updates.  The true FP64 residual is checked every check_every
+ * iterations (doubling up to 400) and decides convergence. */
+typedef struct pg_cocg_opts {
+  int max_it;
+  double rtol;
+  int precision;
+  int check_every;
+} pg_cocg_opts;
+
+void pg_cocg_default_opts(pg_cocg_opts* opts);
+size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts);
+/* Same conventions as pg_gmres (result.restarts = number of residual checks). */
+int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz, const double* b,
+            double* x, int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result, double* relres_per_rhs,
+            void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

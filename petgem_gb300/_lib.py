@@ -28,13 +28,22 @@ class GmresResult(ctypes.Structure):
                 ("status", ctypes.c_int)]
 
 
+class CocgOpts(ctypes.Structure):
+    """pg_cocg_opts (include/petgem_gb300.h)."""
+    _fields_ = [("max_it", ctypes.c_int), ("rtol", ctypes.c_double), ("precision", ctypes.c_int),
+                ("check_every", ctypes.c_int)]
+
+
 _PO = ctypes.POINTER(GmresOpts)
+_PC = ctypes.POINTER(CocgOpts)
 _PR = ctypes.POINTER(GmresResult)
 
 # name -> (restype, argtypes); mirrors include/petgem_gb300.h
 SIGNATURES = {
     "pg_abi_version": (_INT, []),
     "pg_last_error": (ctypes.c_char_p, []),
+    "pg_fp64_probe": (_INT, [_P, _INT, _INT, _P]),
+    "pg_fp64_probe_flops": (_I64, [_INT, _INT]),
     "pg_table_doubles": (_I64, [_INT]),
     "pg_tuples_workspace_bytes": (_SZ, [_I64]),
     "pg_orientation_tuples": (_INT, [_P, _P, _I64, _P, _P, _P, _P, _SZ, _P]),
@@ -52,7 +61,10 @@ SIGNATURES = {
     "pg_pattern_columns": (_INT, [_P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P]),
     "pg_assemble_values": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _D, _P, _P]),
     "pg_element_coefficients": (_INT, [_P, _P, _P, _I64, _D, _P, _P, _P]),
-    "pg_assemble_fused": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P]),
+    "pg_pattern_items_workspace_bytes": (_SZ, [_I64]),
+    "pg_pattern_items": (_INT, [_P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _SZ, _P]),
+    "pg_assemble_fused": (_INT, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P,
+                                 _P]),
     "pg_apply_pec": (_INT, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P]),
     "pg_locate_points": (_INT, [_P, _P, _I64, _P, _I64, _D, _P, _P]),
     "pg_source_rhs": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _P, _D, _D, _P, _P, _P]),
@@ -62,6 +74,9 @@ SIGNATURES = {
     "pg_gmres_default_opts": (None, [_PO]),
     "pg_gmres_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PO]),
     "pg_gmres": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PO, _PR, _P, _P, _SZ, _P]),
+    "pg_cocg_default_opts": (None, [_PC]),
+    "pg_cocg_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PC]),
+    "pg_cocg": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PC, _PR, _P, _P, _SZ, _P]),
 }
 
 STATUS = {

@@ -241,43 +241,108 @@ __device__ __forceinline__ int packed_index(int j, int k, int nd) {
   return j * nd - (j * (j - 1)) / 2 + (k - j);
 }
 
-// fused values: warp per pair; each member contributes 12 FMAs per entry
-__global__ void k_values_fused(const double* __restrict__ coef, const int32_t* __restrict__ tuple_of_elem,
-                               const double* __restrict__ tables, const int32_t* __restrict__ members,
-                               const int32_t* __restrict__ pair_start, const int32_t* __restrict__ colstart,
-                               int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, Ent E, int nd,
-                               const int64_t* __restrict__ rowptr, double2* __restrict__ vals) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+// ---- symmetric item lists: one item per upper entry of every pair with a <= b
+__global__ void k_pair_keys_of(const int32_t* members, const int32_t* pair_start, int64_t n_pairs,
+                               const int32_t* elemsE, const int32_t* elemsF, Ent E, int64_t* pair_key,
+                               int32_t* n_items) {
   const int nl2 = E.nl * E.nl;
-  const int64_t NT = (int64_t)nd * (nd + 1) / 2;
-  for (int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; g < n_pairs; g += warps) {
+  const int64_t n_ent = E.count();
+  GRID_STRIDE(g, n_pairs) {
+    const int32_t m = members[pair_start[g]];
+    const int64_t e = m / nl2;
+    const int r = m % nl2;
+    const int64_t a = E.ent(elemsE, elemsF, e, r / E.nl), b = E.ent(elemsE, elemsF, e, r % E.nl);
+    pair_key[g] = a * n_ent + b;
+    const int na = E.nd_ent(a), nb = E.nd_ent(b);
+    n_items[g] = a < b ? na * nb : (a == b ? na * (na + 1) / 2 : 0);
+  }
+}
+
+__global__ void k_partner(const int64_t* pair_key, int64_t n_pairs, Ent E, int32_t* partner) {
+  const int64_t n_ent = E.count();
+  GRID_STRIDE(g, n_pairs) {
+    const int64_t key = pair_key[g];
+    const int64_t want = (key % n_ent) * n_ent + key / n_ent;
+    int64_t lo = 0, hi = n_pairs - 1, found = -1;
+    while (lo <= hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      const int64_t v = pair_key[mid];
+      if (v == want) { found = mid; break; }
+      if (v < want) lo = mid + 1; else hi = mid - 1;
+    }
+    partner[g] = (int32_t)found;
+  }
+}
+
+__global__ void k_items(const int32_t* n_items, const int32_t* item_start, int64_t n_pairs, int64_t* items) {
+  GRID_STRIDE(g, n_pairs) {
+    const int c = n_items[g];
+    const int64_t base = item_start[g];
+    for (int t = 0; t < c; ++t) items[base + t] = ((int64_t)g << 12) | t;
+  }
+}
+
+__global__ void k_store_i64(const int32_t* src, int64_t* dst) { *dst = *src; }
+
+// fused symmetric values: one thread per item; members summed in element order,
+// 12 FMAs per member; the value goes to slot (a,b) and to its transpose (b,a).
+template <int P>
+__global__ void __launch_bounds__(256) k_values_sym(const double* __restrict__ coef,
+                                                    const int32_t* __restrict__ tuple_of_elem,
+                                                    const double* __restrict__ tables,
+                                                    const int32_t* __restrict__ members,
+                                                    const int32_t* __restrict__ pair_start,
+                                                    const int32_t* __restrict__ colstart,
+                                                    const int32_t* __restrict__ partner,
+                                                    const int64_t* __restrict__ items, int64_t n_items,
+                                                    const int32_t* __restrict__ elemsE,
+                                                    const int32_t* __restrict__ elemsF, int64_t nE, int64_t nF,
+                                                    int64_t T, const int64_t* __restrict__ rowptr,
+                                                    double2* __restrict__ vals) {
+  constexpr int NL = P == 1 ? 6 : (P == 2 ? 10 : 11);
+  constexpr int NL2 = NL * NL;
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  constexpr int NT = ND * (ND + 1) / 2;
+  const Ent E(nE, nF, T, P);
+  GRID_STRIDE(idx, n_items) {
+    const int64_t it = items[idx];
+    const int64_t g = it >> 12;
+    int t = (int)(it & 4095);
     const int32_t s0 = pair_start[g], s1 = pair_start[g + 1];
     const int32_t m0 = members[s0];
-    const int64_t e0 = m0 / nl2;
-    const int r0 = m0 % nl2;
-    const int64_t a = E.ent(elemsE, elemsF, e0, r0 / E.nl), b = E.ent(elemsE, elemsF, e0, r0 % E.nl);
+    const int64_t e0 = m0 / NL2;
+    const int r0 = m0 % NL2;
+    const int64_t a = E.ent(elemsE, elemsF, e0, r0 / NL), b = E.ent(elemsE, elemsF, e0, r0 % NL);
     const int na = E.nd_ent(a), nb = E.nd_ent(b);
-    const int64_t fa = E.first_dof(a);
-    const int cs = colstart[g];
-    for (int t = lane; t < na * nb; t += 32) {
-      const int i = t / nb, j = t % nb;
-      double re = 0.0, im = 0.0;
-      for (int32_t s = s0; s < s1; ++s) {
-        const int32_t m = members[s];
-        const int64_t e = m / nl2;
-        const int r = m % nl2;
-        const int jl = E.local_off(r / E.nl) + i, kl = E.local_off(r % E.nl) + j;
-        const double* tb = tables + (int64_t)tuple_of_elem[e] * 12 * NT + packed_index(jl, kl, nd);
-        const double* cf = coef + 12 * e;
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-          re = fma(cf[q], __ldg(tb + (6 + q) * NT), re);
-          im = fma(cf[6 + q], __ldg(tb + q * NT), im);
-        }
-      }
-      vals[rowptr[fa + i] + cs + j] = make_double2(re, im);
+    int i, j;
+    if (a != b) {
+      i = t / nb;
+      j = t - i * nb;
+    } else {  // upper triangle of an na x na block, row by row
+      i = 0;
+      while (t >= na - i) { t -= na - i; ++i; }
+      j = i + t;
     }
+    double re = 0.0, im = 0.0;
+    for (int32_t q = s0; q < s1; ++q) {
+      const int32_t m = members[q];
+      const int64_t e = m / NL2;
+      const int r = m - (int)(e * NL2);
+      const int la = r / NL, lb = r - la * NL;
+      const int jl = E.local_off(la) + i, kl = E.local_off(lb) + j;
+      const double* tb = tables + (int64_t)__ldg(tuple_of_elem + e) * (12 * NT) + packed_index(jl, kl, ND);
+      const double* cf = coef + 12 * e;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        re = fma(__ldg(cf + k), __ldg(tb + (6 + k) * NT), re);
+        im = fma(__ldg(cf + 6 + k), __ldg(tb + k * NT), im);
+      }
+    }
+    const double2 v = make_double2(re, im);
+    const int64_t fa = E.first_dof(a), fb = E.first_dof(b);
+    vals[rowptr[fa + i] + colstart[g] + j] = v;
+    if (a != b) vals[rowptr[fb + j] + colstart[partner[g]] + i] = v;
+    else if (i != j) vals[rowptr[fa + j] + colstart[g] + i] = v;
   }
 }
 
@@ -429,20 +494,71 @@ extern "C" int pg_element_coefficients(const double* nodes, const int32_t* elems
   return PG_OK;
 }
 
+extern "C" size_t pg_pattern_items_workspace_bytes(int64_t n_pairs) {
+  return pg_align256(sizeof(int64_t) * n_pairs) + pg_align256(sizeof(int32_t) * (n_pairs + 1)) * 2 +
+         pg::scan_workspace_bytes(n_pairs + 1) + 1024;
+}
+
+extern "C" int pg_pattern_items(const int32_t* members, const int32_t* pair_start, int64_t n_pairs,
+                                const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF,
+                                int p, int32_t* pair_partner, int64_t* items, int64_t* n_items, void* workspace,
+                                size_t workspace_bytes, void* stream) {
+  if (p < 1 || p > 6 || n_pairs < 1 || !members || !pair_start || !pair_partner || !items || !n_items) {
+    pg_set_error("pg_pattern_items: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (!workspace || workspace_bytes < pg_pattern_items_workspace_bytes(n_pairs)) {
+    pg_set_error("pg_pattern_items: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  cudaStream_t s = pg_stream(stream);
+  Ent E(nE, nF, n_elems, p);
+  PgArena ar(workspace, workspace_bytes);
+  int64_t* pair_key = ar.take<int64_t>(n_pairs);
+  int32_t* cnt = ar.take<int32_t>(n_pairs + 1);
+  int32_t* start = ar.take<int32_t>(n_pairs + 1);
+  const size_t scan_b = pg::scan_workspace_bytes(n_pairs + 1);
+  void* scan_ws = ar.take<char>(scan_b);
+  int32_t* tot = ar.take<int32_t>(4);
+  if (!pair_key || !cnt || !start || !scan_ws || !tot) return PG_ERR_WORKSPACE;
+  const unsigned gP = pg_blocks(n_pairs, 256);
+  k_pair_keys_of<<<gP, 256, 0, s>>>(members, pair_start, n_pairs, elemsE, elemsF, E, pair_key, cnt);
+  k_partner<<<gP, 256, 0, s>>>(pair_key, n_pairs, E, pair_partner);
+  int st = pg::scan_exclusive_i32(cnt, start, n_pairs, tot, scan_ws, scan_b, s);
+  if (st) return st;
+  k_items<<<gP, 256, 0, s>>>(cnt, start, n_pairs, items);
+  k_store_i64<<<1, 1, 0, s>>>(tot, n_items);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
 extern "C" int pg_assemble_fused(const double* coef, const int32_t* tuple_of_elem, const double* tables,
                                  const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
-                                 int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems,
-                                 int64_t nE, int64_t nF, int p, const int64_t* rowptr, double* vals, void* stream) {
-  if (p < 1 || p > 6 || n_pairs < 1 || !coef || !tuple_of_elem || !tables || !members || !pair_start ||
-      !pair_colstart || !rowptr || !vals) {
+                                 const int32_t* pair_partner, const int64_t* items, int64_t n_items, int64_t n_pairs,
+                                 const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE,
+                                 int64_t nF, int p, const int64_t* rowptr, double* vals, void* stream) {
+  if (p < 1 || p > 6 || n_pairs < 1 || n_items < 1 || !coef || !tuple_of_elem || !tables || !members ||
+      !pair_start || !pair_colstart || !pair_partner || !items || !rowptr || !vals) {
     pg_set_error("pg_assemble_fused: bad argument");
     return PG_ERR_ARG;
   }
-  Ent E(nE, nF, n_elems, p);
-  k_values_fused<<<warp_grid(n_pairs), 256, 0, pg_stream(stream)>>>(coef, tuple_of_elem, tables, members, pair_start,
-                                                                    pair_colstart, n_pairs, elemsE, elemsF, E,
-                                                                    pg_nd_elem(p), rowptr,
-                                                                    reinterpret_cast<double2*>(vals));
+  cudaStream_t s = pg_stream(stream);
+  double2* v = reinterpret_cast<double2*>(vals);
+  int64_t blocks = (n_items + 255) / 256;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  const unsigned grid = (unsigned)blocks;
+#define PG_SYM(P) k_values_sym<P><<<grid, 256, 0, s>>>(coef, tuple_of_elem, tables, members, pair_start, pair_colstart, \
+                                                       pair_partner, items, n_items, elemsE, elemsF, nE, nF, n_elems,   \
+                                                       rowptr, v)
+  switch (p) {
+    case 1: PG_SYM(1); break;
+    case 2: PG_SYM(2); break;
+    case 3: PG_SYM(3); break;
+    case 4: PG_SYM(4); break;
+    case 5: PG_SYM(5); break;
+    case 6: PG_SYM(6); break;
+  }
+#undef PG_SYM
   PG_LAUNCH_CHECK();
   return PG_OK;
 }

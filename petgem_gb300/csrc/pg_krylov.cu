@@ -222,18 +222,24 @@ template <typename C, int K>
 __global__ void k_dots_final(const double2* partial, int nblocks, int j, int m, RhsState* st, C* coef, int second,
                              const Ctl* ctl) {
   if (!ctl->any_active) return;
-  for (int t = threadIdx.x; t < (j + 1) * K; t += blockDim.x) {  // t = i * K + rhs
+  // one warp per (i, rhs) item; lanes sum the block partials in a fixed pattern
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int t = warp; t < (j + 1) * K; t += nwarps) {  // t = i * K + rhs
     const int i = t / K, rhs = t % K;
-    RhsState& S = st[rhs];
     double2 s = make_double2(0.0, 0.0);
-    for (int b = 0; b < nblocks; ++b) s = dadd(s, partial[((int64_t)b * (kMaxM + 1) + i) * K + rhs]);
-    const double aj = second ? 1.0 : S.alpha[j];
-    const double2 h = dscale(S.alpha[i] * aj, s);
-    if (S.active) {
-      if (second) S.H[j * (m + 1) + i] = dadd(S.H[j * (m + 1) + i], h);
-      else S.H[j * (m + 1) + i] = h;
+    for (int b = lane; b < nblocks; b += 32) s = dadd(s, partial[((int64_t)b * (kMaxM + 1) + i) * K + rhs]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s = dadd(s, shfl_xor(s, off));
+    if (lane == 0) {
+      RhsState& S = st[rhs];
+      const double aj = second ? 1.0 : S.alpha[j];
+      const double2 h = dscale(S.alpha[i] * aj, s);
+      if (S.active) {
+        if (second) S.H[j * (m + 1) + i] = dadd(S.H[j * (m + 1) + i], h);
+        else S.H[j * (m + 1) + i] = h;
+      }
+      coef[i * K + rhs] = cfrom<C>(dscale(S.alpha[i], h));
     }
-    coef[i * K + rhs] = cfrom<C>(dscale(S.alpha[i], h));
   }
 }
 
@@ -260,14 +266,13 @@ __global__ void __launch_bounds__(kThreads) k_update(const C* __restrict__ V, in
     C v = w[e];
     v.x *= aj[rhs];
     v.y *= aj[rhs];
-#pragma unroll
-    for (int i = 0; i < kMaxM; ++i)
-      if (i <= j) {
-        const C c = cf[i * K + rhs];
-        const C b = V[(int64_t)i * stride + e];
-        v.x -= c.x * b.x - c.y * b.y;
-        v.y -= c.x * b.y + c.y * b.x;
-      }
+#pragma unroll 4
+    for (int i = 0; i <= j; ++i) {
+      const C c = cf[i * K + rhs];
+      const C b = V[(int64_t)i * stride + e];
+      v.x -= c.x * b.x - c.y * b.y;
+      v.y -= c.x * b.y + c.y * b.x;
+    }
     w[e] = v;
     nrm_f += v.x * v.x + v.y * v.y;
   }
@@ -282,12 +287,14 @@ __global__ void k_givens(const double2* partial, int nblocks, int j, int m, RhsS
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
   __syncthreads();
-  const int rhs = threadIdx.x;
+  const int lane = threadIdx.x & 31, rhs = threadIdx.x >> 5;  // one warp per rhs
   if (rhs < K) {
     RhsState& S = st[rhs];
-    if (S.active) {
-      double ss = 0.0;
-      for (int b = 0; b < nblocks; ++b) ss += partial[(int64_t)b * K + rhs].x;
+    double ss = 0.0;
+    for (int b = lane; b < nblocks; b += 32) ss += partial[(int64_t)b * K + rhs].x;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, off);
+    if (lane == 0 && S.active) {
       const double hn = sqrt(ss);
       double2* Hc = S.H + j * (m + 1);
       Hc[j + 1] = make_double2(hn, 0.0);
@@ -331,7 +338,8 @@ __global__ void k_givens(const double2* partial, int nblocks, int j, int m, RhsS
       if (lucky) S.breakdown = 1;
       if (S.res_est <= S.target || lucky || last || !isfinite(S.res_est)) S.active = 0;
     }
-    if (S.active) atomicOr(&any, 1);
+    __syncwarp();
+    if (lane == 0 && S.active) atomicOr(&any, 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) ctl->any_active = any;
@@ -387,11 +395,13 @@ __global__ void __launch_bounds__(kThreads) k_norm2(const double2* __restrict__ 
 
 template <int K>
 __global__ void k_norm_final(const double2* partial, int nblocks, double* out) {
-  const int rhs = threadIdx.x;
+  const int lane = threadIdx.x & 31, rhs = threadIdx.x >> 5;  // one warp per rhs
   if (rhs >= K) return;
   double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += partial[(int64_t)b * K + rhs].x;
-  out[rhs] = sqrt(s);
+  for (int b = lane; b < nblocks; b += 32) s += partial[(int64_t)b * K + rhs].x;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) out[rhs] = sqrt(s);
 }
 
 template <typename C, int K>
@@ -482,11 +492,17 @@ size_t ws_layout(const Plan& P, size_t* off /* 14 */) {
 }
 
 int pick_blocks(int64_t n, int k) {
-  int64_t nb = (n * k + 4095) / 4096;
-  if (nb > 152 * 4) nb = 152 * 4;
+  int64_t nb = (n * k + 1023) / 1024;
+  if (nb > 152 * 8) nb = 152 * 8;
   if (nb < 1) nb = 1;
   return (int)nb;
 }
+
+// Lanes per row: complex128 is FP64-pipe bound, so few lanes keep the
+// shuffle reduction (FP64 adds) small; complex64 is bandwidth bound and uses
+// more lanes for wider coalesced row segments.
+template <typename C> struct LanesPerRow { static int pick(int64_t npr) { return npr > 48 ? 32 : (npr > 20 ? 16 : 8); } };
+template <> struct LanesPerRow<double2> { static int pick(int64_t npr) { return npr > 64 ? 8 : 4; } };
 
 template <typename C>
 void launch_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const C* val, const C* x, C* y,
@@ -494,9 +510,12 @@ void launch_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const
   const unsigned grid = 152 * 16;
   switch (P.k) {
     case 1:
-      if (nnz_per_row > 48) k_spmv1<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl);
-      else if (nnz_per_row > 20) k_spmv1<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl);
-      else k_spmv1<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl);
+      switch (LanesPerRow<C>::pick(nnz_per_row)) {
+        case 32: k_spmv1<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+        case 16: k_spmv1<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+        case 8: k_spmv1<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+        default: k_spmv1<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
+      }
       break;
     case 2: k_spmm<C, 2><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
     case 4: k_spmm<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, x, y, bsub, ctl); break;
@@ -547,7 +566,7 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   // ||b|| per RHS
   std::vector<double> bnorm(k), rn(k), tgt(k);
   std::vector<int> wnt(k);
-  PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, npart), k_norm_final<K><<<1, 32, 0, s>>>(npart, nb, rnorm)));
+  PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, npart), k_norm_final<K><<<1, 32 * K, 0, s>>>(npart, nb, rnorm)));
   PG_LAUNCH_CHECK();
   PG_CUDA_TRY(cudaMemcpyAsync(bnorm.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
   int hstatus = 0;
@@ -574,7 +593,7 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   for (;;) {
     // r = b - A x (FP64), ||r||
     launch_spmv<double2>(P, rowptr, col, A, x, r, b, nullptr, npr, s);
-    PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r, P.n, npart), k_norm_final<K><<<1, 32, 0, s>>>(npart, nb, rnorm)));
+    PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r, P.n, npart), k_norm_final<K><<<1, 32 * K, 0, s>>>(npart, nb, rnorm)));
     PG_LAUNCH_CHECK();
     PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
     PG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -616,7 +635,7 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
                        k_dots_final<C, K><<<1, 1024, 0, s>>>(dpart, nb, j, m, st, coef, pass, ctl),
                        k_update<C, K><<<nb, kThreads, 0, s>>>(V, stride, w, P.n, j, coef, st, pass, npart, ctl)));
       }
-      PG_KSWITCH(k, (k_givens<K><<<1, 32, 0, s>>>(npart, nb, j, m, st, ctl, j == steps - 1)));
+      PG_KSWITCH(k, (k_givens<K><<<1, 32 * K, 0, s>>>(npart, nb, j, m, st, ctl, j == steps - 1)));
     }
     PG_LAUNCH_CHECK();
     PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
@@ -652,6 +671,547 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
     res->status = status;
   }
   if (status == PG_ERR_NOT_CONVERGED) pg_set_error("pg_gmres: max_it reached before rtol");
+  return status;
+}
+
+
+// ============================================================================
+// COCG: conjugate orthogonal CG for complex-symmetric A (A^T = A, not
+// Hermitian), the short-recurrence Krylov method for the complex symmetric
+// systems of frequency-domain edge-element EM.  Jacobi enters as a symmetric
+// scaling  At = S A S,  S = D^-1/2  (complex principal square root), which
+// keeps At complex symmetric; the iteration solves At y = S r and x += S y.
+// The recurrence works in the Arnoldi-equivalent "compute" precision (complex
+// 128 or 64).  At every host check (every `check_every` iterations) the FP64
+// true residual  r = b - A x  replaces the recurrence residual (reliable
+// update: the search direction p is kept), and convergence is decided on it.
+// Per iteration: SpMV fused with mu = p^T q; alpha; y += alpha p, r -= alpha q
+// fused with rho = r^T r and the true-residual weight sum |r_i|^2 |D_i|; beta;
+// p = r + beta p.  Reductions are fixed-order (deterministic).
+// ============================================================================
+
+struct CgState {
+  double2 rho;     // r^T r (bilinear)
+  double2 alpha, beta;
+  double target;   // absolute true-residual target
+  double res;      // recurrence estimate of the true residual
+  double res0;     // true residual at the start of this cycle
+  int active;      // iterating (not converged)
+  int its;
+  int breakdown;
+  int beta_iter;   // launch index whose beta is current (p is updated once per beta)
+};
+
+struct CgCtl {
+  int any_active;      // some RHS still iterating in this cycle
+  int nonfinite;
+  unsigned counter;    // last-block-done counter (reset by the last block)
+  int pad;
+};
+
+template <typename C>
+__device__ __forceinline__ double2 bilin(C a, C b) {  // a*b (no conjugate) in double
+  const double2 x = to_d(a), y = to_d(b);
+  return make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+}
+
+// Every block publishes its partial; the block that arrives last (atomic
+// ticket) reduces all partials in block order - a fixed order, so the result
+// does not depend on which block is last.  Nothing waits: no spin.
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return last;
+}
+
+// block-wide fixed-order sum of partial[b * K + rhs] over b, per rhs (K <= 32)
+template <int K>
+__device__ double2 sum_partials(const double2* partial, int nblocks, int rhs, double2* smem) {
+  // thread t handles rhs = t % K, blocks b = t / K, t / K + 256 / K, ...
+  const int my_rhs = threadIdx.x % K;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int b = threadIdx.x / K; b < nblocks; b += kThreads / K) acc = dadd(acc, __ldcg(partial + (int64_t)b * K + my_rhs));
+  block_reduce_rhs<K>(acc, smem, smem + (kThreads / 32) * K);
+  const double2 out = smem[(kThreads / 32) * K + rhs];
+  __syncthreads();
+  return out;
+}
+
+// q = At p (k = 1, G lanes per row), partial mu = p^T q; last block: alpha
+template <typename C, int G>
+__global__ void __launch_bounds__(kThreads) k_cg_spmv1(const int64_t* __restrict__ rowptr,
+                                                       const int32_t* __restrict__ col, const C* __restrict__ val,
+                                                       int64_t n, const C* __restrict__ pv, C* __restrict__ q,
+                                                       double2* partial, CgState* st, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  double2 mu = make_double2(0.0, 0.0);
+  for (int64_t rw = warp_base; rw < n; rw += groups) {
+    const int64_t r = rw + (gid - warp_base);
+    const bool valid = r < n;
+    C acc = czero<C>();
+    if (valid) {
+      const int64_t e = rowptr[r + 1];
+      for (int64_t k = rowptr[r] + lane; k < e; k += G) acc = cfma(val[k], pv[col[k]], acc);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) acc = cadd(acc, shfl_xor(acc, off));
+    if (valid && lane == 0) {
+      q[r] = acc;
+      mu = dadd(mu, bilin(pv[r], acc));
+    }
+  }
+  block_reduce_rhs<1>(mu, smem, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) {
+    const double2 m = sum_partials<1>(partial, gridDim.x, 0, smem);
+    if (threadIdx.x == 0) {
+      CgState& S = st[0];
+      if (S.active) {
+        if (m.x == 0.0 && m.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.alpha = make_double2(0.0, 0.0);
+        } else {
+          S.alpha = ddiv(S.rho, m);
+        }
+      } else {
+        S.alpha = make_double2(0.0, 0.0);
+      }
+      ctl->counter = 0;
+    }
+  }
+}
+
+// q = At p for k > 1 RHS (thread per (row, rhs)), partial mu; last block: alpha
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_cg_spmm(const int64_t* __restrict__ rowptr,
+                                                      const int32_t* __restrict__ col, const C* __restrict__ val,
+                                                      int64_t n, const C* __restrict__ pv, C* __restrict__ q,
+                                                      double2* partial, CgState* st, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int rhs = threadIdx.x % K;
+  const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / K;
+  double2 mu = make_double2(0.0, 0.0);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; r < n; r += rows_per_pass) {
+    C acc = czero<C>();
+    const int64_t e = rowptr[r + 1];
+    for (int64_t k = rowptr[r]; k < e; ++k) acc = cfma(val[k], pv[(int64_t)col[k] * K + rhs], acc);
+    q[r * K + rhs] = acc;
+    mu = dadd(mu, bilin(pv[r * K + rhs], acc));
+  }
+  block_reduce_rhs<K>(mu, smem, partial + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) {
+    const double2 m = sum_partials<K>(partial, gridDim.x, threadIdx.x < K ? threadIdx.x : 0, smem);
+    if (threadIdx.x < K) {
+      CgState& S = st[threadIdx.x];
+      if (S.active) {
+        if (m.x == 0.0 && m.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.alpha = make_double2(0.0, 0.0);
+        } else {
+          S.alpha = ddiv(S.rho, m);
+        }
+      } else {
+        S.alpha = make_double2(0.0, 0.0);
+      }
+    }
+    if (threadIdx.x == 0) ctl->counter = 0;
+  }
+}
+
+// y += alpha p ; r -= alpha q ; partials rho = r^T r, w = sum |r|^2 |D|.
+// Last block: beta, residual estimate, activity; the cycle stops for every
+// RHS when one needs a reliable update (estimate dropped below delta * res0
+// or grew above 1e3 * res0), or when all have converged.
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_cg_update(C* __restrict__ y, C* __restrict__ r,
+                                                        const C* __restrict__ pv, const C* __restrict__ q,
+                                                        const typename Real<C>::T* __restrict__ wd, int64_t n,
+                                                        CgState* st, double2* prho, double2* pw, CgCtl* ctl,
+                                                        int iter, double delta) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ C al[kMaxK];
+  if (threadIdx.x < K) al[threadIdx.x] = cfrom<C>(st[threadIdx.x].alpha);
+  __syncthreads();
+  const int rhs = threadIdx.x % K;
+  const C a = al[rhs];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  typedef typename Real<C>::T R;
+  R rr = 0, ri = 0, ww = 0;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const C pe = pv[e], qe = q[e];
+    C ye = y[e], re = r[e];
+    ye = cfma(a, pe, ye);
+    re.x -= a.x * qe.x - a.y * qe.y;
+    re.y -= a.x * qe.y + a.y * qe.x;
+    y[e] = ye;
+    r[e] = re;
+    rr += re.x * re.x - re.y * re.y;
+    ri += 2 * re.x * re.y;
+    ww += (re.x * re.x + re.y * re.y) * wd[e / K];
+  }
+  block_reduce_rhs<K>(make_double2((double)rr, (double)ri), smem, prho + (int64_t)blockIdx.x * K);
+  block_reduce_rhs<K>(make_double2((double)ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) {
+    const int my = threadIdx.x < K ? threadIdx.x : 0;
+    const double2 rho = sum_partials<K>(prho, gridDim.x, my, smem);
+    const double2 w = sum_partials<K>(pw, gridDim.x, my, smem);
+    __shared__ int any, stop;
+    if (threadIdx.x == 0) { any = 0; stop = 0; }
+    __syncthreads();
+    if (threadIdx.x < K) {
+      CgState& S = st[threadIdx.x];
+      if (S.active) {
+        S.beta_iter = iter;
+        S.its += 1;
+        S.res = sqrt(w.x);
+        if (!isfinite(S.res)) ctl->nonfinite = 1;
+        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.beta = make_double2(0.0, 0.0);
+        } else {
+          S.beta = ddiv(rho, S.rho);
+        }
+        S.rho = rho;
+        if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
+        else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
+      } else {
+        S.beta = make_double2(0.0, 0.0);
+      }
+      if (S.active) atomicOr(&any, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      ctl->any_active = any && !stop;
+      ctl->counter = 0;
+    }
+  }
+}
+
+// p = r + beta p for every RHS whose beta was computed in this launch
+// (iteration `iter`); RHS that were already inactive keep their p.
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_cg_pupdate(C* __restrict__ pv, const C* __restrict__ r, int64_t n,
+                                                         const CgState* st, int iter) {
+  __shared__ C bt[kMaxK];
+  __shared__ int use[kMaxK];
+  if (threadIdx.x < K) {
+    bt[threadIdx.x] = cfrom<C>(st[threadIdx.x].beta);
+    use[threadIdx.x] = st[threadIdx.x].beta_iter == iter;
+  }
+  __syncthreads();
+  int anyuse = 0;
+  for (int i = 0; i < K; ++i) anyuse |= use[i];
+  if (!anyuse) return;
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    if (use[e % K]) pv[e] = cfma(bt[e % K], pv[e], r[e]);
+}
+
+// S = D^-1/2 (principal root), wd = |D|, At = S A S in precision C
+__global__ void k_cg_scaling(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n, double2* S,
+                             double* wd, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 d = make_double2(0.0, 0.0);
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      if (col[k] == r) d = val[k];
+    const double ad = sqrt(dabs2(d));
+    if (ad == 0.0) {
+      *status = PG_ERR_BREAKDOWN;
+      S[r] = make_double2(1.0, 0.0);
+      wd[r] = 1.0;
+      continue;
+    }
+    const double sr = sqrt(0.5 * (ad + d.x));
+    double si = sqrt(fmax(0.0, 0.5 * (ad - d.x)));
+    if (d.y < 0) si = -si;
+    S[r] = ddiv(make_double2(1.0, 0.0), make_double2(sr, si));
+    wd[r] = ad;
+  }
+}
+
+template <typename C>
+__global__ void k_cg_scale_matrix(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n,
+                                  const double2* S, C* out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 sr = S[r];
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) out[k] = cfrom<C>(cmul(sr, cmul(val[k], S[col[k]])));
+  }
+}
+
+template <typename C>
+__global__ void k_cg_wd(const double* wd, int64_t n, typename Real<C>::T* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (typename Real<C>::T)wd[i];
+}
+
+// r~ = S r64 (cast), y = 0 ; first cycle also p = r~ ; partial rho
+template <typename C, int K>
+__global__ void k_cg_start(const double2* __restrict__ r64, const double2* __restrict__ S, int64_t n, C* r, C* y, C* pv,
+                           int set_p, double2* prho) {
+  __shared__ double2 smem[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double2 rho = make_double2(0.0, 0.0);
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const C v = cfrom<C>(cmul(S[e / K], r64[e]));
+    r[e] = v;
+    y[e] = czero<C>();
+    if (set_p) pv[e] = v;
+    rho = dadd(rho, bilin(v, v));
+  }
+  block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
+}
+
+template <int K>
+__global__ void k_cg_cycle_init(const double2* prho, int nblocks, CgState* st, const double* rnorm,
+                                const double* target, const int* want, CgCtl* ctl, int first) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, rhs = threadIdx.x >> 5;
+  if (rhs < K) {
+    double2 rho = make_double2(0.0, 0.0);
+    for (int b = lane; b < nblocks; b += 32) rho = dadd(rho, prho[(int64_t)b * K + rhs]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) rho = dadd(rho, shfl_xor(rho, off));
+    if (lane == 0) {
+      CgState& S = st[rhs];
+      if (first) {
+        S.its = 0;
+        S.breakdown = 0;
+        S.beta_iter = 0;
+      }
+      S.rho = rho;
+      S.target = target[rhs];
+      S.res = rnorm[rhs];
+      S.res0 = rnorm[rhs];
+      S.active = want[rhs] && rnorm[rhs] > 0.0;
+      S.alpha = S.beta = make_double2(0.0, 0.0);
+      if (S.active) atomicOr(&any, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any;
+    ctl->nonfinite = 0;
+    ctl->counter = 0;
+  }
+}
+
+// x64 += S y
+template <typename C, int K>
+__global__ void k_cg_xupdate(const C* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    x[e] = dadd(x[e], cmul(S[e / K], to_d(y[e])));
+}
+
+size_t cg_layout(const Plan& P, size_t* off /* 14 */) {
+  size_t o = 0;
+  auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
+  const size_t rsize = P.csize / 2;
+  put(0, P.nnz * P.csize);                      // At
+  put(1, sizeof(double2) * P.n);                // S
+  put(2, sizeof(double) * P.n);                 // |D| (f64)
+  put(3, rsize * P.n);                          // |D| (compute precision)
+  put(4, P.csize * P.n * P.k);                  // p
+  put(5, P.csize * P.n * P.k);                  // q
+  put(6, P.csize * P.n * P.k);                  // r
+  put(7, P.csize * P.n * P.k);                  // y
+  put(8, sizeof(double2) * P.n * P.k);          // r64
+  put(9, sizeof(double2) * (size_t)P.nb * P.k * 3);  // partials (mu/rho, w)
+  put(10, sizeof(CgState) * P.k);
+  put(11, sizeof(CgCtl));
+  put(12, sizeof(double) * P.k * 3);            // rnorm, target, (spare)
+  put(13, sizeof(int) * (P.k + 1));             // want, status
+  return o;
+}
+
+template <typename C>
+void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const C* val, const C* pv, C* q,
+                    double2* partial, CgState* st, CgCtl* ctl, int64_t npr, int grid, cudaStream_t s) {
+  switch (P.k) {
+    case 1:
+      switch (LanesPerRow<C>::pick(npr)) {
+        case 32: k_cg_spmv1<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+        case 16: k_cg_spmv1<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+        case 8: k_cg_spmv1<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+        default: k_cg_spmv1<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+      }
+      break;
+    case 2: k_cg_spmm<C, 2><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+    case 4: k_cg_spmm<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+    case 8: k_cg_spmm<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+    case 16: k_cg_spmm<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+    case 32: k_cg_spmm<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+  }
+}
+
+template <typename C>
+int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
+             const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
+  typedef typename Real<C>::T R;
+  size_t off[14];
+  cg_layout(P, off);
+  C* At = reinterpret_cast<C*>(ws + off[0]);
+  double2* S = reinterpret_cast<double2*>(ws + off[1]);
+  double* wd64 = reinterpret_cast<double*>(ws + off[2]);
+  R* wd = reinterpret_cast<R*>(ws + off[3]);
+  C* pv = reinterpret_cast<C*>(ws + off[4]);
+  C* q = reinterpret_cast<C*>(ws + off[5]);
+  C* r = reinterpret_cast<C*>(ws + off[6]);
+  C* y = reinterpret_cast<C*>(ws + off[7]);
+  double2* r64 = reinterpret_cast<double2*>(ws + off[8]);
+  double2* part = reinterpret_cast<double2*>(ws + off[9]);
+  double2* part2 = part + (size_t)P.nb * P.k;
+  CgState* st = reinterpret_cast<CgState*>(ws + off[10]);
+  CgCtl* ctl = reinterpret_cast<CgCtl*>(ws + off[11]);
+  double* rnorm = reinterpret_cast<double*>(ws + off[12]);
+  double* target = rnorm + P.k;
+  int* want = reinterpret_cast<int*>(ws + off[13]);
+  int* dstatus = want + P.k;
+  const int k = P.k, nb = P.nb;
+  const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
+  const int spmv_grid = 152 * 16;
+  if (spmv_grid > nb) return PG_ERR_ARG;  // partial buffers are sized by nb
+
+  PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd64, dstatus);
+  k_cg_scale_matrix<C><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
+  k_cg_wd<C><<<pg_blocks(P.n, 256), 256, 0, s>>>(wd64, P.n, wd);
+  PG_LAUNCH_CHECK();
+  std::vector<double> bnorm(k), rn(k), tgt(k);
+  std::vector<int> wnt(k);
+  PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, part), k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+  PG_LAUNCH_CHECK();
+  PG_CUDA_TRY(cudaMemcpyAsync(bnorm.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  int hstatus = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hstatus) {
+    pg_set_error("pg_cocg: zero diagonal entry (Jacobi scaling undefined)");
+    return PG_ERR_BREAKDOWN;
+  }
+  const char* mon_env = getenv("PG_KSP_MONITOR");
+  const bool monitor = mon_env && mon_env[0] && mon_env[0] != '0';
+  int64_t its = 0, checks = 0;
+  int status = PG_OK;
+  const int64_t max_it = o->max_it > 0 ? o->max_it : 100000;
+  int chunk = o->check_every > 0 ? o->check_every : 50;
+  bool first = true;
+  int64_t launch_iter = 1;
+  for (;;) {
+    launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+    PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
+                   k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+    PG_LAUNCH_CHECK();
+    PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    Ctl hctl;
+    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!first && hctl.nonfinite) {
+      pg_set_error("pg_cocg: non-finite residual");
+      status = PG_ERR_NONFINITE;
+      break;
+    }
+    bool all = true;
+    for (int i = 0; i < k; ++i) {
+      if (monitor)
+        fprintf(stderr, "pg_cocg: check %lld its %lld rhs %d true ||r||/||b|| = %.6e\n", (long long)checks,
+                (long long)its, i, bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0);
+      if (!isfinite(rn[i])) {
+        pg_set_error("pg_cocg: non-finite residual");
+        status = PG_ERR_NONFINITE;
+      }
+      const double tb = o->rtol * bnorm[i];
+      const bool ok = rn[i] <= tb || bnorm[i] == 0.0;
+      wnt[i] = ok ? 0 : 1;
+      tgt[i] = 0.5 * tb;
+      if (!ok) all = false;
+    }
+    if (status || all) break;
+    if (its >= max_it) {
+      status = PG_ERR_NOT_CONVERGED;
+      break;
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    PG_KSWITCH(k, (k_cg_start<C, K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part),
+                   k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    first = false;
+    const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
+    const double delta = P.prec ? 0.1 : 0.0;
+    for (int it = 0; it < steps; ++it) {
+      const int iter = (int)(launch_iter + it);
+      launch_cg_spmv<C>(P, rowptr, col, At, pv, q, part, st, ctl, npr, spmv_grid, s);
+      PG_KSWITCH(k, (k_cg_update<C, K><<<nb, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
+                     k_cg_pupdate<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter)));
+    }
+    PG_LAUNCH_CHECK();
+    launch_iter += steps;
+    PG_KSWITCH(k, (k_cg_xupdate<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    std::vector<int> hits(k);
+    std::vector<int> hbrk(k);
+    for (int i = 0; i < k; ++i) {
+      PG_CUDA_TRY(cudaMemcpyAsync(&hits[i], &st[i].its, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaMemcpyAsync(&hbrk[i], &st[i].breakdown, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    int used = 0;
+    for (int i = 0; i < k; ++i) used = hits[i] > used ? hits[i] : used;
+    const int64_t cycle_its = used - its;
+    its = used;
+    ++checks;
+    bool brk = false;
+    for (int i = 0; i < k; ++i) brk = brk || hbrk[i];
+    if (brk) {
+      pg_set_error("pg_cocg: breakdown (p^T A p = 0 or r^T r = 0)");
+      status = PG_ERR_BREAKDOWN;
+      // still report the residual of the last iterate below
+      launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+      PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
+                     k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+      PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaStreamSynchronize(s));
+      break;
+    }
+    if (P.prec) {
+      // cycles end on-device at the reliable-update trigger; size the next
+      // launch batch from this cycle's length to limit no-op launches
+      int64_t c2 = cycle_its + cycle_its / 4 + 8;
+      chunk = (int)(c2 < 16 ? 16 : (c2 > 2000 ? 2000 : c2));
+    } else if (chunk < 400) {
+      chunk *= 2;
+    }
+  }
+  double worst = 0.0;
+  for (int i = 0; i < k; ++i) {
+    const double rr = bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0;
+    if (relres_out) relres_out[i] = rr;
+    worst = rr > worst ? rr : worst;
+  }
+  if (res) {
+    res->iterations = its;
+    res->restarts = checks;
+    res->relres = worst;
+    res->status = status;
+  }
+  if (status == PG_ERR_NOT_CONVERGED) pg_set_error("pg_cocg: max_it reached before rtol");
   return status;
 }
 
@@ -729,4 +1289,49 @@ extern "C" int pg_spmv_c(const int64_t* rowptr, const int32_t* col, const float*
                       reinterpret_cast<float2*>(y), nullptr, nullptr, 43, pg_stream(stream));
   PG_LAUNCH_CHECK();
   return PG_OK;
+}
+
+extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->max_it = 100000;
+  o->rtol = 1e-8;
+  o->precision = 0;
+  o->check_every = 50;
+}
+
+static Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
+  int nb = pick_blocks(n, nrhs);
+  if (nb < 152 * 16) nb = 152 * 16;  // partials also hold the SpMV's per-block sums
+  return Plan{n, nnz, nrhs, 1, o->precision, nb, o->precision ? sizeof(float2) : sizeof(double2)};
+}
+
+extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
+  if (!opts || n < 1 || !valid_k(nrhs)) return 0;
+  Plan P = cg_plan(n, nnz, nrhs, opts);
+  size_t off[14];
+  return cg_layout(P, off) + 256;
+}
+
+extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
+                       const double* b, double* x, int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result,
+                       double* relres_per_rhs, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!opts || !rowptr || !col || !vals || !b || !x || n < 1 || nnz < n || !valid_k(nrhs) || !(opts->rtol > 0.0) ||
+      (opts->precision != 0 && opts->precision != 1)) {
+    pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1)");
+    return PG_ERR_ARG;
+  }
+  const size_t need = pg_cocg_workspace_bytes(n, nnz, nrhs, opts);
+  if (!workspace || workspace_bytes < need) {
+    pg_set_error("pg_cocg: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  char* ws = reinterpret_cast<char*>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+  Plan P = cg_plan(n, nnz, nrhs, opts);
+  cudaStream_t s = pg_stream(stream);
+  const double2* A = reinterpret_cast<const double2*>(vals);
+  const double2* bb = reinterpret_cast<const double2*>(b);
+  double2* xx = reinterpret_cast<double2*>(x);
+  if (P.prec == 0) return run_cocg<double2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
+  return run_cocg<float2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
 }

@@ -162,6 +162,17 @@ class DeviceMesh:
         self.col = torch.empty(self.nnz, dtype=torch.int32, device=dev)
         _lib.call("pg_pattern_columns", _p(self.members), _p(self.pair_start), _p(self.pair_colstart), self.n_pairs,
                   _p(self.elemsE), _p(self.elemsF), T, self.nE, self.nF, p, _p(self.rowptr), _p(self.col), _s())
+        # symmetric work list for the fused assembly
+        self.pair_partner = torch.empty(self.n_pairs, dtype=torch.int32, device=dev)
+        items = torch.empty(self.nnz, dtype=torch.int64, device=dev)
+        nit = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = _ws(_lib.query("pg_pattern_items_workspace_bytes", self.n_pairs), dev)
+        _lib.call("pg_pattern_items", _p(self.members), _p(self.pair_start), self.n_pairs, _p(self.elemsE),
+                  _p(self.elemsF), T, self.nE, self.nF, p, _p(self.pair_partner), _p(items), _p(nit), _p(ws),
+                  ws.numel(), _s())
+        self.n_items = int(nit.item())
+        self.items = items[:self.n_items].contiguous()
+        del items, ws
 
     # ---------------------------------------------------------------- per-model work
     def sigma_tensor(self, sigma):
@@ -202,8 +213,9 @@ class DeviceMesh:
             if coef is None:
                 coef = self.element_coefficients(sigma, frequency)
             _lib.call("pg_assemble_fused", _p(coef), _p(self.tuple_of_elem), _p(self.tables), _p(self.members),
-                      _p(self.pair_start), _p(self.pair_colstart), self.n_pairs, _p(self.elemsE), _p(self.elemsF),
-                      self.T, self.nE, self.nF, self.p, _p(self.rowptr), _p(vals), _s())
+                      _p(self.pair_start), _p(self.pair_colstart), _p(self.pair_partner), _p(self.items), self.n_items,
+                      self.n_pairs, _p(self.elemsE), _p(self.elemsF), self.T, self.nE, self.nF, self.p, _p(self.rowptr),
+                      _p(vals), _s())
         else:
             M, K = self.elemental_matrices(sigma)
             omu = 2.0 * math.pi * float(frequency) * MU0
@@ -255,26 +267,41 @@ class DeviceMesh:
         return vals, b
 
     def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True):
-        """Right-Jacobi GMRES; b complex128 [N] or [N, k] (k in 1,2,4,8,16,32)."""
+              raise_on_fail=True, ksp="gmres", check_every=50):
+        """Solve A x = b; b complex128 [N] or [N, k] (k in 1,2,4,8,16,32).
+
+        ksp="gmres": right-Jacobi restarted GMRES(restart) (PETSc -ksp_type gmres -pc_type jacobi);
+        ksp="cocg":  Jacobi-scaled COCG for the complex-symmetric A.
+        precision="fp64" (complex128) or "mixed" (complex64 recurrence, complex128 residual/refinement).
+        Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
+        """
         nrhs = 1 if b.ndim == 1 else int(b.shape[1])
         x = torch.zeros_like(b) if x0 is None else x0.clone()
-        o = _lib.GmresOpts()
-        _lib.load().pg_gmres_default_opts(ctypes.byref(o))
-        o.restart, o.max_it, o.rtol = int(restart), int(max_it), float(rtol)
-        o.precision = {"fp64": 0, "mixed": 1}[precision]
-        o.reorth = 1 if reorth else 0
+        prec = {"fp64": 0, "mixed": 1}[precision]
         res = _lib.GmresResult()
         rr = (ctypes.c_double * nrhs)()
-        nbytes = _lib.query("pg_gmres_workspace_bytes", self.N, self.nnz, nrhs, ctypes.byref(o))
+        lib = _lib.load()
+        if ksp == "gmres":
+            o = _lib.GmresOpts()
+            lib.pg_gmres_default_opts(ctypes.byref(o))
+            o.restart, o.max_it, o.rtol, o.precision, o.reorth = int(restart), int(max_it), float(rtol), prec, int(reorth)
+            nbytes = _lib.query("pg_gmres_workspace_bytes", self.N, self.nnz, nrhs, ctypes.byref(o))
+            fn = lib.pg_gmres
+        elif ksp == "cocg":
+            o = _lib.CocgOpts()
+            lib.pg_cocg_default_opts(ctypes.byref(o))
+            o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), prec, int(check_every)
+            nbytes = _lib.query("pg_cocg_workspace_bytes", self.N, self.nnz, nrhs, ctypes.byref(o))
+            fn = lib.pg_cocg
+        else:
+            raise ValueError(f"unknown ksp type {ksp!r} (gmres, cocg)")
         ws = _ws(nbytes + 256, self.device)
-        st = _lib.load().pg_gmres(_p(self.rowptr), _p(self.col), _p(vals), self.N, self.nnz, _p(b.contiguous()), _p(x),
-                                  nrhs, ctypes.byref(o), ctypes.byref(res), ctypes.cast(rr, ctypes.c_void_p), _p(ws),
-                                  ws.numel(), _s())
+        st = fn(_p(self.rowptr), _p(self.col), _p(vals), self.N, self.nnz, _p(b.contiguous()), _p(x), nrhs,
+                ctypes.byref(o), ctypes.byref(res), ctypes.cast(rr, ctypes.c_void_p), _p(ws), ws.numel(), _s())
         info = SolveInfo(int(res.iterations), int(res.restarts), float(res.relres), int(st), list(rr))
         if st != 0 and (raise_on_fail or st != -7):
-            msg = _lib.load().pg_last_error()
-            raise _lib.PetgemError("pg_gmres", st, msg.decode() if msg else "")
+            msg = lib.pg_last_error()
+            raise _lib.PetgemError(f"pg_{ksp}", st, msg.decode() if msg else "")
         return x, info
 
     def receiver_fields(self, x, receivers, frequency):

@@ -114,8 +114,9 @@ def test_pec_matches_oracle():
     assert rel_norm(b.cpu().numpy(), bo) < ELEM_TOL
 
 
+@pytest.mark.parametrize("ksp", ["gmres", "cocg"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_solve_and_receivers_vs_reference(precision):
+def test_solve_and_receivers_vs_reference(precision, ksp):
     g = load("pipeline_n3.npz")
     pts, tets, sigma = g["points"], g["tets"], g["sigma"]
     src = json.loads(str(g["src"]))
@@ -125,7 +126,7 @@ def test_solve_and_receivers_vs_reference(precision):
     assert se == int(g["src_elem"])
     m.apply_pec(vals, b)
     assert rel_norm(b.cpu().numpy(), g["b"]) < ELEM_TOL
-    x, info = m.solve(vals, b, rtol=1e-10, precision=precision)
+    x, info = m.solve(vals, b, rtol=1e-10, precision=precision, ksp=ksp)
     assert info.relres <= 1e-10
     A = _csr(m, vals)
     xn = x.cpu().numpy()
@@ -148,12 +149,13 @@ def test_multi_rhs_matches_single():
         m.apply_pec(vals.clone(), b)                     # zero the PEC entries of b
         bs.append(b)
     B = torch.stack(bs, 1).contiguous()
-    for prec in ("fp64", "mixed"):
-        X, info = m.solve(vals, B, rtol=1e-9, precision=prec)
-        assert max(info.relres_per_rhs) <= 1e-9
-        for k in range(4):
-            xk, _ = m.solve(vals, bs[k], rtol=1e-11)
-            assert rel_norm(X[:, k].cpu().numpy(), xk.cpu().numpy()) < 1e-6
+    ref = [m.solve(vals, bs[k], rtol=1e-11)[0].cpu().numpy() for k in range(4)]
+    for ksp in ("gmres", "cocg"):
+        for prec in ("fp64", "mixed"):
+            X, info = m.solve(vals, B, rtol=1e-9, precision=prec, ksp=ksp)
+            assert max(info.relres_per_rhs) <= 1e-9
+            for k in range(4):
+                assert rel_norm(X[:, k].cpu().numpy(), ref[k]) < 1e-6
 
 
 def test_gmres_maxit_status_is_returned():
@@ -167,6 +169,8 @@ def test_gmres_maxit_status_is_returned():
     assert info.status == -7 and info.iterations <= 30
     with pytest.raises(_lib.PetgemError):
         m.solve(vals, b, rtol=1e-14, max_it=5)
+    x, info = m.solve(vals, b, rtol=1e-14, max_it=5, raise_on_fail=False, ksp="cocg", check_every=5)
+    assert info.status == -7 and info.iterations == 5
 
 
 def test_source_outside_mesh_raises():
