@@ -140,6 +140,23 @@ size_t pg_boundary_workspace_bytes(int64_t nE, int64_t nF);
 int pg_boundary_dofs(const int32_t* face_nelem, const int32_t* facesE, int64_t nE, int64_t nF, int p, int32_t* bnd,
                      int64_t* n_bnd, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Single-function building blocks (used by the drop-in mesh entry points):
+ *  - pg_faces_edges: facesE [nF*3] from elemsF/elemsE, lowest-index owner
+ *    element (petgem/mesh.py:92 computeFacesEdges); owner_ws int32 [nF].
+ *  - pg_face_counts: elements sharing each face (1 = boundary,
+ *    petgem/mesh.py:149 computeBoundaryFaces).
+ *  - pg_flag_edges_of_pairs: flags [nE] = 1 for edges whose sorted node pair
+ *    appears in pairs [n_pairs*2] (petgem/mesh.py:224 computeBoundaryEdges).
+ *  - pg_select_equal: ascending indices i with values[i] == target. */
+int pg_faces_edges(const int32_t* elemsF, const int32_t* elemsE, int64_t n_elems, int64_t nF, int32_t* facesE,
+                   int32_t* owner_ws, int32_t* status, void* stream);
+int pg_face_counts(const int32_t* elemsF, int64_t n_elems, int64_t nF, int32_t* face_nelem, void* stream);
+int pg_flag_edges_of_pairs(const int32_t* edgesNodes, int64_t nE, const int32_t* pairs, int64_t n_pairs,
+                           int32_t* flags, void* stream);
+size_t pg_select_workspace_bytes(int64_t n);
+int pg_select_equal(const int32_t* values, int64_t n, int32_t target, int32_t* out, int64_t* count,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------
  * CSR pattern and value assembly (replaces petgem/parallel.py:150
  * createParallelMatrix + the Mat.setValues(ADD_VALUES)/assemblyBegin/End
@@ -180,16 +197,20 @@ int pg_assemble_values(const double* M, const double* K, const int32_t* members,
 int pg_element_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t n_elems,
                             double omega_mu, double* coef, int32_t* status, void* stream);
 
-size_t pg_pattern_items_workspace_bytes(int64_t n_pairs);
+size_t pg_pattern_items_workspace_bytes(int64_t n_pairs, int64_t max_items);
 
 /* Work list of the symmetric fused assembly: for every entity pair (a, b)
  * with a <= b, one item per entry of its upper block (all na*nb entries when
  * a < b, the na(na+1)/2 upper entries when a == b), encoded (pair << 12) |
- * entry; pair_partner[g] = index of the transposed pair (b, a).
- * Out: pair_partner int32 [n_pairs]; items int64 [cap nnz]; n_items int64 [1]. */
+ * entry, ordered by the pair's member count (stable) so that neighbouring
+ * items run equal loop trip counts; pair_partner[g] = index of the
+ * transposed pair (b, a).  Synchronises the stream once (item count).
+ * Out: pair_partner int32 [n_pairs]; items int64 [max_items >= count];
+ * n_items int64 [1]. */
 int pg_pattern_items(const int32_t* members, const int32_t* pair_start, int64_t n_pairs, const int32_t* elemsE,
-                     const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, int32_t* pair_partner,
-                     int64_t* items, int64_t* n_items, void* workspace, size_t workspace_bytes, void* stream);
+                     const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, int64_t max_items,
+                     int32_t* pair_partner, int64_t* items, int64_t* n_items, void* workspace,
+                     size_t workspace_bytes, void* stream);
 
 /* Fused elemental + assembly: vals complex128 [nnz] without materialising
  * elemental matrices.  Each item sums 12 FMAs per member element (element

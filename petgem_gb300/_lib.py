@@ -55,14 +55,19 @@ SIGNATURES = {
     "pg_element_orientation": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _P]),
     "pg_boundary_workspace_bytes": (_SZ, [_I64, _I64]),
     "pg_boundary_dofs": (_INT, [_P, _P, _I64, _I64, _INT, _P, _P, _P, _SZ, _P]),
+    "pg_faces_edges": (_INT, [_P, _P, _I64, _I64, _P, _P, _P, _P]),
+    "pg_face_counts": (_INT, [_P, _I64, _I64, _P, _P]),
+    "pg_flag_edges_of_pairs": (_INT, [_P, _I64, _P, _I64, _P, _P]),
+    "pg_select_workspace_bytes": (_SZ, [_I64]),
+    "pg_select_equal": (_INT, [_P, _I64, _INT, _P, _P, _P, _SZ, _P]),
     "pg_pattern_local_entities": (_INT, [_INT]),
     "pg_pattern_workspace_bytes": (_SZ, [_I64, _I64, _I64, _INT]),
     "pg_pattern_build": (_INT, [_P, _P, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "pg_pattern_columns": (_INT, [_P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P]),
     "pg_assemble_values": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _D, _P, _P]),
     "pg_element_coefficients": (_INT, [_P, _P, _P, _I64, _D, _P, _P, _P]),
-    "pg_pattern_items_workspace_bytes": (_SZ, [_I64]),
-    "pg_pattern_items": (_INT, [_P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _SZ, _P]),
+    "pg_pattern_items_workspace_bytes": (_SZ, [_I64, _I64]),
+    "pg_pattern_items": (_INT, [_P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _I64, _P, _P, _P, _P, _SZ, _P]),
     "pg_assemble_fused": (_INT, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P,
                                  _P]),
     "pg_apply_pec": (_INT, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P]),

@@ -284,6 +284,23 @@ __global__ void k_items(const int32_t* n_items, const int32_t* item_start, int64
 
 __global__ void k_store_i64(const int32_t* src, int64_t* dst) { *dst = *src; }
 
+// sort key of every item: member count of its pair
+__global__ void k_item_keys(const int64_t* items, const int32_t* n_items_dev, const int32_t* pair_start,
+                            uint64_t* keys, int32_t* vals) {
+  const int64_t n = *n_items_dev;
+  GRID_STRIDE(i, n) {
+    const int64_t g = items[i] >> 12;
+    const int32_t c = pair_start[g + 1] - pair_start[g];
+    keys[i] = (uint64_t)(c < 255 ? c : 255);
+    vals[i] = (int32_t)i;
+  }
+}
+
+__global__ void k_item_gather(const int64_t* items, const int32_t* n_items_dev, const int32_t* order, int64_t* out) {
+  const int64_t n = *n_items_dev;
+  GRID_STRIDE(i, n) out[i] = items[order[i]];
+}
+
 // fused symmetric values: one thread per item; members summed in element order,
 // 12 FMAs per member; the value goes to slot (a,b) and to its transpose (b,a).
 template <int P>
@@ -494,20 +511,23 @@ extern "C" int pg_element_coefficients(const double* nodes, const int32_t* elems
   return PG_OK;
 }
 
-extern "C" size_t pg_pattern_items_workspace_bytes(int64_t n_pairs) {
+extern "C" size_t pg_pattern_items_workspace_bytes(int64_t n_pairs, int64_t max_items) {
   return pg_align256(sizeof(int64_t) * n_pairs) + pg_align256(sizeof(int32_t) * (n_pairs + 1)) * 2 +
-         pg::scan_workspace_bytes(n_pairs + 1) + 1024;
+         pg::scan_workspace_bytes(n_pairs + 1) + pg_align256(sizeof(uint64_t) * max_items) +
+         pg_align256(sizeof(int32_t) * max_items) + pg_align256(sizeof(int64_t) * max_items) +
+         pg::sort_workspace_bytes(max_items) + 1024;
 }
 
 extern "C" int pg_pattern_items(const int32_t* members, const int32_t* pair_start, int64_t n_pairs,
                                 const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF,
-                                int p, int32_t* pair_partner, int64_t* items, int64_t* n_items, void* workspace,
-                                size_t workspace_bytes, void* stream) {
+                                int p, int64_t max_items, int32_t* pair_partner, int64_t* items, int64_t* n_items,
+                                void* workspace, size_t workspace_bytes, void* stream) {
   if (p < 1 || p > 6 || n_pairs < 1 || !members || !pair_start || !pair_partner || !items || !n_items) {
     pg_set_error("pg_pattern_items: bad argument");
     return PG_ERR_ARG;
   }
-  if (!workspace || workspace_bytes < pg_pattern_items_workspace_bytes(n_pairs)) {
+  if (max_items < 1 || max_items >= (1ll << 31) || !workspace ||
+      workspace_bytes < pg_pattern_items_workspace_bytes(n_pairs, max_items)) {
     pg_set_error("pg_pattern_items: workspace too small");
     return PG_ERR_WORKSPACE;
   }
@@ -520,14 +540,33 @@ extern "C" int pg_pattern_items(const int32_t* members, const int32_t* pair_star
   const size_t scan_b = pg::scan_workspace_bytes(n_pairs + 1);
   void* scan_ws = ar.take<char>(scan_b);
   int32_t* tot = ar.take<int32_t>(4);
-  if (!pair_key || !cnt || !start || !scan_ws || !tot) return PG_ERR_WORKSPACE;
+  uint64_t* ikeys = ar.take<uint64_t>(max_items);
+  int32_t* ivals = ar.take<int32_t>(max_items);
+  int64_t* itmp = ar.take<int64_t>(max_items);
+  const size_t sort_b = pg::sort_workspace_bytes(max_items);
+  void* sort_ws = ar.take<char>(sort_b);
+  if (!pair_key || !cnt || !start || !scan_ws || !tot || !ikeys || !ivals || !itmp || !sort_ws)
+    return PG_ERR_WORKSPACE;
   const unsigned gP = pg_blocks(n_pairs, 256);
   k_pair_keys_of<<<gP, 256, 0, s>>>(members, pair_start, n_pairs, elemsE, elemsF, E, pair_key, cnt);
   k_partner<<<gP, 256, 0, s>>>(pair_key, n_pairs, E, pair_partner);
   int st = pg::scan_exclusive_i32(cnt, start, n_pairs, tot, scan_ws, scan_b, s);
   if (st) return st;
-  k_items<<<gP, 256, 0, s>>>(cnt, start, n_pairs, items);
+  k_items<<<gP, 256, 0, s>>>(cnt, start, n_pairs, itmp);
   k_store_i64<<<1, 1, 0, s>>>(tot, n_items);
+  // bucket items by member count (stable), so warps see uniform loop trip counts
+  int32_t h_tot = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&h_tot, tot, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h_tot > max_items) {
+    pg_set_error("pg_pattern_items: max_items too small");
+    return PG_ERR_ARG;
+  }
+  const unsigned gI = pg_blocks(h_tot > 0 ? h_tot : 1, 256);
+  k_item_keys<<<gI, 256, 0, s>>>(itmp, tot, pair_start, ikeys, ivals);
+  st = pg::sort_pairs(ikeys, ivals, h_tot, 8, sort_ws, sort_b, s);
+  if (st) return st;
+  k_item_gather<<<gI, 256, 0, s>>>(itmp, tot, ivals, items);
   PG_LAUNCH_CHECK();
   return PG_OK;
 }

@@ -327,3 +327,130 @@ extern "C" int pg_boundary_dofs(const int32_t* face_nelem, const int32_t* facesE
   PG_LAUNCH_CHECK();
   return PG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Small building blocks behind the single-function mesh entry points.
+namespace {
+
+__global__ void k_owner_init(int32_t* owner, int64_t n) { GRID_STRIDE(i, n) owner[i] = 0x7fffffff; }
+
+__global__ void k_owner_min(const int32_t* elemsF, int64_t T, int64_t nF, int32_t* owner, int32_t* status) {
+  GRID_STRIDE(i, 4 * T) {
+    const int32_t f = elemsF[i];
+    if (f < 0 || f >= nF) { *status = PG_ERR_ARG; continue; }
+    atomicMin(&owner[f], (int32_t)i);   // i = 4 e + l: lowest element, then lowest local face
+  }
+}
+
+__global__ void k_faces_edges(const int32_t* owner, const int32_t* elemsE, int64_t nF, int32_t* facesE) {
+  GRID_STRIDE(f, nF) {
+    const int32_t v = owner[f];
+    if (v == 0x7fffffff) continue;
+    const int64_t e = v / 4;
+    const int l = v % 4;
+    for (int k = 0; k < 3; ++k) facesE[3 * f + k] = elemsE[6 * e + kFE[l][k]];
+  }
+}
+
+__global__ void k_face_counts(const int32_t* elemsF, int64_t T, int64_t nF, int32_t* cnt) {
+  GRID_STRIDE(i, 4 * T) {
+    const int32_t f = elemsF[i];
+    if (f >= 0 && f < nF) atomicAdd(&cnt[f], 1);
+  }
+}
+
+// pairs (sorted node pairs) -> flag[edge id] = 1 by binary search in the
+// lexicographically sorted edgesNodes table
+__global__ void k_flag_pairs(const int32_t* edgesNodes, int64_t nE, const int32_t* pairs, int64_t npairs,
+                             int32_t* flag) {
+  GRID_STRIDE(i, npairs) {
+    const int64_t a = pairs[2 * i], b = pairs[2 * i + 1];
+    int64_t lo = 0, hi = nE - 1;
+    while (lo <= hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      const int64_t ma = edgesNodes[2 * mid], mb = edgesNodes[2 * mid + 1];
+      if (ma == a && mb == b) { flag[mid] = 1; break; }
+      if (ma < a || (ma == a && mb < b)) lo = mid + 1; else hi = mid - 1;
+    }
+  }
+}
+
+__global__ void k_eq_flags(const int32_t* v, int64_t n, int32_t target, int32_t* flags) {
+  GRID_STRIDE(i, n) flags[i] = v[i] == target ? 1 : 0;
+}
+
+__global__ void k_compact(const int32_t* flags, const int32_t* pos, int64_t n, int32_t* out) {
+  GRID_STRIDE(i, n) if (flags[i]) out[pos[i]] = (int32_t)i;
+}
+
+}  // namespace
+
+extern "C" int pg_faces_edges(const int32_t* elemsF, const int32_t* elemsE, int64_t n_elems, int64_t nF,
+                              int32_t* facesE, int32_t* owner_ws, int32_t* status, void* stream) {
+  if (n_elems < 1 || nF < 1 || !elemsF || !elemsE || !facesE || !owner_ws || !status) {
+    pg_set_error("pg_faces_edges: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  k_owner_init<<<pg_blocks(nF, 256), 256, 0, s>>>(owner_ws, nF);
+  k_owner_min<<<pg_blocks(4 * n_elems, 256), 256, 0, s>>>(elemsF, n_elems, nF, owner_ws, status);
+  k_faces_edges<<<pg_blocks(nF, 256), 256, 0, s>>>(owner_ws, elemsE, nF, facesE);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_face_counts(const int32_t* elemsF, int64_t n_elems, int64_t nF, int32_t* face_nelem, void* stream) {
+  if (n_elems < 1 || nF < 1 || !elemsF || !face_nelem) {
+    pg_set_error("pg_face_counts: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  PG_CUDA_TRY(cudaMemsetAsync(face_nelem, 0, sizeof(int32_t) * nF, s));
+  k_face_counts<<<pg_blocks(4 * n_elems, 256), 256, 0, s>>>(elemsF, n_elems, nF, face_nelem);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_flag_edges_of_pairs(const int32_t* edgesNodes, int64_t nE, const int32_t* pairs, int64_t n_pairs,
+                                      int32_t* flags, void* stream) {
+  if (nE < 1 || n_pairs < 0 || !edgesNodes || !flags || (n_pairs > 0 && !pairs)) {
+    pg_set_error("pg_flag_edges_of_pairs: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  PG_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int32_t) * nE, s));
+  if (n_pairs > 0) k_flag_pairs<<<pg_blocks(n_pairs, 256), 256, 0, s>>>(edgesNodes, nE, pairs, n_pairs, flags);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" size_t pg_select_workspace_bytes(int64_t n) {
+  return pg_align256(sizeof(int32_t) * n) * 2 + pg::scan_workspace_bytes(n) + 512;
+}
+
+extern "C" int pg_select_equal(const int32_t* values, int64_t n, int32_t target, int32_t* out, int64_t* count,
+                               void* workspace, size_t workspace_bytes, void* stream) {
+  if (n < 1 || !values || !out || !count) {
+    pg_set_error("pg_select_equal: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (!workspace || workspace_bytes < pg_select_workspace_bytes(n)) {
+    pg_set_error("pg_select_equal: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  cudaStream_t s = pg_stream(stream);
+  PgArena ar(workspace, workspace_bytes);
+  int32_t* flags = ar.take<int32_t>(n);
+  int32_t* pos = ar.take<int32_t>(n);
+  const size_t scan_b = pg::scan_workspace_bytes(n);
+  void* scan_ws = ar.take<char>(scan_b);
+  int32_t* tot = ar.take<int32_t>(2);
+  if (!flags || !pos || !scan_ws || !tot) return PG_ERR_WORKSPACE;
+  k_eq_flags<<<pg_blocks(n, 256), 256, 0, s>>>(values, n, target, flags);
+  int st = pg::scan_exclusive_i32(flags, pos, n, tot, scan_ws, scan_b, s);
+  if (st) return st;
+  k_compact<<<pg_blocks(n, 256), 256, 0, s>>>(flags, pos, n, out);
+  k_store_count<<<1, 1, 0, s>>>(tot, count);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

@@ -166,10 +166,10 @@ class DeviceMesh:
         self.pair_partner = torch.empty(self.n_pairs, dtype=torch.int32, device=dev)
         items = torch.empty(self.nnz, dtype=torch.int64, device=dev)
         nit = torch.zeros(1, dtype=torch.int64, device=dev)
-        ws = _ws(_lib.query("pg_pattern_items_workspace_bytes", self.n_pairs), dev)
+        ws = _ws(_lib.query("pg_pattern_items_workspace_bytes", self.n_pairs, self.nnz), dev)
         _lib.call("pg_pattern_items", _p(self.members), _p(self.pair_start), self.n_pairs, _p(self.elemsE),
-                  _p(self.elemsF), T, self.nE, self.nF, p, _p(self.pair_partner), _p(items), _p(nit), _p(ws),
-                  ws.numel(), _s())
+                  _p(self.elemsF), T, self.nE, self.nF, p, self.nnz, _p(self.pair_partner), _p(items), _p(nit),
+                  _p(ws), ws.numel(), _s())
         self.n_items = int(nit.item())
         self.items = items[:self.n_items].contiguous()
         del items, ws
