@@ -740,11 +740,14 @@ __device__ double2 sum_partials(const double2* partial, int nblocks, int rhs, do
   return out;
 }
 
-// q = At p (k = 1, G lanes per row), partial mu = p^T q; last block: alpha
-template <typename C, int G>
+// q = At p (k = 1, G lanes per row) in the matrix precision CM, gathering
+// the CM-typed copy pm of p; partial mu = p^T q with p in FP64; last block:
+// alpha = rho / mu.
+template <typename CM, int G>
 __global__ void __launch_bounds__(kThreads) k_cg_spmv1(const int64_t* __restrict__ rowptr,
-                                                       const int32_t* __restrict__ col, const C* __restrict__ val,
-                                                       int64_t n, const C* __restrict__ pv, C* __restrict__ q,
+                                                       const int32_t* __restrict__ col, const CM* __restrict__ val,
+                                                       int64_t n, const CM* __restrict__ pm,
+                                                       const double2* __restrict__ p64, CM* __restrict__ q,
                                                        double2* partial, CgState* st, CgCtl* ctl) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
@@ -756,16 +759,16 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv1(const int64_t* __restrict
   for (int64_t rw = warp_base; rw < n; rw += groups) {
     const int64_t r = rw + (gid - warp_base);
     const bool valid = r < n;
-    C acc = czero<C>();
+    CM acc = czero<CM>();
     if (valid) {
       const int64_t e = rowptr[r + 1];
-      for (int64_t k = rowptr[r] + lane; k < e; k += G) acc = cfma(val[k], pv[col[k]], acc);
+      for (int64_t k = rowptr[r] + lane; k < e; k += G) acc = cfma(val[k], pm[col[k]], acc);
     }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) acc = cadd(acc, shfl_xor(acc, off));
     if (valid && lane == 0) {
       q[r] = acc;
-      mu = dadd(mu, bilin(pv[r], acc));
+      mu = dadd(mu, cmul(p64[r], to_d(acc)));
     }
   }
   block_reduce_rhs<1>(mu, smem, partial + blockIdx.x);
@@ -790,10 +793,11 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv1(const int64_t* __restrict
 }
 
 // q = At p for k > 1 RHS (thread per (row, rhs)), partial mu; last block: alpha
-template <typename C, int K>
+template <typename CM, int K>
 __global__ void __launch_bounds__(kThreads) k_cg_spmm(const int64_t* __restrict__ rowptr,
-                                                      const int32_t* __restrict__ col, const C* __restrict__ val,
-                                                      int64_t n, const C* __restrict__ pv, C* __restrict__ q,
+                                                      const int32_t* __restrict__ col, const CM* __restrict__ val,
+                                                      int64_t n, const CM* __restrict__ pm,
+                                                      const double2* __restrict__ p64, CM* __restrict__ q,
                                                       double2* partial, CgState* st, CgCtl* ctl) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
@@ -801,11 +805,11 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmm(const int64_t* __restrict_
   const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / K;
   double2 mu = make_double2(0.0, 0.0);
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; r < n; r += rows_per_pass) {
-    C acc = czero<C>();
+    CM acc = czero<CM>();
     const int64_t e = rowptr[r + 1];
-    for (int64_t k = rowptr[r]; k < e; ++k) acc = cfma(val[k], pv[(int64_t)col[k] * K + rhs], acc);
+    for (int64_t k = rowptr[r]; k < e; ++k) acc = cfma(val[k], pm[(int64_t)col[k] * K + rhs], acc);
     q[r * K + rhs] = acc;
-    mu = dadd(mu, bilin(pv[r * K + rhs], acc));
+    mu = dadd(mu, cmul(p64[r * K + rhs], to_d(acc)));
   }
   block_reduce_rhs<K>(mu, smem, partial + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) {
@@ -828,31 +832,30 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmm(const int64_t* __restrict_
   }
 }
 
-// y += alpha p ; r -= alpha q ; partials rho = r^T r, w = sum |r|^2 |D|.
+// y += alpha p ; r -= alpha q (FP64) ; partials rho = r^T r, w = sum |r|^2 |D|.
 // Last block: beta, residual estimate, activity; the cycle stops for every
 // RHS when one needs a reliable update (estimate dropped below delta * res0
 // or grew above 1e3 * res0), or when all have converged.
-template <typename C, int K>
-__global__ void __launch_bounds__(kThreads) k_cg_update(C* __restrict__ y, C* __restrict__ r,
-                                                        const C* __restrict__ pv, const C* __restrict__ q,
-                                                        const typename Real<C>::T* __restrict__ wd, int64_t n,
-                                                        CgState* st, double2* prho, double2* pw, CgCtl* ctl,
-                                                        int iter, double delta) {
+template <typename CM, int K>
+__global__ void __launch_bounds__(kThreads) k_cg_update(double2* __restrict__ y, double2* __restrict__ r,
+                                                        const double2* __restrict__ pv, const CM* __restrict__ q,
+                                                        const double* __restrict__ wd, int64_t n, CgState* st,
+                                                        double2* prho, double2* pw, CgCtl* ctl, int iter,
+                                                        double delta) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
-  __shared__ C al[kMaxK];
-  if (threadIdx.x < K) al[threadIdx.x] = cfrom<C>(st[threadIdx.x].alpha);
+  __shared__ double2 al[kMaxK];
+  if (threadIdx.x < K) al[threadIdx.x] = st[threadIdx.x].alpha;
   __syncthreads();
   const int rhs = threadIdx.x % K;
-  const C a = al[rhs];
+  const double2 a = al[rhs];
   const int64_t total = n * K;
   const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
   const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
-  typedef typename Real<C>::T R;
-  R rr = 0, ri = 0, ww = 0;
+  double rr = 0, ri = 0, ww = 0;
   for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
-    const C pe = pv[e], qe = q[e];
-    C ye = y[e], re = r[e];
+    const double2 pe = pv[e], qe = to_d(q[e]);
+    double2 ye = y[e], re = r[e];
     ye = cfma(a, pe, ye);
     re.x -= a.x * qe.x - a.y * qe.y;
     re.y -= a.x * qe.y + a.y * qe.x;
@@ -862,8 +865,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(C* __restrict__ y, C* __
     ri += 2 * re.x * re.y;
     ww += (re.x * re.x + re.y * re.y) * wd[e / K];
   }
-  block_reduce_rhs<K>(make_double2((double)rr, (double)ri), smem, prho + (int64_t)blockIdx.x * K);
-  block_reduce_rhs<K>(make_double2((double)ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
+  block_reduce_rhs<K>(make_double2(rr, ri), smem, prho + (int64_t)blockIdx.x * K);
+  block_reduce_rhs<K>(make_double2(ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) {
     const int my = threadIdx.x < K ? threadIdx.x : 0;
     const double2 rho = sum_partials<K>(prho, gridDim.x, my, smem);
@@ -901,15 +904,16 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(C* __restrict__ y, C* __
   }
 }
 
-// p = r + beta p for every RHS whose beta was computed in this launch
-// (iteration `iter`); RHS that were already inactive keep their p.
-template <typename C, int K>
-__global__ void __launch_bounds__(kThreads) k_cg_pupdate(C* __restrict__ pv, const C* __restrict__ r, int64_t n,
-                                                         const CgState* st, int iter) {
-  __shared__ C bt[kMaxK];
+// p = r + beta p (FP64) and its matrix-precision copy pm, for every RHS whose
+// beta was computed in this launch (iteration `iter`).
+template <typename CM, int K>
+__global__ void __launch_bounds__(kThreads) k_cg_pupdate(double2* __restrict__ pv, CM* __restrict__ pm,
+                                                         const double2* __restrict__ r, int64_t n, const CgState* st,
+                                                         int iter, int write_pm) {
+  __shared__ double2 bt[kMaxK];
   __shared__ int use[kMaxK];
   if (threadIdx.x < K) {
-    bt[threadIdx.x] = cfrom<C>(st[threadIdx.x].beta);
+    bt[threadIdx.x] = st[threadIdx.x].beta;
     use[threadIdx.x] = st[threadIdx.x].beta_iter == iter;
   }
   __syncthreads();
@@ -918,10 +922,14 @@ __global__ void __launch_bounds__(kThreads) k_cg_pupdate(C* __restrict__ pv, con
   if (!anyuse) return;
   const int64_t total = n * K;
   for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
-    if (use[e % K]) pv[e] = cfma(bt[e % K], pv[e], r[e]);
+    if (use[e % K]) {
+      const double2 v = cfma(bt[e % K], pv[e], r[e]);
+      pv[e] = v;
+      if (write_pm) pm[e] = cfrom<CM>(v);
+    }
 }
 
-// S = D^-1/2 (principal root), wd = |D|, At = S A S in precision C
+// S = D^-1/2 (principal root), wd = |D|, At = S A S in precision CM
 __global__ void k_cg_scaling(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n, double2* S,
                              double* wd, int* status) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
@@ -943,36 +951,33 @@ __global__ void k_cg_scaling(const int64_t* rowptr, const int32_t* col, const do
   }
 }
 
-template <typename C>
+template <typename CM>
 __global__ void k_cg_scale_matrix(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n,
-                                  const double2* S, C* out) {
+                                  const double2* S, CM* out) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     const double2 sr = S[r];
-    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) out[k] = cfrom<C>(cmul(sr, cmul(val[k], S[col[k]])));
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) out[k] = cfrom<CM>(cmul(sr, cmul(val[k], S[col[k]])));
   }
 }
 
-template <typename C>
-__global__ void k_cg_wd(const double* wd, int64_t n, typename Real<C>::T* out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = (typename Real<C>::T)wd[i];
-}
-
-// r~ = S r64 (cast), y = 0 ; first cycle also p = r~ ; partial rho
-template <typename C, int K>
-__global__ void k_cg_start(const double2* __restrict__ r64, const double2* __restrict__ S, int64_t n, C* r, C* y, C* pv,
-                           int set_p, double2* prho) {
+// r = S r64, y = 0 ; first cycle also p = r (and pm) ; partial rho
+template <typename CM, int K>
+__global__ void k_cg_start(const double2* __restrict__ r64, const double2* __restrict__ S, int64_t n, double2* r,
+                           double2* y, double2* pv, CM* pm, int set_p, int write_pm, double2* prho) {
   __shared__ double2 smem[(kThreads / 32) * kMaxK];
   const int64_t total = n * K;
   const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
   const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
   double2 rho = make_double2(0.0, 0.0);
   for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
-    const C v = cfrom<C>(cmul(S[e / K], r64[e]));
+    const double2 v = cmul(S[e / K], r64[e]);
     r[e] = v;
-    y[e] = czero<C>();
-    if (set_p) pv[e] = v;
-    rho = dadd(rho, bilin(v, v));
+    y[e] = make_double2(0.0, 0.0);
+    if (set_p) {
+      pv[e] = v;
+      if (write_pm) pm[e] = cfrom<CM>(v);
+    }
+    rho = dadd(rho, cmul(v, v));
   }
   block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
 }
@@ -1013,26 +1018,25 @@ __global__ void k_cg_cycle_init(const double2* prho, int nblocks, CgState* st, c
   }
 }
 
-// x64 += S y
-template <typename C, int K>
-__global__ void k_cg_xupdate(const C* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
+// x += S y
+template <int K>
+__global__ void k_cg_xupdate(const double2* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
   const int64_t total = n * K;
   for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
-    x[e] = dadd(x[e], cmul(S[e / K], to_d(y[e])));
+    x[e] = dadd(x[e], cmul(S[e / K], y[e]));
 }
 
 size_t cg_layout(const Plan& P, size_t* off /* 14 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
-  const size_t rsize = P.csize / 2;
-  put(0, P.nnz * P.csize);                      // At
+  put(0, P.nnz * P.csize);                      // At (matrix precision)
   put(1, sizeof(double2) * P.n);                // S
-  put(2, sizeof(double) * P.n);                 // |D| (f64)
-  put(3, rsize * P.n);                          // |D| (compute precision)
-  put(4, P.csize * P.n * P.k);                  // p
-  put(5, P.csize * P.n * P.k);                  // q
-  put(6, P.csize * P.n * P.k);                  // r
-  put(7, P.csize * P.n * P.k);                  // y
+  put(2, sizeof(double) * P.n);                 // |D|
+  put(3, P.csize * P.n * P.k);                  // p in matrix precision (gathered by the SpMV)
+  put(4, sizeof(double2) * P.n * P.k);          // p
+  put(5, P.csize * P.n * P.k);                  // q (matrix precision)
+  put(6, sizeof(double2) * P.n * P.k);          // r
+  put(7, sizeof(double2) * P.n * P.k);          // y
   put(8, sizeof(double2) * P.n * P.k);          // r64
   put(9, sizeof(double2) * (size_t)P.nb * P.k * 3);  // partials (mu/rho, w)
   put(10, sizeof(CgState) * P.k);
@@ -1042,40 +1046,41 @@ size_t cg_layout(const Plan& P, size_t* off /* 14 */) {
   return o;
 }
 
-template <typename C>
-void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const C* val, const C* pv, C* q,
-                    double2* partial, CgState* st, CgCtl* ctl, int64_t npr, int grid, cudaStream_t s) {
+template <typename CM>
+void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const CM* val, const CM* pm,
+                    const double2* p64, CM* q, double2* partial, CgState* st, CgCtl* ctl, int64_t npr, int grid,
+                    cudaStream_t s) {
   switch (P.k) {
     case 1:
-      switch (LanesPerRow<C>::pick(npr)) {
-        case 32: k_cg_spmv1<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-        case 16: k_cg_spmv1<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-        case 8: k_cg_spmv1<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-        default: k_cg_spmv1<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+      switch (LanesPerRow<CM>::pick(npr)) {
+        case 32: k_cg_spmv1<CM, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+        case 16: k_cg_spmv1<CM, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+        case 8: k_cg_spmv1<CM, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+        default: k_cg_spmv1<CM, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
       }
       break;
-    case 2: k_cg_spmm<C, 2><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-    case 4: k_cg_spmm<C, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-    case 8: k_cg_spmm<C, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-    case 16: k_cg_spmm<C, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
-    case 32: k_cg_spmm<C, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pv, q, partial, st, ctl); break;
+    case 2: k_cg_spmm<CM, 2><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+    case 4: k_cg_spmm<CM, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+    case 8: k_cg_spmm<CM, 8><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+    case 16: k_cg_spmm<CM, 16><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
+    case 32: k_cg_spmm<CM, 32><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, pm, p64, q, partial, st, ctl); break;
   }
 }
 
-template <typename C>
+template <typename CM>
 int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
              const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  typedef typename Real<C>::T R;
   size_t off[14];
   cg_layout(P, off);
-  C* At = reinterpret_cast<C*>(ws + off[0]);
+  CM* At = reinterpret_cast<CM*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
-  double* wd64 = reinterpret_cast<double*>(ws + off[2]);
-  R* wd = reinterpret_cast<R*>(ws + off[3]);
-  C* pv = reinterpret_cast<C*>(ws + off[4]);
-  C* q = reinterpret_cast<C*>(ws + off[5]);
-  C* r = reinterpret_cast<C*>(ws + off[6]);
-  C* y = reinterpret_cast<C*>(ws + off[7]);
+  double* wd = reinterpret_cast<double*>(ws + off[2]);
+  const bool same = sizeof(CM) == sizeof(double2);   // fp64: p doubles as its own matrix-precision copy
+  double2* pv = reinterpret_cast<double2*>(ws + off[4]);
+  CM* pm = same ? reinterpret_cast<CM*>(pv) : reinterpret_cast<CM*>(ws + off[3]);
+  CM* q = reinterpret_cast<CM*>(ws + off[5]);
+  double2* r = reinterpret_cast<double2*>(ws + off[6]);
+  double2* y = reinterpret_cast<double2*>(ws + off[7]);
   double2* r64 = reinterpret_cast<double2*>(ws + off[8]);
   double2* part = reinterpret_cast<double2*>(ws + off[9]);
   double2* part2 = part + (size_t)P.nb * P.k;
@@ -1085,15 +1090,15 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   double* target = rnorm + P.k;
   int* want = reinterpret_cast<int*>(ws + off[13]);
   int* dstatus = want + P.k;
+  const int write_pm = same ? 0 : 1;
   const int k = P.k, nb = P.nb;
   const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
   const int spmv_grid = 152 * 16;
   if (spmv_grid > nb) return PG_ERR_ARG;  // partial buffers are sized by nb
 
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
-  k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd64, dstatus);
-  k_cg_scale_matrix<C><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
-  k_cg_wd<C><<<pg_blocks(P.n, 256), 256, 0, s>>>(wd64, P.n, wd);
+  k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
+  k_cg_scale_matrix<CM><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
   PG_LAUNCH_CHECK();
   std::vector<double> bnorm(k), rn(k), tgt(k);
   std::vector<int> wnt(k);
@@ -1151,20 +1156,21 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
-    PG_KSWITCH(k, (k_cg_start<C, K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part),
+    PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, pm, first ? 1 : 0, write_pm, part),
                    k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
     const double delta = P.prec ? 0.1 : 0.0;
     for (int it = 0; it < steps; ++it) {
       const int iter = (int)(launch_iter + it);
-      launch_cg_spmv<C>(P, rowptr, col, At, pv, q, part, st, ctl, npr, spmv_grid, s);
-      PG_KSWITCH(k, (k_cg_update<C, K><<<nb, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
-                     k_cg_pupdate<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter)));
+      launch_cg_spmv<CM>(P, rowptr, col, At, pm, pv, q, part, st, ctl, npr, spmv_grid, s);
+      PG_KSWITCH(k, (k_cg_update<CM, K><<<nb, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
+                     k_cg_pupdate<CM, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, pm, r, P.n, st, iter,
+                                                                                          write_pm)));
     }
     PG_LAUNCH_CHECK();
     launch_iter += steps;
-    PG_KSWITCH(k, (k_cg_xupdate<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    PG_KSWITCH(k, (k_cg_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
     std::vector<int> hits(k);
     std::vector<int> hbrk(k);
     for (int i = 0; i < k; ++i) {

@@ -41,3 +41,18 @@ def read(path):
         phys.append(int(v[3]) if ntags > 0 else 0)
         tets.append([tag_to_index[int(x)] for x in v[3 + ntags:3 + ntags + 4]])
     return GmshMesh(points, np.asarray(tets, dtype=np.int64), np.asarray(phys, dtype=np.int64))
+
+
+def write(path, points, tets, physical=None):
+    """Write a gmsh 2.2 ASCII file with tetrahedra (type 4) and physical tags."""
+    points = np.asarray(points, dtype=np.float64)
+    tets = np.asarray(tets, dtype=np.int64)
+    phys = np.ones(len(tets), dtype=np.int64) if physical is None else np.asarray(physical, dtype=np.int64)
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(points))
+        for i, (x, y, z) in enumerate(points):
+            f.write("%d %.17g %.17g %.17g\n" % (i + 1, x, y, z))
+        f.write("$EndNodes\n$Elements\n%d\n" % len(tets))
+        for i, (t, ph) in enumerate(zip(tets, phys)):
+            f.write("%d 4 2 %d %d %d %d %d %d\n" % (i + 1, ph, ph, t[0] + 1, t[1] + 1, t[2] + 1, t[3] + 1))
+        f.write("$EndElements\n")
