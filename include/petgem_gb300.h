@@ -157,6 +157,22 @@ size_t pg_select_workspace_bytes(int64_t n);
 int pg_select_equal(const int32_t* values, int64_t n, int32_t target, int32_t* out, int64_t* count,
                     void* workspace, size_t workspace_bytes, void* stream);
 
+/* Allocation-free pg_select_equal (no counterpart in the reference).  For
+ * callers that cannot allocate device memory (their device memory is owned
+ * by another allocator, or their request path must not allocate): the
+ * scratch is a static device array inside this library, so the call makes no
+ * allocation.  Limit: n <= PG_NOALLOC_MAX_N (larger n returns PG_ERR_ARG;
+ * use pg_select_equal with a workspace instead).  Every GPU that loads the
+ * library keeps the ~2 MB array until exit.  The first call on a device looks
+ * up the array's device address with that device current; make that first
+ * call before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (concurrent streams, or several host threads) race and
+ * must be serialised by the caller. */
+#define PG_NOALLOC_MAX_N 262144
+int64_t pg_select_equal_noalloc_max_n(void);
+int pg_select_equal_noalloc(const int32_t* values, int64_t n, int32_t target, int32_t* out, int64_t* count,
+                            void* stream);
+
 /* ------------------------------------------------------------------------
  * CSR pattern and value assembly (replaces petgem/parallel.py:150
  * createParallelMatrix + the Mat.setValues(ADD_VALUES)/assemblyBegin/End

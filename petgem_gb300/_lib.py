@@ -60,6 +60,8 @@ SIGNATURES = {
     "pg_flag_edges_of_pairs": (_INT, [_P, _I64, _P, _I64, _P, _P]),
     "pg_select_workspace_bytes": (_SZ, [_I64]),
     "pg_select_equal": (_INT, [_P, _I64, _INT, _P, _P, _P, _SZ, _P]),
+    "pg_select_equal_noalloc_max_n": (_I64, []),
+    "pg_select_equal_noalloc": (_INT, [_P, _I64, _INT, _P, _P, _P]),
     "pg_pattern_local_entities": (_INT, [_INT]),
     "pg_pattern_workspace_bytes": (_SZ, [_I64, _I64, _I64, _INT]),
     "pg_pattern_build": (_INT, [_P, _P, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _P, _P, _SZ, _P]),
