@@ -329,19 +329,27 @@ def run_solves(args, torch, mesh, model, vals, b):
         B[:, k] = bk
     B[mesh.bnd.long(), :] = 0
     x64, r64 = timed("cocg", "fp64", b, args.max_it)
-    xmx, rmx = timed("cocg", "mixed", b, args.max_it)
-    Xb, rb = timed("cocg", "mixed", B.contiguous(), args.max_it)
+    xdf, rdf = timed("cocg", "df64", b, args.max_it)
+    Xdb, rdb = timed("cocg", "df64", B.contiguous(), args.max_it)
+    # the FP32-operator form stalls above 1e-8 at this conditioning: capped, per-iteration cost reported
+    xmx, rmx = timed("cocg", "mixed", b, 3000)
+    Xb, rb = timed("cocg", "mixed", B.contiguous(), 1000)
     _, rg = timed("gmres", "mixed", b, 300)
     # receiver-field error of each form against a tight FP64 solve
-    xt, _ = mesh.solve(vals, b, rtol=1e-11, precision="fp64", max_it=4 * args.max_it, raise_on_fail=False, ksp="cocg")
+    xt, _ = mesh.solve(vals, b, rtol=1e-11, precision="fp64", max_it=3 * args.max_it, raise_on_fail=False, ksp="cocg")
     Ft, _ = mesh.receiver_fields(xt, model.receivers, model.source["frequency"])
-    for x, r in ((x64, r64), (xmx, rmx)):
+    for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb)):
         F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
         r["receiver_rel_err_vs_fp64_1e-11"] = float(torch.linalg.norm(F - Ft) / torch.linalg.norm(Ft))
     out["fp64"] = r64
+    out["df64"] = rdf
+    out["df64_batched"] = rdb
     out["mixed"] = rmx
     out["mixed_batched"] = rb
     out["gmres30_mixed_300its"] = rg
+    out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; mixed = complex64 "
+                   "matrix/SpMV + FP64 recurrence, which cannot reach 1e-8 at this conditioning (eps32*kappa ~ 1)")
+    out["speedup_df64_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rdb["ms_per_rhs"], 1e-9), 2)
     out["speedup_mixed_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rb["ms_per_rhs"], 1e-9), 2)
     return out
 
@@ -350,7 +358,8 @@ def profile_solves(args, torch, mesh, vals, b):
     """Fixed iteration counts of every solver form (for kernel launch lists)."""
     out = {}
     B = torch.stack([b] * args.nrhs, 1).contiguous()
-    for name, ksp, prec, rhs in (("cocg_fp64", "cocg", "fp64", b), ("cocg_mixed", "cocg", "mixed", b),
+    for name, ksp, prec, rhs in (("cocg_fp64", "cocg", "fp64", b), ("cocg_df64", "cocg", "df64", b),
+                                 ("cocg_df64_batched", "cocg", "df64", B), ("cocg_mixed", "cocg", "mixed", b),
                                  ("cocg_mixed_batched", "cocg", "mixed", B), ("gmres_mixed", "gmres", "mixed", b),
                                  ("gmres_fp64", "gmres", "fp64", b)):
         torch.cuda.synchronize()

@@ -311,8 +311,10 @@ int pg_gmres(const int64_t* rowptr, const int32_t* col, const double* vals, int6
 /* COCG (conjugate orthogonal CG) for the complex-symmetric A with symmetric
  * Jacobi scaling; an additional KSP type beside GMRES for the same system
  * (petgem configures PETSc's KSP from the options file, solver.py:588).
- * precision 0: complex128 recurrence; 1: complex64 recurrence with complex128
- * reliable updates.  The true FP64 residual is checked every check_every
+ * precision 0: complex128 throughout; 1: complex64 matrix and SpMV with a
+ * complex128 recurrence and FP64 reliable updates; 2 ("df64"): matrix and
+ * recurrence in double-float (FP32 hi + lo pairs, ~48-bit mantissa) computed
+ * on the FP32 pipes, FP64 reliable updates.  The true FP64 residual is checked every check_every
  * iterations (doubling up to 400) and decides convergence. */
 typedef struct pg_cocg_opts {
   int max_it;

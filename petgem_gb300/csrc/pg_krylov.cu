@@ -1221,6 +1221,456 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   return status;
 }
 
+
+// ============================================================================
+// df64: FP64-accurate COCG on the FP32 pipes.  Values are double-float pairs
+// (hi + lo, ~48-bit mantissa); a complex number is a float4
+// (re.hi, re.lo, im.hi, im.lo), 16 bytes like complex128.  Products are made
+// error-free with FMA, sums are compensated (two-sum), so every operation
+// costs ~11 FP32 instructions instead of one FP64 instruction - and GB300's
+// FP32 pipe is ~57x faster than its FP64 pipe, which makes the SpMV HBM-bound
+// instead of FP64-bound.  FP64 is kept for the scaling, the true residual, the
+// reliable updates and x.
+// ============================================================================
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (sh, sl) += (ah, al) * (bh, bl); the accumulator stays unnormalised
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float ph = ah * bh;
+  float pl = fmaf(ah, bh, -ph);
+  pl = fmaf(ah, bl, pl);
+  pl = fmaf(al, bh, pl);
+  float t, e;
+  two_sum(sh, ph, t, e);
+  sh = t;
+  sl = sl + (e + pl);
+}
+
+// (sh, sl) += (bh, bl)
+__device__ __forceinline__ void df_add(float& sh, float& sl, float bh, float bl) {
+  float t, e;
+  two_sum(sh, bh, t, e);
+  sh = t;
+  sl = sl + (e + bl);
+}
+
+__device__ __forceinline__ float4 df_norm(float4 v) {
+  float s = v.x + v.y;
+  const float e1 = v.y - (s - v.x);
+  float t = v.z + v.w;
+  const float e2 = v.w - (t - v.z);
+  return make_float4(s, e1, t, e2);
+}
+
+// c += a * b (complex double-float)
+__device__ __forceinline__ void cdf_mac(float4& c, float4 a, float4 b) {
+  df_mac(c.x, c.y, a.x, a.y, b.x, b.y);
+  df_mac(c.x, c.y, -a.z, -a.w, b.z, b.w);
+  df_mac(c.z, c.w, a.x, a.y, b.z, b.w);
+  df_mac(c.z, c.w, a.z, a.w, b.x, b.y);
+}
+
+__device__ __forceinline__ float4 cdf_from(double2 v) {
+  const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
+  return make_float4(rh, __double2float_rn(v.x - (double)rh), ih, __double2float_rn(v.y - (double)ih));
+}
+__device__ __forceinline__ double2 cdf_to(float4 v) {
+  return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+__device__ __forceinline__ float4 shfl_xor4(float4 v, int m) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
+                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
+}
+__device__ __forceinline__ void cdf_add(float4& a, float4 b) {
+  df_add(a.x, a.y, b.x, b.y);
+  df_add(a.z, a.w, b.z, b.w);
+}
+
+// alpha / beta finalisation shared by the df kernels (last block only)
+template <int K>
+__device__ void cg_alpha_final(const double2* partial, int nblocks, CgState* st, CgCtl* ctl, double2* smem) {
+  const double2 m = sum_partials<K>(partial, nblocks, threadIdx.x < K ? threadIdx.x : 0, smem);
+  if (threadIdx.x < K) {
+    CgState& S = st[threadIdx.x];
+    if (S.active) {
+      if (m.x == 0.0 && m.y == 0.0) {
+        S.breakdown = 1;
+        S.active = 0;
+        S.alpha = make_double2(0.0, 0.0);
+      } else {
+        S.alpha = ddiv(S.rho, m);
+      }
+    } else {
+      S.alpha = make_double2(0.0, 0.0);
+    }
+  }
+  if (threadIdx.x == 0) ctl->counter = 0;
+}
+
+template <int K>
+__device__ void cg_beta_final(const double2* prho, const double2* pw, int nblocks, CgState* st, CgCtl* ctl, int iter,
+                              double delta, double2* smem) {
+  const int my = threadIdx.x < K ? threadIdx.x : 0;
+  const double2 rho = sum_partials<K>(prho, nblocks, my, smem);
+  const double2 w = sum_partials<K>(pw, nblocks, my, smem);
+  __shared__ int any, stop;
+  if (threadIdx.x == 0) { any = 0; stop = 0; }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    CgState& S = st[threadIdx.x];
+    if (S.active) {
+      S.beta_iter = iter;
+      S.its += 1;
+      S.res = sqrt(w.x);
+      if (!isfinite(S.res)) ctl->nonfinite = 1;
+      if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+        S.breakdown = 1;
+        S.active = 0;
+        S.beta = make_double2(0.0, 0.0);
+      } else {
+        S.beta = ddiv(rho, S.rho);
+      }
+      S.rho = rho;
+      if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
+      else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
+    } else {
+      S.beta = make_double2(0.0, 0.0);
+    }
+    if (S.active) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any && !stop;
+    ctl->counter = 0;
+  }
+}
+
+// q = At p (double-float), partial mu = p^T q; last block: alpha
+template <int G>
+__global__ void __launch_bounds__(kThreads) k_df_spmv1(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                       const float4* __restrict__ val, int64_t n,
+                                                       const float4* __restrict__ pv, float4* __restrict__ q,
+                                                       double2* partial, CgState* st, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t rw = warp_base; rw < n; rw += groups) {
+    const int64_t r = rw + (gid - warp_base);
+    const bool valid = r < n;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      const int64_t e = rowptr[r + 1];
+      for (int64_t k = rowptr[r] + lane; k < e; k += G) cdf_mac(acc, val[k], pv[col[k]]);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) cdf_add(acc, shfl_xor4(acc, off));
+    if (valid && lane == 0) {
+      acc = df_norm(acc);
+      q[r] = acc;
+      cdf_mac(mu, pv[r], acc);
+    }
+  }
+  block_reduce_rhs<1>(cdf_to(mu), smem, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_df_spmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                      const float4* __restrict__ val, int64_t n,
+                                                      const float4* __restrict__ pv, float4* __restrict__ q,
+                                                      double2* partial, CgState* st, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int rhs = threadIdx.x % K;
+  const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / K;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; r < n; r += rows_per_pass) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t e = rowptr[r + 1];
+    for (int64_t k = rowptr[r]; k < e; ++k) cdf_mac(acc, val[k], pv[(int64_t)col[k] * K + rhs]);
+    acc = df_norm(acc);
+    q[r * K + rhs] = acc;
+    cdf_mac(mu, pv[r * K + rhs], acc);
+  }
+  block_reduce_rhs<K>(cdf_to(mu), smem, partial + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
+}
+
+// y += alpha p ; r -= alpha q ; partials rho = r^T r (df), w = sum |r|^2 |D| (FP32 estimate)
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, float4* __restrict__ r,
+                                                        const float4* __restrict__ pv, const float4* __restrict__ q,
+                                                        const float* __restrict__ wd, int64_t n, CgState* st,
+                                                        double2* prho, double2* pw, CgCtl* ctl, int iter,
+                                                        double delta) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float4 al[kMaxK];
+  if (threadIdx.x < K) {
+    const double2 a = st[threadIdx.x].alpha;
+    al[threadIdx.x] = cdf_from(a);
+  }
+  __syncthreads();
+  const int rhs = threadIdx.x % K;
+  const float4 a = al[rhs];
+  const float4 na = make_float4(-a.x, -a.y, -a.z, -a.w);
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
+  float ww = 0.f;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    float4 ye = y[e], re = r[e];
+    cdf_mac(ye, a, pv[e]);
+    cdf_mac(re, na, q[e]);
+    ye = df_norm(ye);
+    re = df_norm(re);
+    y[e] = ye;
+    r[e] = re;
+    cdf_mac(rho, re, re);
+    ww += (re.x * re.x + re.z * re.z) * wd[e / K];
+  }
+  block_reduce_rhs<K>(cdf_to(rho), smem, prho + (int64_t)blockIdx.x * K);
+  block_reduce_rhs<K>(make_double2((double)ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) cg_beta_final<K>(prho, pw, gridDim.x, st, ctl, iter, delta, smem);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_df_pupdate(float4* __restrict__ pv, const float4* __restrict__ r, int64_t n,
+                                                         const CgState* st, int iter) {
+  __shared__ float4 bt[kMaxK];
+  __shared__ int use[kMaxK];
+  if (threadIdx.x < K) {
+    bt[threadIdx.x] = cdf_from(st[threadIdx.x].beta);
+    use[threadIdx.x] = st[threadIdx.x].beta_iter == iter;
+  }
+  __syncthreads();
+  int anyuse = 0;
+  for (int i = 0; i < K; ++i) anyuse |= use[i];
+  if (!anyuse) return;
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    if (use[e % K]) {
+      float4 v = r[e];
+      cdf_mac(v, bt[e % K], pv[e]);
+      pv[e] = df_norm(v);
+    }
+}
+
+__global__ void k_df_scale_matrix(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n,
+                                  const double2* S, float4* out, float* wdf, const double* wd) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 sr = S[r];
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) out[k] = cdf_from(cmul(sr, cmul(val[k], S[col[k]])));
+    wdf[r] = (float)wd[r];
+  }
+}
+
+template <int K>
+__global__ void k_df_start(const double2* __restrict__ r64, const double2* __restrict__ S, int64_t n, float4* r,
+                           float4* y, float4* pv, int set_p, double2* prho) {
+  __shared__ double2 smem[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double2 rho = make_double2(0.0, 0.0);
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const double2 v = cmul(S[e / K], r64[e]);
+    const float4 vf = cdf_from(v);
+    r[e] = vf;
+    y[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (set_p) pv[e] = vf;
+    rho = dadd(rho, cmul(v, v));
+  }
+  block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
+}
+
+template <int K>
+__global__ void k_df_xupdate(const float4* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    x[e] = dadd(x[e], cmul(S[e / K], cdf_to(y[e])));
+}
+
+size_t df_layout(const Plan& P, size_t* off /* 14 */) {
+  size_t o = 0;
+  auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
+  put(0, P.nnz * sizeof(float4));               // At (double-float)
+  put(1, sizeof(double2) * P.n);                // S
+  put(2, sizeof(double) * P.n);                 // |D|
+  put(3, sizeof(float) * P.n);                  // |D| f32
+  put(4, sizeof(float4) * P.n * P.k);           // p
+  put(5, sizeof(float4) * P.n * P.k);           // q
+  put(6, sizeof(float4) * P.n * P.k);           // r
+  put(7, sizeof(float4) * P.n * P.k);           // y
+  put(8, sizeof(double2) * P.n * P.k);          // r64
+  put(9, sizeof(double2) * (size_t)P.nb * P.k * 3);
+  put(10, sizeof(CgState) * P.k);
+  put(11, sizeof(CgCtl));
+  put(12, sizeof(double) * P.k * 3);
+  put(13, sizeof(int) * (P.k + 1));
+  return o;
+}
+
+int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
+                const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
+  size_t off[14];
+  df_layout(P, off);
+  float4* At = reinterpret_cast<float4*>(ws + off[0]);
+  double2* S = reinterpret_cast<double2*>(ws + off[1]);
+  double* wd = reinterpret_cast<double*>(ws + off[2]);
+  float* wdf = reinterpret_cast<float*>(ws + off[3]);
+  float4* pv = reinterpret_cast<float4*>(ws + off[4]);
+  float4* q = reinterpret_cast<float4*>(ws + off[5]);
+  float4* r = reinterpret_cast<float4*>(ws + off[6]);
+  float4* y = reinterpret_cast<float4*>(ws + off[7]);
+  double2* r64 = reinterpret_cast<double2*>(ws + off[8]);
+  double2* part = reinterpret_cast<double2*>(ws + off[9]);
+  double2* part2 = part + (size_t)P.nb * P.k;
+  CgState* st = reinterpret_cast<CgState*>(ws + off[10]);
+  CgCtl* ctl = reinterpret_cast<CgCtl*>(ws + off[11]);
+  double* rnorm = reinterpret_cast<double*>(ws + off[12]);
+  double* target = rnorm + P.k;
+  int* want = reinterpret_cast<int*>(ws + off[13]);
+  int* dstatus = want + P.k;
+  const int k = P.k, nb = P.nb;
+  const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
+  const int spmv_grid = 152 * 16;
+  if (spmv_grid > nb) return PG_ERR_ARG;
+
+  PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
+  k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
+  PG_LAUNCH_CHECK();
+  std::vector<double> bnorm(k), rn(k), tgt(k);
+  std::vector<int> wnt(k);
+  PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, part), k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+  PG_LAUNCH_CHECK();
+  PG_CUDA_TRY(cudaMemcpyAsync(bnorm.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  int hstatus = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hstatus) {
+    pg_set_error("pg_cocg: zero diagonal entry (Jacobi scaling undefined)");
+    return PG_ERR_BREAKDOWN;
+  }
+  const char* mon_env = getenv("PG_KSP_MONITOR");
+  const bool monitor = mon_env && mon_env[0] && mon_env[0] != '0';
+  int64_t its = 0, checks = 0, launch_iter = 1;
+  int status = PG_OK;
+  const int64_t max_it = o->max_it > 0 ? o->max_it : 100000;
+  int chunk = o->check_every > 0 ? o->check_every : 50;
+  bool first = true;
+  const double delta = 1e-3;   // double-float recurrence: replace after 3 decades
+  for (;;) {
+    launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+    PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
+                   k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+    PG_LAUNCH_CHECK();
+    PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    Ctl hctl;
+    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!first && hctl.nonfinite) {
+      pg_set_error("pg_cocg: non-finite residual");
+      status = PG_ERR_NONFINITE;
+      break;
+    }
+    bool all = true;
+    for (int i = 0; i < k; ++i) {
+      if (monitor)
+        fprintf(stderr, "pg_cocg(df64): check %lld its %lld rhs %d true ||r||/||b|| = %.6e\n", (long long)checks,
+                (long long)its, i, bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0);
+      if (!isfinite(rn[i])) {
+        pg_set_error("pg_cocg: non-finite residual");
+        status = PG_ERR_NONFINITE;
+      }
+      const double tb = o->rtol * bnorm[i];
+      const bool ok = rn[i] <= tb || bnorm[i] == 0.0;
+      wnt[i] = ok ? 0 : 1;
+      tgt[i] = 0.5 * tb;
+      if (!ok) all = false;
+    }
+    if (status || all) break;
+    if (its >= max_it) {
+      status = PG_ERR_NOT_CONVERGED;
+      break;
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part),
+                   k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    first = false;
+    const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
+    for (int it = 0; it < steps; ++it) {
+      const int iter = (int)(launch_iter + it);
+      switch (k) {
+        case 1:
+          switch (npr > 64 ? 8 : 4) {
+            case 8: k_df_spmv1<8><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, pv, q, part, st, ctl); break;
+            default: k_df_spmv1<4><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, pv, q, part, st, ctl); break;
+          }
+          break;
+        default:
+          PG_KSWITCH(k, (k_df_spmm<K><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, pv, q, part, st, ctl)));
+      }
+      PG_KSWITCH(k, (k_df_update<K><<<nb, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter, delta),
+                     k_df_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter)));
+    }
+    PG_LAUNCH_CHECK();
+    launch_iter += steps;
+    PG_KSWITCH(k, (k_df_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    std::vector<int> hits(k), hbrk(k);
+    for (int i = 0; i < k; ++i) {
+      PG_CUDA_TRY(cudaMemcpyAsync(&hits[i], &st[i].its, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaMemcpyAsync(&hbrk[i], &st[i].breakdown, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    int used = 0;
+    for (int i = 0; i < k; ++i) used = hits[i] > used ? hits[i] : used;
+    const int64_t cycle_its = used - its;
+    its = used;
+    ++checks;
+    bool brk = false;
+    for (int i = 0; i < k; ++i) brk = brk || hbrk[i];
+    if (brk) {
+      pg_set_error("pg_cocg: breakdown (p^T A p = 0 or r^T r = 0)");
+      status = PG_ERR_BREAKDOWN;
+      launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+      PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
+                     k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+      PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaStreamSynchronize(s));
+      break;
+    }
+    int64_t c2 = cycle_its + cycle_its / 4 + 8;
+    chunk = (int)(c2 < 16 ? 16 : (c2 > 4000 ? 4000 : c2));
+  }
+  double worst = 0.0;
+  for (int i = 0; i < k; ++i) {
+    const double rr = bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0;
+    if (relres_out) relres_out[i] = rr;
+    worst = rr > worst ? rr : worst;
+  }
+  if (res) {
+    res->iterations = its;
+    res->restarts = checks;
+    res->relres = worst;
+    res->status = status;
+  }
+  if (status == PG_ERR_NOT_CONVERGED) pg_set_error("pg_cocg: max_it reached before rtol");
+  return status;
+}
+
 bool valid_k(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32; }
 
 }  // namespace
@@ -1309,22 +1759,22 @@ extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
 static Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
   int nb = pick_blocks(n, nrhs);
   if (nb < 152 * 16) nb = 152 * 16;  // partials also hold the SpMV's per-block sums
-  return Plan{n, nnz, nrhs, 1, o->precision, nb, o->precision ? sizeof(float2) : sizeof(double2)};
+  return Plan{n, nnz, nrhs, 1, o->precision, nb, o->precision == 1 ? sizeof(float2) : sizeof(double2)};
 }
 
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = cg_plan(n, nnz, nrhs, opts);
   size_t off[14];
-  return cg_layout(P, off) + 256;
+  return (opts->precision == 2 ? df_layout(P, off) : cg_layout(P, off)) + 256;
 }
 
 extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
                        const double* b, double* x, int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result,
                        double* relres_per_rhs, void* workspace, size_t workspace_bytes, void* stream) {
   if (!opts || !rowptr || !col || !vals || !b || !x || n < 1 || nnz < n || !valid_k(nrhs) || !(opts->rtol > 0.0) ||
-      (opts->precision != 0 && opts->precision != 1)) {
-    pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1)");
+      opts->precision < 0 || opts->precision > 2) {
+    pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1/2)");
     return PG_ERR_ARG;
   }
   const size_t need = pg_cocg_workspace_bytes(n, nnz, nrhs, opts);
@@ -1339,5 +1789,6 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
   const double2* bb = reinterpret_cast<const double2*>(b);
   double2* xx = reinterpret_cast<double2*>(x);
   if (P.prec == 0) return run_cocg<double2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
+  if (P.prec == 2) return run_cocg_df(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
   return run_cocg<float2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
 }

@@ -272,12 +272,15 @@ class DeviceMesh:
 
         ksp="gmres": right-Jacobi restarted GMRES(restart) (PETSc -ksp_type gmres -pc_type jacobi);
         ksp="cocg":  Jacobi-scaled COCG for the complex-symmetric A.
-        precision="fp64" (complex128) or "mixed" (complex64 recurrence, complex128 residual/refinement).
+        precision="fp64" (complex128), "mixed" (complex64 matrix/SpMV, FP64 recurrence and
+        refinement) or "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy).
         Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
         """
         nrhs = 1 if b.ndim == 1 else int(b.shape[1])
         x = torch.zeros_like(b) if x0 is None else x0.clone()
-        prec = {"fp64": 0, "mixed": 1}[precision]
+        prec = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
+        if prec == 2 and ksp != "cocg":
+            raise ValueError("precision='df64' is implemented for ksp='cocg'")
         res = _lib.GmresResult()
         rr = (ctypes.c_double * nrhs)()
         lib = _lib.load()
