@@ -39,10 +39,14 @@ METRIC = "p=2 Melem/s assembled; ms/RHS to 1e-8 residual, FP64 vs mixed-prec bat
 WORKLOAD = "csem_p2_32cubed_jittered_logsigma (196,608 tets, 1,276,096 DOFs)"
 
 
+def workload(n):
+    return WORKLOAD if n == 32 else f"csem_p2_{n}cubed_jittered_logsigma ({6 * n ** 3:,} tets)"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=32, help="cubes per axis (32 = the metric's configuration)")
@@ -51,6 +55,10 @@ def parse():
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of a baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--assembly", default="df64", choices=["df64", "fp64"],
+                    help="arithmetic of the fused assembly (df64: double-float on the FP32 pipes)")
+    ap.add_argument("--no-records", action="store_true",
+                    help="assemble from the item list instead of the per-mesh assembly records")
     ap.add_argument("--solve-iters", type=int, default=0,
                     help="profiling mode: run each solver form for exactly this many iterations")
     return ap.parse_args()
@@ -67,8 +75,8 @@ def _cpu_worker(args):
     return A.nnz
 
 
-def cpu_assembly_rate(model, seconds, cores):
-    """Melem/s of the oracle assembly on a bounded sample; returns (rate, sample_elems, wall)."""
+def cpu_prepare(model):
+    """Per-mesh oracle topology (not timed): per-element coordinates, orientations, DOFs."""
     from oracle import topology
     tets = model.tets
     eE, eN = topology.compute_edges(tets)
@@ -76,7 +84,15 @@ def cpu_assembly_rate(model, seconds, cores):
     fE = topology.compute_faces_edges(eF, eE, fN.shape[0])
     eo, fo = topology.element_orientation(tets, eE, eN, eF, fE)
     dofs, _, _, _, N = topology.compute_connectivity_dofs(eE, eF, model.p)
-    coords = model.nodes[tets]
+    return {"coords": model.nodes[tets], "eo": eo, "fo": fo, "dofs": dofs, "N": N}
+
+
+def cpu_assembly_rate(model, seconds, cores, prep=None, pool=None):
+    """Melem/s of the oracle assembly on a bounded sample; returns (rate, sample_elems, wall).
+    pool: a spawn-context Pool of `cores` workers (made here when None)."""
+    prep = prep or cpu_prepare(model)
+    tets = model.tets
+    coords, eo, fo, dofs, N = prep["coords"], prep["eo"], prep["fo"], prep["dofs"], prep["N"]
 
     def job(idx):
         return (coords[idx], eo[idx], fo[idx], model.sigma[idx], dofs[idx], model.p, N)
@@ -88,34 +104,65 @@ def cpu_assembly_rate(model, seconds, cores):
     n_el = int(min(len(tets), max(cores * 64, seconds * cores / max(per_elem, 1e-6))))
     idx = np.arange(n_el)
     parts = np.array_split(idx, cores * 4)
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
+    own = pool is None
+    if own:
+        pool = mp.get_context("spawn").Pool(cores)
+    try:
         pool.map(_cpu_worker, [job(parts[0][:8])] * cores)     # warm the workers
         t = time.time()
         pool.map(_cpu_worker, [job(pp) for pp in parts])
         wall = time.time() - t
+    finally:
+        if own:
+            pool.close()
+            pool.join()
     return n_el / wall / 1e6, n_el, wall
 
 
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 20 ms from a reader
+    thread that stamps each line on arrival; summary() keeps the samples that
+    arrived between mark_start() and mark_end() (plus one interval of grace)."""
+
+    INTERVAL_MS = 20
+
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join("/tmp", f"pg_clocks_{os.getpid()}.csv")
+        self.rows = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
+        import threading
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
-            self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, stdin=subprocess.DEVNULL,
+                                         text=True)
         except Exception:
             self.proc = None
+            return self
+        self.started = threading.Event()
+
+        def reader():
+            for ln in self.proc.stdout:
+                self.rows.append((time.time(), ln))
+                self.started.set()
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+        self.started.wait(timeout=5.0)            # sampling is live before the timed region
         return self
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+        time.sleep(2 * self.INTERVAL_MS / 1e3)
 
     def __exit__(self, *a):
         if self.proc is not None:
@@ -124,14 +171,14 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-            self.f.close()
 
     def summary(self):
-        try:
-            rows = [ln.split(",") for ln in open(self.path).read().strip().splitlines() if ln.strip()]
-        except Exception:
+        if not self.rows or self.t0 is None or self.t1 is None:
             return None
-        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        grace = self.INTERVAL_MS / 1e3
+        rows = [ln for t, ln in self.rows if self.t0 <= t <= self.t1 + grace]
+        rows = [[c.strip() for c in r.split(",")] for r in rows]
+        rows = [r for r in rows if len(r) >= 9]
         if not rows:
             return None
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -139,7 +186,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "window_ms": round((self.t1 - self.t0) * 1e3, 1)}
 
 
 # ----------------------------------------------------------------------------- GPU leg
@@ -157,6 +204,15 @@ def fp64_peak(torch, lib):
     e1.record()
     torch.cuda.synchronize()
     return 5 * lib.pg_fp64_probe_flops(blocks, iters) / (e0.elapsed_time(e1) * 1e-3) / 1e12
+
+
+def measured_hbm():
+    """HBM copy bandwidth from MEASURED_PEAKS.json, else the 6.8 TB/s fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s)"
 
 
 def read_traffic(name):
@@ -186,23 +242,34 @@ def run_gpu(args, rank, world, local_rank):
 
     t0 = time.time()
     mesh = DeviceMesh(model.nodes, model.tets, model.p, device=f"cuda:{local_rank}")
+    if not args.no_records:
+        mesh.records()
+        mesh.tables_entry_major(args.assembly)
     torch.cuda.synchronize()
     setup_ms = (time.time() - t0) * 1e3
     T = mesh.T
     sigma = mesh.sigma_tensor(model.sigma)
-    coef = torch.empty((T, 12), dtype=torch.float64, device="cuda")
+    df = args.assembly == "df64"
+    if df:
+        coef = torch.empty((T, 12, 2), dtype=torch.float32, device="cuda")
+    else:
+        coef = torch.empty((T, 12), dtype=torch.float64, device="cuda")
     vals = torch.empty(mesh.nnz, dtype=torch.complex128, device="cuda")
     b = torch.zeros(mesh.N, dtype=torch.complex128, device="cuda")
     src_elem = mesh.locate_source(model.source)
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
-    launches_per_step = 5   # coefficients, fused assembly, source, PEC mark, PEC rows
+    launches_per_step = 4   # coefficients, fused assembly + PEC rows/columns, source, PEC on b
+
+    def assemble():
+        mesh.assemble(sigma, freq, out=vals, coef=coef, arithmetic=args.assembly, pec=True,
+                      records=not args.no_records)
 
     def step():
-        mesh.element_coefficients(sigma, freq, out=coef, check=False)
-        mesh.assemble(sigma, freq, out=vals, coef=coef)
+        mesh.element_coefficients(sigma, freq, out=coef, check=False, arithmetic=args.assembly)
+        assemble()
         b.zero_()
         mesh.source_rhs(model.source, src_elem, b, status=status)
-        mesh.apply_pec(vals, b)
+        mesh.pec_rhs(b)
 
     for _ in range(args.warmup):
         step()
@@ -218,11 +285,13 @@ def run_gpu(args, rank, world, local_rank):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     with ClockSampler(local_rank) as clk:
+        clk.mark_start()
         e0.record()
         for _ in range(args.steps):
             step()
         e1.record()
         barrier()
+        clk.mark_end()
     ms = e0.elapsed_time(e1)
     ms_max = ms
     if dist is not None:
@@ -236,21 +305,38 @@ def run_gpu(args, rank, world, local_rank):
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record()
     for _ in range(args.steps):
-        mesh.assemble(sigma, freq, out=vals, coef=coef)
+        assemble()
     k1.record()
     torch.cuda.synchronize()
     k_ms = k0.elapsed_time(k1) / args.steps
     nd = mesh.nd
-    flops = T * (nd * (nd + 1) // 2) * 12 * 2          # 12 FMA per unique elemental entry
+    flops = T * (nd * (nd + 1) // 2) * 12 * 2          # 12 multiply-adds per unique elemental entry
+    # algorithmic bytes: A values written once; per item its record (or item
+    # word) read once; per element its 12 coefficients and tuple id; every
+    # member of an upper pair (a <= b) once
+    nl = {1: 6, 2: 10}.get(mesh.p, 11)
+    work_bytes = mesh.n_items * (8 if args.no_records else _lib.query("pg_assembly_record_bytes", mesh.nnz))
+    nbytes = int(mesh.nnz * 16 + work_bytes + T * (12 * 8 + 4) + T * (nl * (nl + 1) // 2) * 4)
     peak64 = fp64_peak(torch, lib)
-    achieved = flops / (k_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "kernel": "k_values_sym (fused elemental + CSR assembly)",
-                "achieved": round(achieved, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
-                "frac": round(achieved / peak64, 4), "peak_source": "measured live (FP64 FMA probe)",
-                "traffic": read_traffic("assembly_cfg1_ncu.md"),
-                "algorithmic_flops_per_launch": flops, "ms_per_launch": round(k_ms, 4),
-                "algorithmic_bytes_per_launch": int(mesh.nnz * 16 + mesh.items.numel() * 8 + T * (12 * 8 + 4) +
-                                                    mesh.members.numel() * 4)}
+    if df:
+        hbm = measured_hbm()
+        achieved = nbytes / (k_ms * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": ("k_values_rec<2, df>" if not args.no_records else "k_values_sym_df<2>")
+                    + " (fused elemental + CSR assembly + PEC, double-float)",
+                    "achieved": round(achieved, 1), "peak": hbm[0], "unit": "GB/s", "frac": round(achieved / hbm[0], 4),
+                    "peak_source": hbm[1], "traffic": read_traffic("assembly_df64_cfg1_ncu.md"),
+                    "algorithmic_bytes_per_launch": nbytes, "ms_per_launch": round(k_ms, 4),
+                    "fp64_equivalent_tflops": round(flops / (k_ms * 1e-3) / 1e12, 4),
+                    "fp64_peak_tflops": round(peak64, 4)}
+    else:
+        achieved = flops / (k_ms * 1e-3) / 1e12
+        roofline = {"bound": "fp64", "kernel": ("k_values_rec<2, fp64>" if not args.no_records else "k_values_sym<2>")
+                    + " (fused elemental + CSR assembly + PEC)",
+                    "achieved": round(achieved, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
+                    "frac": round(achieved / peak64, 4), "peak_source": "measured live (FP64 FMA probe)",
+                    "traffic": read_traffic("assembly_cfg1_ncu.md"),
+                    "algorithmic_flops_per_launch": flops, "ms_per_launch": round(k_ms, 4),
+                    "algorithmic_bytes_per_launch": nbytes}
 
     # end to end: host buffers in (pinned), A values and b back to the host
     nodes_h = torch.from_numpy(np.ascontiguousarray(model.nodes)).pin_memory()
@@ -289,8 +375,8 @@ def run_gpu(args, rank, world, local_rank):
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Melem/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
                 "higher_is_better": True, "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic (seeded Kuhn-cube mesh, jittered; log-uniform sigma)",
-                "config": {"workload": WORKLOAD, "p": 2, "tets": T, "dofs": mesh.N, "nnz": mesh.nnz,
+                "dtype": "f64" if not df else "df64 (f32 pairs) -> f64", "data": "synthetic (seeded Kuhn-cube mesh, jittered; log-uniform sigma)",
+                "config": {"workload": workload(args.n), "p": 2, "tets": T, "dofs": mesh.N, "nnz": mesh.nnz,
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "l2": "working set per step > 1 GB (A values alone 876 MB) > 129 MB L2",
                            "pattern_setup_ms": round(setup_ms, 1), "orientation_tuples": mesh.n_tuples},
@@ -321,13 +407,14 @@ def run_solves(args, torch, mesh, model, vals, b):
                    "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4),
                    "relres": info.relres, "converged": info.status == 0}
 
-    srcs = synthetic.config2_sources()[:args.nrhs]
+    # column 0: the workload's own HED; columns 1..: x-HEDs of the batched configuration
+    srcs = [model.source] + synthetic.config2_sources()[:args.nrhs - 1]
     B = torch.zeros((mesh.N, len(srcs)), dtype=torch.complex128, device="cuda")
     for k, s in enumerate(srcs):
         bk = torch.zeros(mesh.N, dtype=torch.complex128, device="cuda")
         mesh.source_rhs(s, mesh.locate_source(s), bk)
         B[:, k] = bk
-    B[mesh.bnd.long(), :] = 0
+    mesh.pec_rhs(B)
     x64, r64 = timed("cocg", "fp64", b, args.max_it)
     xdf, rdf = timed("cocg", "df64", b, args.max_it)
     Xdb, rdb = timed("cocg", "df64", B.contiguous(), args.max_it)
@@ -350,7 +437,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; mixed = complex64 "
                    "matrix/SpMV + FP64 recurrence, which cannot reach 1e-8 at this conditioning (eps32*kappa ~ 1)")
     out["speedup_df64_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rdb["ms_per_rhs"], 1e-9), 2)
-    out["speedup_mixed_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rb["ms_per_rhs"], 1e-9), 2)
+
     return out
 
 
@@ -379,18 +466,22 @@ def run_reference(args, rank):
     from petgem_gb300 import synthetic
     model = synthetic.config1(args.n)
     cores = os.cpu_count() or 1
+    prep = cpu_prepare(model)
     rates = []
     samples = []
-    for _ in range(max(args.steps, 1)):
-        rate, n_el, wall = cpu_assembly_rate(model, args.cpu_seconds / 4, cores)
-        rates.append(rate)
-        samples.append(n_el)
+    # each step a bounded sample; the whole K-step run stays within a few minutes
+    per_step = max(0.5, min(args.cpu_seconds / 4, 120.0 / max(args.steps, 1)))
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for _ in range(max(args.steps, 1)):
+            rate, n_el, wall = cpu_assembly_rate(model, per_step, cores, prep, pool)
+            rates.append(rate)
+            samples.append(n_el)
     v = float(np.median(rates))
     sample = (f"oracle elemental matrices + COO/CSR assembly of the first {samples[0]} of {len(model.tets)} "
               f"elements per step, {cores} processes")
     return {"metric": METRIC, "value": round(v, 6), "unit": "Melem/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD, "p": 2},
+            "dtype": "f64", "data": "synthetic", "config": {"workload": workload(args.n), "p": 2},
             "cpu_baseline": {"value": round(v, 6), "unit": "Melem/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 6), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -213,6 +213,11 @@ int pg_assemble_values(const double* M, const double* K, const int32_t* members,
 int pg_element_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t n_elems,
                             double omega_mu, double* coef, int32_t* status, void* stream);
 
+/* The same coefficients as double-float pairs, float [T*24] = (hi, lo) per
+ * value, for pg_assemble_fused_ex arithmetic 1. */
+int pg_element_coefficients_df(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t n_elems,
+                               double omega_mu, float* coef_pairs, int32_t* status, void* stream);
+
 size_t pg_pattern_items_workspace_bytes(int64_t n_pairs, int64_t max_items);
 
 /* Work list of the symmetric fused assembly: for every entity pair (a, b)
@@ -238,6 +243,59 @@ int pg_assemble_fused(const double* coef, const int32_t* tuple_of_elem, const do
                       const int64_t* items, int64_t n_items, int64_t n_pairs, const int32_t* elemsE,
                       const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, const int64_t* rowptr,
                       double* vals, void* stream);
+
+/* pg_assemble_fused with two options: arithmetic 0 = FP64 (coef, tables
+ * are double), 1 = double-float on the FP32 pipes (coef, tables are (hi, lo)
+ * float pairs from pg_to_double_float; ~2^-48 relative rounding, output
+ * complex128); pec_flags (uint8 [N], from pg_pec_flags, may be NULL) applies
+ * zeroRowsColumns(diag=1) while writing, replacing a pg_apply_pec pass. */
+int pg_assemble_fused_ex(const void* coef, const int32_t* tuple_of_elem, const void* tables, const int32_t* members,
+                         const int32_t* pair_start, const int32_t* pair_colstart, const int32_t* pair_partner,
+                         const int64_t* items, int64_t n_items, int64_t n_pairs, const int32_t* elemsE,
+                         const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, const int64_t* rowptr,
+                         const uint8_t* pec_flags, int arithmetic, double* vals, void* stream);
+
+/* Assembly records: the mesh-only part of every item of the symmetric work
+ * list (pg_pattern_items) resolved once per mesh, in the same order, so the
+ * per-model pass (pg_assemble_records) reads one record, the pair's members,
+ * the element coefficients and one table entry per member.  A record is
+ * pg_assembly_record_bytes(nnz) bytes (16 while nnz < 2^31, else 24): output
+ * position, transpose position, first member, meta (member count, local DOF
+ * indices, transpose / PEC flags).  pec_flags (uint8 [N] from pg_pec_flags,
+ * may be NULL) marks items in PEC rows or columns.  records 16-byte aligned.
+ * status int32 [1] <- PG_ERR_UNSUPPORTED when a pair has > 255 members. */
+int64_t pg_assembly_record_bytes(int64_t nnz);
+int pg_assembly_records(const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
+                        const int32_t* pair_partner, const int64_t* items, int64_t n_items, const int32_t* elemsE,
+                        const int32_t* elemsF, int64_t n_elems, int64_t nE, int64_t nF, int p, const int64_t* rowptr,
+                        int64_t nnz, const uint8_t* pec_flags, void* records, int32_t* status, void* stream);
+
+/* Tables of pg_tuple_tables re-laid entry-major, [U][NT][12] in the order of
+ * the element coefficients: doubles (arithmetic 0) or (hi, lo) float pairs
+ * (arithmetic 1).  out holds U*NT*12 doubles or float pairs. */
+int pg_tuple_tables_entry_major(const double* tables, int64_t n_tuples, int p, int arithmetic, void* out,
+                                void* stream);
+
+/* A values from records: arithmetic 0 = FP64 (coef from
+ * pg_element_coefficients, entry-major double tables), 1 = double-float
+ * (coef from pg_element_coefficients_df, entry-major pair tables); output
+ * complex128 either way.  apply_pec != 0 writes zeroRowsColumns(diag=1)
+ * values for the entries flagged by pg_assembly_records.  coef, tables,
+ * records and vals 16-byte aligned.  Same values, bit for bit, as
+ * pg_assemble_fused_ex with the same arithmetic. */
+int pg_assemble_records(const void* coef, const int32_t* tuple_of_elem, const void* tables_entry_major,
+                        const int32_t* members, const void* records, int64_t n_items, int64_t nnz, int p,
+                        int arithmetic, int apply_pec, double* vals, void* stream);
+
+/* out_pairs [2n] float = (hi, lo) with hi = fl32(x), lo = fl32(x - hi). */
+int pg_to_double_float(const double* in, int64_t n, float* out_pairs, void* stream);
+
+/* flags uint8 [n_dofs] = 1 on the PEC DOFs bnd [n_bnd]. */
+int pg_pec_flags(const int32_t* bnd, int64_t n_bnd, int64_t n_dofs, uint8_t* flags, void* stream);
+
+/* b[bnd[i] * nrhs + k] = 0 for every RHS k (b complex128 [N * nrhs]), the
+ * RHS half of petgem's PEC (solver.py:565-567). */
+int pg_pec_rhs(const int32_t* bnd, int64_t n_bnd, int nrhs, double* b, void* stream);
 
 /* PETSc MatZeroRowsColumns(rows, diag=1) and b[rows] = 0
  * (petgem/solver.py:552-577).  b may be NULL.  flag_ws uint8 [n_dofs]. */

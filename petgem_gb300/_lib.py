@@ -68,11 +68,21 @@ SIGNATURES = {
     "pg_pattern_columns": (_INT, [_P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P]),
     "pg_assemble_values": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _D, _P, _P]),
     "pg_element_coefficients": (_INT, [_P, _P, _P, _I64, _D, _P, _P, _P]),
+    "pg_element_coefficients_df": (_INT, [_P, _P, _P, _I64, _D, _P, _P, _P]),
     "pg_pattern_items_workspace_bytes": (_SZ, [_I64, _I64]),
     "pg_pattern_items": (_INT, [_P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _I64, _P, _P, _P, _P, _SZ, _P]),
     "pg_assemble_fused": (_INT, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P,
                                  _P]),
     "pg_apply_pec": (_INT, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P]),
+    "pg_assemble_fused_ex": (_INT, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _P,
+                                    _INT, _P, _P]),
+    "pg_to_double_float": (_INT, [_P, _I64, _P, _P]),
+    "pg_assembly_record_bytes": (_I64, [_I64]),
+    "pg_assembly_records": (_INT, [_P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64, _INT, _P, _I64, _P, _P, _P, _P]),
+    "pg_tuple_tables_entry_major": (_INT, [_P, _I64, _INT, _INT, _P, _P]),
+    "pg_assemble_records": (_INT, [_P, _P, _P, _P, _P, _I64, _I64, _INT, _INT, _INT, _P, _P]),
+    "pg_pec_flags": (_INT, [_P, _I64, _I64, _P, _P]),
+    "pg_pec_rhs": (_INT, [_P, _I64, _INT, _P, _P]),
     "pg_locate_points": (_INT, [_P, _P, _I64, _P, _I64, _D, _P, _P]),
     "pg_source_rhs": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _P, _D, _D, _P, _P, _P]),
     "pg_gather_fields": (_INT, [_P, _P, _P, _P, _P, _P, _INT, _P, _P, _I64, _D, _P, _P]),

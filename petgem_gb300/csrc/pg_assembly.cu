@@ -20,6 +20,7 @@
 // geometry coefficients and its orientation tuple's moment tables, so the
 // elemental matrices are never written to memory.
 #include "pg_common.cuh"
+#include "pg_df.cuh"
 #include "pg_sort.cuh"
 
 namespace {
@@ -186,9 +187,17 @@ __global__ void k_values_mk(const double* __restrict__ Mm, const double* __restr
   }
 }
 
-// per-element coefficients for the fused path: [cK(6) | -omega mu det S (6)]
+__device__ __forceinline__ void put_coef(double* cf, int t, double v) { cf[t] = v; }
+__device__ __forceinline__ void put_coef(float2* cf, int t, double v) {
+  const float h = __double2float_rn(v);
+  cf[t] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
+// per-element coefficients for the fused path: [cK(6) | -omega mu det S (6)],
+// as doubles or as (hi, lo) double-float pairs
+template <typename C>
 __global__ void k_coefficients(const double* nodes, const int32_t* elemsN, const double* sigma, int64_t T, double omu,
-                               double* coef, int32_t* status) {
+                               C* coef, int32_t* status) {
   GRID_STRIDE(e, T) {
     double x[4][3];
     for (int v = 0; v < 4; ++v) {
@@ -204,10 +213,10 @@ __global__ void k_coefficients(const double* nodes, const int32_t* elemsN, const
     const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
     const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
     const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-    double* cf = coef + 12 * e;
+    C* cf = coef + 12 * e;
     if (!(det != 0.0) || !isfinite(det)) {
       *status = PG_ERR_DEGENERATE;
-      for (int t = 0; t < 12; ++t) cf[t] = 0.0;
+      for (int t = 0; t < 12; ++t) put_coef(cf, t, 0.0);
       continue;
     }
     const double id = 1.0 / det;
@@ -230,8 +239,8 @@ __global__ void k_coefficients(const double* nodes, const int32_t* elemsN, const
         s += inv[c][pa[t]] * D[c] * inv[c][pb[t]];
         g += J[pa[t]][c] * J[pb[t]][c];
       }
-      cf[t] = g * id;
-      cf[6 + t] = -omu * (det * s);
+      put_coef(cf, t, g * id);
+      put_coef(cf, 6 + t, -omu * (det * s));
     }
   }
 }
@@ -240,6 +249,8 @@ __device__ __forceinline__ int packed_index(int j, int k, int nd) {
   if (k < j) { int t = j; j = k; k = t; }
   return j * nd - (j * (j - 1)) / 2 + (k - j);
 }
+
+__device__ __forceinline__ double2 pec_value(const uint8_t* pec, int64_t row, int64_t col, double2 v);
 
 // ---- symmetric item lists: one item per upper entry of every pair with a <= b
 __global__ void k_pair_keys_of(const int32_t* members, const int32_t* pair_start, int64_t n_pairs,
@@ -315,7 +326,7 @@ __global__ void __launch_bounds__(256) k_values_sym(const double* __restrict__ c
                                                     const int32_t* __restrict__ elemsE,
                                                     const int32_t* __restrict__ elemsF, int64_t nE, int64_t nF,
                                                     int64_t T, const int64_t* __restrict__ rowptr,
-                                                    double2* __restrict__ vals) {
+                                                    const uint8_t* __restrict__ pec, double2* __restrict__ vals) {
   constexpr int NL = P == 1 ? 6 : (P == 2 ? 10 : 11);
   constexpr int NL2 = NL * NL;
   constexpr int ND = P * (P + 2) * (P + 3) / 2;
@@ -357,10 +368,95 @@ __global__ void __launch_bounds__(256) k_values_sym(const double* __restrict__ c
     }
     const double2 v = make_double2(re, im);
     const int64_t fa = E.first_dof(a), fb = E.first_dof(b);
-    vals[rowptr[fa + i] + colstart[g] + j] = v;
-    if (a != b) vals[rowptr[fb + j] + colstart[partner[g]] + i] = v;
-    else if (i != j) vals[rowptr[fa + j] + colstart[g] + i] = v;
+    vals[rowptr[fa + i] + colstart[g] + j] = pec_value(pec, fa + i, fb + j, v);
+    if (a != b) vals[rowptr[fb + j] + colstart[partner[g]] + i] = pec_value(pec, fb + j, fa + i, v);
+    else if (i != j) vals[rowptr[fa + j] + colstart[g] + i] = pec_value(pec, fa + j, fa + i, v);
   }
+}
+
+
+// PEC applied while writing (zeroRowsColumns(rows, diag=1), solver.py:562):
+// entries in a boundary row or column become 0, the boundary diagonal 1.
+__device__ __forceinline__ double2 pec_value(const uint8_t* pec, int64_t row, int64_t col, double2 v) {
+  if (pec && (pec[row] | pec[col])) return make_double2(row == col && pec[row] ? 1.0 : 0.0, 0.0);
+  return v;
+}
+
+// Double-float variant of k_values_sym: coefficients and tables are (hi, lo)
+// FP32 pairs, the 12 products per member are double-float multiply-adds on
+// the FP32 pipes; only the final conversion to complex128 uses FP64.
+template <int P>
+__global__ void __launch_bounds__(256) k_values_sym_df(const float2* __restrict__ coef,
+                                                       const int32_t* __restrict__ tuple_of_elem,
+                                                       const float2* __restrict__ tables,
+                                                       const int32_t* __restrict__ members,
+                                                       const int32_t* __restrict__ pair_start,
+                                                       const int32_t* __restrict__ colstart,
+                                                       const int32_t* __restrict__ partner,
+                                                       const int64_t* __restrict__ items, int64_t n_items,
+                                                       const int32_t* __restrict__ elemsE,
+                                                       const int32_t* __restrict__ elemsF, int64_t nE, int64_t nF,
+                                                       int64_t T, const int64_t* __restrict__ rowptr,
+                                                       const uint8_t* __restrict__ pec, double2* __restrict__ vals) {
+  constexpr int NL = P == 1 ? 6 : (P == 2 ? 10 : 11);
+  constexpr int NL2 = NL * NL;
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  constexpr int NT = ND * (ND + 1) / 2;
+  const Ent E(nE, nF, T, P);
+  GRID_STRIDE(idx, n_items) {
+    const int64_t it = items[idx];
+    const int64_t g = it >> 12;
+    int t = (int)(it & 4095);
+    const int32_t s0 = pair_start[g], s1 = pair_start[g + 1];
+    const int32_t m0 = members[s0];
+    const int64_t e0 = m0 / NL2;
+    const int r0 = m0 % NL2;
+    const int64_t a = E.ent(elemsE, elemsF, e0, r0 / NL), b = E.ent(elemsE, elemsF, e0, r0 % NL);
+    const int na = E.nd_ent(a), nb = E.nd_ent(b);
+    int i, j;
+    if (a != b) {
+      i = t / nb;
+      j = t - i * nb;
+    } else {
+      i = 0;
+      while (t >= na - i) { t -= na - i; ++i; }
+      j = i + t;
+    }
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int32_t q = s0; q < s1; ++q) {
+      const int32_t m = members[q];
+      const int64_t e = m / NL2;
+      const int r = m - (int)(e * NL2);
+      const int la = r / NL, lb = r - la * NL;
+      const int jl = E.local_off(la) + i, kl = E.local_off(lb) + j;
+      const float2* tb = tables + (int64_t)__ldg(tuple_of_elem + e) * (12 * NT) + packed_index(jl, kl, ND);
+      const float2* cf = coef + 12 * e;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const float2 ck = __ldg(cf + k), tk = __ldg(tb + (6 + k) * NT);
+        df_mac(rh, rl, ck.x, ck.y, tk.x, tk.y);
+        const float2 cm = __ldg(cf + 6 + k), tm = __ldg(tb + k * NT);
+        df_mac(ih, il, cm.x, cm.y, tm.x, tm.y);
+      }
+    }
+    const double2 v = make_double2(df_to_double(rh, rl), df_to_double(ih, il));
+    const int64_t fa = E.first_dof(a), fb = E.first_dof(b);
+    vals[rowptr[fa + i] + colstart[g] + j] = pec_value(pec, fa + i, fb + j, v);
+    if (a != b) vals[rowptr[fb + j] + colstart[partner[g]] + i] = pec_value(pec, fb + j, fa + i, v);
+    else if (i != j) vals[rowptr[fa + j] + colstart[g] + i] = pec_value(pec, fa + j, fa + i, v);
+  }
+}
+
+__global__ void k_to_df(const double* __restrict__ in, int64_t n, float2* __restrict__ out) {
+  GRID_STRIDE(i, n) {
+    const double v = in[i];
+    const float h = __double2float_rn(v);
+    out[i] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
+__global__ void k_pec_rhs(const int32_t* bnd, int64_t n_bnd, int nrhs, double2* b) {
+  GRID_STRIDE(i, n_bnd * nrhs) b[(int64_t)bnd[i / nrhs] * nrhs + i % nrhs] = make_double2(0.0, 0.0);
 }
 
 __global__ void k_mark_bnd(const int32_t* bnd, int64_t nb, uint8_t* flag, double2* b) {
@@ -511,6 +607,19 @@ extern "C" int pg_element_coefficients(const double* nodes, const int32_t* elems
   return PG_OK;
 }
 
+extern "C" int pg_element_coefficients_df(const double* nodes, const int32_t* elemsN, const double* sigma,
+                                          int64_t n_elems, double omega_mu, float* coef_pairs, int32_t* status,
+                                          void* stream) {
+  if (n_elems < 1 || !nodes || !elemsN || !sigma || !coef_pairs || !status) {
+    pg_set_error("pg_element_coefficients_df: bad argument");
+    return PG_ERR_ARG;
+  }
+  k_coefficients<<<pg_blocks(n_elems, 256), 256, 0, pg_stream(stream)>>>(
+      nodes, elemsN, sigma, n_elems, omega_mu, reinterpret_cast<float2*>(coef_pairs), status);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
 extern "C" size_t pg_pattern_items_workspace_bytes(int64_t n_pairs, int64_t max_items) {
   return pg_align256(sizeof(int64_t) * n_pairs) + pg_align256(sizeof(int32_t) * (n_pairs + 1)) * 2 +
          pg::scan_workspace_bytes(n_pairs + 1) + pg_align256(sizeof(uint64_t) * max_items) +
@@ -588,7 +697,7 @@ extern "C" int pg_assemble_fused(const double* coef, const int32_t* tuple_of_ele
   const unsigned grid = (unsigned)blocks;
 #define PG_SYM(P) k_values_sym<P><<<grid, 256, 0, s>>>(coef, tuple_of_elem, tables, members, pair_start, pair_colstart, \
                                                        pair_partner, items, n_items, elemsE, elemsF, nE, nF, n_elems,   \
-                                                       rowptr, v)
+                                                       rowptr, nullptr, v)
   switch (p) {
     case 1: PG_SYM(1); break;
     case 2: PG_SYM(2); break;
@@ -613,6 +722,421 @@ extern "C" int pg_apply_pec(const int64_t* rowptr, const int32_t* col, double* v
   if (n_bnd > 0)
     k_mark_bnd<<<pg_blocks(n_bnd, 256), 256, 0, s>>>(bnd, n_bnd, flag_ws, reinterpret_cast<double2*>(b));
   k_pec<<<warp_grid(n_dofs), 256, 0, s>>>(rowptr, col, reinterpret_cast<double2*>(vals), n_dofs, flag_ws);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_to_double_float(const double* in, int64_t n, float* out_pairs, void* stream) {
+  if (n < 1 || !in || !out_pairs) {
+    pg_set_error("pg_to_double_float: bad argument");
+    return PG_ERR_ARG;
+  }
+  k_to_df<<<pg_blocks(n, 256), 256, 0, pg_stream(stream)>>>(in, n, reinterpret_cast<float2*>(out_pairs));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_pec_flags(const int32_t* bnd, int64_t n_bnd, int64_t n_dofs, uint8_t* flags, void* stream) {
+  if (n_dofs < 1 || !flags || (n_bnd > 0 && !bnd)) {
+    pg_set_error("pg_pec_flags: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  PG_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)n_dofs, s));
+  if (n_bnd > 0) k_mark_bnd<<<pg_blocks(n_bnd, 256), 256, 0, s>>>(bnd, n_bnd, flags, nullptr);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_pec_rhs(const int32_t* bnd, int64_t n_bnd, int nrhs, double* b, void* stream) {
+  if (nrhs < 1 || !b || (n_bnd > 0 && !bnd)) {
+    pg_set_error("pg_pec_rhs: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (n_bnd > 0)
+    k_pec_rhs<<<pg_blocks(n_bnd * nrhs, 256), 256, 0, pg_stream(stream)>>>(bnd, n_bnd, nrhs,
+                                                                           reinterpret_cast<double2*>(b));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_assemble_fused_ex(const void* coef, const int32_t* tuple_of_elem, const void* tables,
+                                    const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
+                                    const int32_t* pair_partner, const int64_t* items, int64_t n_items,
+                                    int64_t n_pairs, const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems,
+                                    int64_t nE, int64_t nF, int p, const int64_t* rowptr, const uint8_t* pec_flags,
+                                    int arithmetic, double* vals, void* stream) {
+  if (p < 1 || p > 6 || n_pairs < 1 || n_items < 1 || !coef || !tuple_of_elem || !tables || !members ||
+      !pair_start || !pair_colstart || !pair_partner || !items || !rowptr || !vals ||
+      (arithmetic != 0 && arithmetic != 1)) {
+    pg_set_error("pg_assemble_fused_ex: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  double2* v = reinterpret_cast<double2*>(vals);
+  int64_t blocks = (n_items + 255) / 256;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  const unsigned grid = (unsigned)blocks;
+  if (arithmetic == 0) {
+    const double* c = reinterpret_cast<const double*>(coef);
+    const double* tb = reinterpret_cast<const double*>(tables);
+#define PG_SYM64(P) k_values_sym<P><<<grid, 256, 0, s>>>(c, tuple_of_elem, tb, members, pair_start, pair_colstart, \
+                                                         pair_partner, items, n_items, elemsE, elemsF, nE, nF, n_elems, \
+                                                         rowptr, pec_flags, v)
+    switch (p) {
+      case 1: PG_SYM64(1); break;
+      case 2: PG_SYM64(2); break;
+      case 3: PG_SYM64(3); break;
+      case 4: PG_SYM64(4); break;
+      case 5: PG_SYM64(5); break;
+      case 6: PG_SYM64(6); break;
+    }
+#undef PG_SYM64
+  } else {
+    const float2* c = reinterpret_cast<const float2*>(coef);
+    const float2* tb = reinterpret_cast<const float2*>(tables);
+#define PG_SYMDF(P) k_values_sym_df<P><<<grid, 256, 0, s>>>(c, tuple_of_elem, tb, members, pair_start, pair_colstart, \
+                                                            pair_partner, items, n_items, elemsE, elemsF, nE, nF,      \
+                                                            n_elems, rowptr, pec_flags, v)
+    switch (p) {
+      case 1: PG_SYMDF(1); break;
+      case 2: PG_SYMDF(2); break;
+      case 3: PG_SYMDF(3); break;
+      case 4: PG_SYMDF(4); break;
+      case 5: PG_SYMDF(5); break;
+      case 6: PG_SYMDF(6); break;
+    }
+#undef PG_SYMDF
+  }
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+// ---- assembly records: the per-mesh part of the work list resolved once ----
+// One record per item of the symmetric work list, in the same order: the
+// output position of the entry, the position of its transpose, the pair's
+// first member and a meta word.  The per-model pass then reads the record,
+// the members, each member's element coefficients and one table entry: three
+// dependent loads instead of the item -> pair -> member -> entity -> rowptr
+// chain.  (Records covering two columns halve the coefficient loads but need
+// ~2x the registers; on GB300 the lost occupancy cost more than the loads.)
+namespace {
+
+// meta: member count (8 bits) | i (6) << 8 | j (6) << 14 | flags
+constexpr uint32_t REC_HAS_T = 1u << 20;   // transpose position present
+constexpr uint32_t REC_PEC_ZERO = 1u << 21;
+constexpr uint32_t REC_PEC_ONE = 1u << 22;
+
+struct ItemView {
+  int64_t g, a, b, fa, fb;
+  int32_t s0, s1;
+  int na, nb, i, j;
+};
+
+// decode one item (pair << 12 | entry) of the symmetric work list
+__device__ __forceinline__ ItemView view_item(int64_t it, const int32_t* members, const int32_t* pair_start,
+                                              const int32_t* elemsE, const int32_t* elemsF, const Ent& E) {
+  ItemView v;
+  v.g = it >> 12;
+  int t = (int)(it & 4095);
+  v.s0 = pair_start[v.g];
+  v.s1 = pair_start[v.g + 1];
+  const int NL = E.nl, NL2 = E.nl * E.nl;
+  const int32_t m0 = members[v.s0];
+  const int64_t e0 = m0 / NL2;
+  const int r0 = m0 % NL2;
+  v.a = E.ent(elemsE, elemsF, e0, r0 / NL);
+  v.b = E.ent(elemsE, elemsF, e0, r0 % NL);
+  v.na = E.nd_ent(v.a);
+  v.nb = E.nd_ent(v.b);
+  if (v.a != v.b) {
+    v.i = t / v.nb;
+    v.j = t - v.i * v.nb;
+  } else {
+    int i = 0;
+    while (t >= v.na - i) { t -= v.na - i; ++i; }
+    v.i = i;
+    v.j = i + t;
+  }
+  v.fa = E.first_dof(v.a);
+  v.fb = E.first_dof(v.b);
+  return v;
+}
+
+struct RecS {   // nnz < 2^31
+  int32_t pos, tpos, s0;
+  uint32_t meta;
+};
+struct RecL {
+  int64_t pos, tpos;
+  int32_t s0;
+  uint32_t meta;
+};
+__device__ __forceinline__ void rec_put(RecS* r, int64_t idx, int64_t p1, int64_t p2, int32_t s0, uint32_t meta) {
+  reinterpret_cast<int4*>(r)[idx] = make_int4((int32_t)p1, (int32_t)p2, s0, (int32_t)meta);
+}
+__device__ __forceinline__ void rec_put(RecL* r, int64_t idx, int64_t p1, int64_t p2, int32_t s0, uint32_t meta) {
+  long long* q = reinterpret_cast<long long*>(r + idx);
+  q[0] = p1;
+  q[1] = p2;
+  q[2] = (long long)(((unsigned long long)meta << 32) | (uint32_t)s0);
+}
+__device__ __forceinline__ void rec_get(const RecS* r, int64_t idx, int64_t& p1, int64_t& p2, int32_t& s0,
+                                        uint32_t& meta) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(r) + idx);
+  p1 = v.x;
+  p2 = v.y;
+  s0 = v.z;
+  meta = (uint32_t)v.w;
+}
+__device__ __forceinline__ void rec_get(const RecL* r, int64_t idx, int64_t& p1, int64_t& p2, int32_t& s0,
+                                        uint32_t& meta) {
+  const long long* q = reinterpret_cast<const long long*>(r + idx);   // 8-byte aligned only
+  p1 = __ldg(q);
+  p2 = __ldg(q + 1);
+  const unsigned long long w = (unsigned long long)__ldg(q + 2);
+  s0 = (int32_t)(uint32_t)(w & 0xffffffffull);
+  meta = (uint32_t)(w >> 32);
+}
+
+template <typename R>
+__global__ void k_records(const int64_t* __restrict__ items, int64_t n_items, const int32_t* __restrict__ members,
+                          const int32_t* __restrict__ pair_start, const int32_t* __restrict__ colstart,
+                          const int32_t* __restrict__ partner, const int32_t* __restrict__ elemsE,
+                          const int32_t* __restrict__ elemsF, Ent E, const int64_t* __restrict__ rowptr,
+                          const uint8_t* __restrict__ pec, R* __restrict__ recs, int32_t* __restrict__ status) {
+  GRID_STRIDE(idx, n_items) {
+    const ItemView v = view_item(items[idx], members, pair_start, elemsE, elemsF, E);
+    const int64_t row = v.fa + v.i, col = v.fb + v.j;
+    const int64_t p1 = rowptr[row] + colstart[v.g] + v.j;
+    int64_t p2 = 0;
+    uint32_t meta = (uint32_t)(v.s1 - v.s0) | ((uint32_t)v.i << 8) | ((uint32_t)v.j << 14);
+    if (v.a != v.b) {
+      p2 = rowptr[col] + colstart[partner[v.g]] + v.i;
+      meta |= REC_HAS_T;
+    } else if (v.i != v.j) {
+      p2 = rowptr[v.fa + v.j] + colstart[v.g] + v.i;
+      meta |= REC_HAS_T;
+    }
+    if (v.s1 - v.s0 > 255) *status = PG_ERR_UNSUPPORTED;
+    if (pec && (pec[row] | pec[col])) meta |= (row == col) ? REC_PEC_ONE : REC_PEC_ZERO;
+    rec_put(recs, idx, p1, p2, v.s0, meta);
+  }
+}
+
+// tables [U][12][NT] (mass R^ab, then stiffness Q^ab) -> entry-major
+// [U][NT][12] ordered like the coefficients (stiffness first, then mass), as
+// doubles or as (hi, lo) double-float pairs
+template <typename C>
+__global__ void k_tables_entry_major(const double* __restrict__ in, int64_t U, int NT, C* __restrict__ out) {
+  GRID_STRIDE(x, U * NT * 12) {
+    const int k = (int)(x % 12);
+    const int64_t ue = x / 12;
+    const int64_t u = ue / NT;
+    const int en = (int)(ue - u * NT);
+    const int src_k = k < 6 ? 6 + k : k - 6;
+    put_coef(out + x, 0, in[(u * 12 + src_k) * NT + en]);
+  }
+}
+
+template <typename C>
+struct Pack12;
+template <>
+struct Pack12<double> {
+  double2 v[6];
+  __device__ __forceinline__ void load(const double* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) v[k] = __ldg(q + k);
+  }
+};
+template <>
+struct Pack12<float2> {
+  float4 v[6];
+  __device__ __forceinline__ void load(const float2* p) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) v[k] = __ldg(q + k);
+  }
+};
+
+struct AccD {
+  double re = 0.0, im = 0.0;
+  __device__ __forceinline__ void mac(const Pack12<double>& c, const Pack12<double>& t) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      re = fma(c.v[k].x, t.v[k].x, re);
+      re = fma(c.v[k].y, t.v[k].y, re);
+      im = fma(c.v[3 + k].x, t.v[3 + k].x, im);
+      im = fma(c.v[3 + k].y, t.v[3 + k].y, im);
+    }
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2(re, im); }
+};
+struct AccDF {
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  __device__ __forceinline__ void mac(const Pack12<float2>& c, const Pack12<float2>& t) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      df_mac(rh, rl, c.v[k].x, c.v[k].y, t.v[k].x, t.v[k].y);
+      df_mac(rh, rl, c.v[k].z, c.v[k].w, t.v[k].z, t.v[k].w);
+      df_mac(ih, il, c.v[3 + k].x, c.v[3 + k].y, t.v[3 + k].x, t.v[3 + k].y);
+      df_mac(ih, il, c.v[3 + k].z, c.v[3 + k].w, t.v[3 + k].z, t.v[3 + k].w);
+    }
+  }
+  __device__ __forceinline__ double2 value() const {
+    return make_double2(df_to_double(rh, rl), df_to_double(ih, il));
+  }
+};
+
+template <int P, typename C, typename Acc, typename R>
+__global__ void __launch_bounds__(256) k_values_rec(const C* __restrict__ coef, const int32_t* __restrict__ tuple_of_elem,
+                                                    const C* __restrict__ tables, const int32_t* __restrict__ members,
+                                                    const R* __restrict__ recs, int64_t n_items, int apply_pec,
+                                                    double2* __restrict__ vals) {
+  constexpr int NL = P == 1 ? 6 : (P == 2 ? 10 : 11);
+  constexpr int NL2 = NL * NL;
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  constexpr int NT = ND * (ND + 1) / 2;
+  constexpr int DE = P, DF = P * (P - 1);
+  GRID_STRIDE(idx, n_items) {
+    int64_t p1, p2;
+    int32_t s0;
+    uint32_t meta;
+    rec_get(recs, idx, p1, p2, s0, meta);
+    double2 v;
+    if (apply_pec && (meta & (REC_PEC_ZERO | REC_PEC_ONE))) {
+      v = make_double2((meta & REC_PEC_ONE) ? 1.0 : 0.0, 0.0);
+    } else {
+      const int c = (int)(meta & 255u);
+      const int i = (int)((meta >> 8) & 63u), j = (int)((meta >> 14) & 63u);
+      Acc acc;
+      auto entry = [&](int32_t m, const C*& cf, const C*& tb) {
+        const int e = m / NL2;
+        const int r = m - e * NL2;
+        const int la = r / NL, lb = r - la * NL;
+        const int ja = (la < 6 ? la * DE : (la < 10 ? 6 * DE + (la - 6) * DF : 6 * DE + 4 * DF)) + i;
+        const int kb = (lb < 6 ? lb * DE : (lb < 10 ? 6 * DE + (lb - 6) * DF : 6 * DE + 4 * DF)) + j;
+        cf = coef + 12 * (int64_t)e;
+        tb = tables + ((int64_t)__ldg(tuple_of_elem + e) * NT + packed_index(ja, kb, ND)) * 12;
+      };
+      int32_t q = s0;
+      const int32_t qe = s0 + c;
+      for (; q + 1 < qe; q += 2) {
+        const C *cfa, *tba, *cfb, *tbb;
+        entry(__ldg(members + q), cfa, tba);
+        entry(__ldg(members + q + 1), cfb, tbb);
+        Pack12<C> ca, ta, cb, tbv;
+        ca.load(cfa);
+        ta.load(tba);
+        cb.load(cfb);
+        tbv.load(tbb);
+        acc.mac(ca, ta);
+        acc.mac(cb, tbv);
+      }
+      if (q < qe) {
+        const C *cfa, *tba;
+        entry(__ldg(members + q), cfa, tba);
+        Pack12<C> ca, ta;
+        ca.load(cfa);
+        ta.load(tba);
+        acc.mac(ca, ta);
+      }
+      v = acc.value();
+    }
+    vals[p1] = v;
+    if (meta & REC_HAS_T) vals[p2] = v;
+  }
+}
+
+}  // namespace
+
+extern "C" int64_t pg_assembly_record_bytes(int64_t nnz) { return nnz < (1ll << 31) ? 16 : 24; }
+
+extern "C" int pg_assembly_records(const int32_t* members, const int32_t* pair_start, const int32_t* pair_colstart,
+                                   const int32_t* pair_partner, const int64_t* items, int64_t n_items,
+                                   const int32_t* elemsE, const int32_t* elemsF, int64_t n_elems, int64_t nE,
+                                   int64_t nF, int p, const int64_t* rowptr, int64_t nnz, const uint8_t* pec_flags,
+                                   void* records, int32_t* status, void* stream) {
+  if (p < 1 || p > 6 || n_items < 1 || nnz < 1 || !members || !pair_start || !pair_colstart || !pair_partner ||
+      !items || !elemsE || !elemsF || !rowptr || !records || !status) {
+    pg_set_error("pg_assembly_records: bad argument");
+    return PG_ERR_ARG;
+  }
+  if ((reinterpret_cast<uintptr_t>(records) & 15) != 0) {
+    pg_set_error("pg_assembly_records: records must be 16-byte aligned");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  const Ent E(nE, nF, n_elems, p);
+  const unsigned g = pg_blocks(n_items, 256);
+  if (pg_assembly_record_bytes(nnz) == 16)
+    k_records<<<g, 256, 0, s>>>(items, n_items, members, pair_start, pair_colstart, pair_partner, elemsE, elemsF, E,
+                                rowptr, pec_flags, reinterpret_cast<RecS*>(records), status);
+  else
+    k_records<<<g, 256, 0, s>>>(items, n_items, members, pair_start, pair_colstart, pair_partner, elemsE, elemsF, E,
+                                rowptr, pec_flags, reinterpret_cast<RecL*>(records), status);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_tuple_tables_entry_major(const double* tables, int64_t n_tuples, int p, int arithmetic, void* out,
+                                           void* stream) {
+  if (p < 1 || p > 6 || n_tuples < 1 || !tables || !out || (arithmetic != 0 && arithmetic != 1)) {
+    pg_set_error("pg_tuple_tables_entry_major: bad argument");
+    return PG_ERR_ARG;
+  }
+  const int nd = p * (p + 2) * (p + 3) / 2;
+  const int NT = nd * (nd + 1) / 2;
+  cudaStream_t s = pg_stream(stream);
+  const unsigned g = pg_blocks(n_tuples * NT * 12, 256);
+  if (arithmetic == 0)
+    k_tables_entry_major<<<g, 256, 0, s>>>(tables, n_tuples, NT, reinterpret_cast<double*>(out));
+  else
+    k_tables_entry_major<<<g, 256, 0, s>>>(tables, n_tuples, NT, reinterpret_cast<float2*>(out));
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+extern "C" int pg_assemble_records(const void* coef, const int32_t* tuple_of_elem, const void* tables_entry_major,
+                                   const int32_t* members, const void* records, int64_t n_items, int64_t nnz, int p,
+                                   int arithmetic, int apply_pec, double* vals, void* stream) {
+  if (p < 1 || p > 6 || n_items < 1 || nnz < 1 || !coef || !tuple_of_elem || !tables_entry_major || !members ||
+      !records || !vals || (arithmetic != 0 && arithmetic != 1)) {
+    pg_set_error("pg_assemble_records: bad argument");
+    return PG_ERR_ARG;
+  }
+  if ((reinterpret_cast<uintptr_t>(coef) | reinterpret_cast<uintptr_t>(tables_entry_major) |
+       reinterpret_cast<uintptr_t>(records) | reinterpret_cast<uintptr_t>(vals)) & 15) {
+    pg_set_error("pg_assemble_records: coef, tables, records and vals must be 16-byte aligned");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  double2* v = reinterpret_cast<double2*>(vals);
+  int64_t blocks = (n_items + 255) / 256;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  const unsigned grid = (unsigned)blocks;
+  const bool small = pg_assembly_record_bytes(nnz) == 16;
+#define PG_REC(P, C, A, R)                                                                                \
+  k_values_rec<P, C, A, R><<<grid, 256, 0, s>>>(reinterpret_cast<const C*>(coef), tuple_of_elem,        \
+                                                reinterpret_cast<const C*>(tables_entry_major), members, \
+                                                reinterpret_cast<const R*>(records), n_items, apply_pec, v)
+#define PG_REC_P(C, A, R)              \
+  switch (p) {                         \
+    case 1: PG_REC(1, C, A, R); break; \
+    case 2: PG_REC(2, C, A, R); break; \
+    case 3: PG_REC(3, C, A, R); break; \
+    case 4: PG_REC(4, C, A, R); break; \
+    case 5: PG_REC(5, C, A, R); break; \
+    case 6: PG_REC(6, C, A, R); break; \
+  }
+  if (arithmetic == 0) {
+    if (small) { PG_REC_P(double, AccD, RecS) } else { PG_REC_P(double, AccD, RecL) }
+  } else {
+    if (small) { PG_REC_P(float2, AccDF, RecS) } else { PG_REC_P(float2, AccDF, RecL) }
+  }
+#undef PG_REC_P
+#undef PG_REC
   PG_LAUNCH_CHECK();
   return PG_OK;
 }

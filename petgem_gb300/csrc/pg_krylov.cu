@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "pg_common.cuh"
+#include "pg_df.cuh"
 
 namespace {
 
@@ -1233,37 +1234,11 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
 // reliable updates and x.
 // ============================================================================
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// (sh, sl) += (ah, al) * (bh, bl); the accumulator stays unnormalised
-__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
-  const float ph = ah * bh;
-  float pl = fmaf(ah, bh, -ph);
-  pl = fmaf(ah, bl, pl);
-  pl = fmaf(al, bh, pl);
-  float t, e;
-  two_sum(sh, ph, t, e);
-  sh = t;
-  sl = sl + (e + pl);
-}
-
-// (sh, sl) += (bh, bl)
-__device__ __forceinline__ void df_add(float& sh, float& sl, float bh, float bl) {
-  float t, e;
-  two_sum(sh, bh, t, e);
-  sh = t;
-  sl = sl + (e + bl);
-}
-
 __device__ __forceinline__ float4 df_norm(float4 v) {
-  float s = v.x + v.y;
-  const float e1 = v.y - (s - v.x);
-  float t = v.z + v.w;
-  const float e2 = v.w - (t - v.z);
+  const float s = __fadd_rn(v.x, v.y);
+  const float e1 = __fsub_rn(v.y, __fsub_rn(s, v.x));
+  const float t = __fadd_rn(v.z, v.w);
+  const float e2 = __fsub_rn(v.w, __fsub_rn(t, v.z));
   return make_float4(s, e1, t, e2);
 }
 

@@ -193,29 +193,104 @@ class DeviceMesh:
             raise _lib.PetgemError("pg_elemental_matrices", int(st.item()), "degenerate element")
         return M, K
 
-    def element_coefficients(self, sigma, frequency, out=None, check=True):
+    def element_coefficients(self, sigma, frequency, out=None, check=True, arithmetic="fp64"):
+        """Per-element geometry coefficients [T, 12] (float64), or with
+        arithmetic="df64" their (hi, lo) float32 pairs [T, 12, 2]."""
         s = self.sigma_tensor(sigma) if not torch.is_tensor(sigma) else sigma
         omu = 2.0 * math.pi * float(frequency) * MU0
-        coef = out if out is not None else torch.empty((self.T, 12), dtype=torch.float64, device=self.device)
         st = torch.zeros(1, dtype=torch.int32, device=self.device)
-        _lib.call("pg_element_coefficients", _p(self.nodes), _p(self.elemsN), _p(s), self.T, omu, _p(coef), _p(st),
-                  _s())
+        if arithmetic == "df64":
+            coef = out if out is not None else torch.empty((self.T, 12, 2), dtype=torch.float32, device=self.device)
+            fn = "pg_element_coefficients_df"
+        else:
+            coef = out if out is not None else torch.empty((self.T, 12), dtype=torch.float64, device=self.device)
+            fn = "pg_element_coefficients"
+        _lib.call(fn, _p(self.nodes), _p(self.elemsN), _p(s), self.T, omu, _p(coef), _p(st), _s())
         if check and int(st.item()) != 0:
             raise _lib.PetgemError("pg_element_coefficients", int(st.item()), "degenerate element")
         return coef
 
-    def assemble(self, sigma, frequency, fused=True, out=None, coef=None):
-        """A values (complex128 [nnz]) before PEC: sum_e K_e - i omega mu M_e."""
+    def tables_entry_major(self, arithmetic="fp64"):
+        """Moment tables entry-major [U][NT][12] (float64, or (hi, lo) float32
+        pairs for arithmetic="df64"), once per mesh."""
+        key = "_tables_em_" + arithmetic
+        if getattr(self, key, None) is None:
+            n = self.tables.numel()
+            t = torch.empty(n if arithmetic == "fp64" else 2 * n,
+                            dtype=torch.float64 if arithmetic == "fp64" else torch.float32, device=self.device)
+            _lib.call("pg_tuple_tables_entry_major", _p(self.tables), self.n_tuples, self.p,
+                      0 if arithmetic == "fp64" else 1, _p(t), _s())
+            setattr(self, key, t)
+        return getattr(self, key)
+
+    def tables_df(self):
+        """Moment tables as (hi, lo) float32 pairs, table-major like self.tables (once per mesh)."""
+        if getattr(self, "_tables_df", None) is None:
+            t = torch.empty(2 * self.tables.numel(), dtype=torch.float32, device=self.device)
+            _lib.call("pg_to_double_float", _p(self.tables), self.tables.numel(), _p(t), _s())
+            self._tables_df = t
+        return self._tables_df
+
+    def pec_mask(self):
+        """uint8 [N] flags of the PEC DOFs (once per mesh)."""
+        if getattr(self, "_pec_mask", None) is None:
+            f = torch.empty(self.N, dtype=torch.uint8, device=self.device)
+            _lib.call("pg_pec_flags", _p(self.bnd), self.bnd.numel(), self.N, _p(f), _s())
+            self._pec_mask = f
+        return self._pec_mask
+
+    def records(self):
+        """Assembly records (once per mesh): output / transpose position,
+        first member and PEC flags of every item of the work list."""
+        if getattr(self, "_records", None) is None:
+            if self.col is None:
+                self._pattern()
+            rb = _lib.query("pg_assembly_record_bytes", self.nnz)
+            r = torch.empty(self.n_items * rb, dtype=torch.uint8, device=self.device)
+            st = torch.zeros(1, dtype=torch.int32, device=self.device)
+            _lib.call("pg_assembly_records", _p(self.members), _p(self.pair_start), _p(self.pair_colstart),
+                      _p(self.pair_partner), _p(self.items), self.n_items, _p(self.elemsE), _p(self.elemsF), self.T,
+                      self.nE, self.nF, self.p, _p(self.rowptr), self.nnz, _p(self.pec_mask()), _p(r), _p(st), _s())
+            if int(st.item()) != 0:
+                raise _lib.PetgemError("pg_assembly_records", int(st.item()), "a CSR pair has more than 255 members")
+            self._records = r
+        return self._records
+
+    def assemble(self, sigma, frequency, fused=True, out=None, coef=None, arithmetic="fp64", pec=False,
+                 records=True):
+        """A values (complex128 [nnz]): sum_e K_e - i omega mu M_e.
+
+        arithmetic="fp64" multiplies the tables in FP64; "df64" in double-float
+        (FP32 pairs, ~2^-48 relative rounding per product, FP64-class result).
+        pec=True applies zeroRowsColumns(boundaries, diag=1) in the same pass
+        (the matrix half of apply_pec; b still needs pec_rhs).
+        coef: precomputed element_coefficients(..., arithmetic=arithmetic).
+        records=True uses the per-mesh assembly records (pg_assemble_records),
+        False the item list directly (pg_assemble_fused_ex); same values."""
         if self.col is None:
             self._pattern()
         vals = out if out is not None else torch.empty(self.nnz, dtype=torch.complex128, device=self.device)
+        if arithmetic not in ("fp64", "df64"):
+            raise ValueError(f"arithmetic={arithmetic!r}: fp64 or df64")
+        if not fused and (arithmetic != "fp64" or pec):
+            raise ValueError("arithmetic='df64' and pec=True need the fused assembly")
         if fused:
             if coef is None:
-                coef = self.element_coefficients(sigma, frequency)
-            _lib.call("pg_assemble_fused", _p(coef), _p(self.tuple_of_elem), _p(self.tables), _p(self.members),
-                      _p(self.pair_start), _p(self.pair_colstart), _p(self.pair_partner), _p(self.items), self.n_items,
-                      self.n_pairs, _p(self.elemsE), _p(self.elemsF), self.T, self.nE, self.nF, self.p, _p(self.rowptr),
-                      _p(vals), _s())
+                coef = self.element_coefficients(sigma, frequency, arithmetic=arithmetic)
+            want = torch.float64 if arithmetic == "fp64" else torch.float32
+            if coef.dtype != want or coef.numel() != self.T * 12 * (1 if arithmetic == "fp64" else 2):
+                raise ValueError("coef does not match the arithmetic")
+            mode = 0 if arithmetic == "fp64" else 1
+            if records:
+                _lib.call("pg_assemble_records", _p(coef), _p(self.tuple_of_elem), _p(self.tables_entry_major(arithmetic)),
+                          _p(self.members), _p(self.records()), self.n_items, self.nnz, self.p, mode, int(pec),
+                          _p(vals), _s())
+            else:
+                tb = self.tables if mode == 0 else self.tables_df()
+                _lib.call("pg_assemble_fused_ex", _p(coef), _p(self.tuple_of_elem), _p(tb), _p(self.members),
+                          _p(self.pair_start), _p(self.pair_colstart), _p(self.pair_partner), _p(self.items),
+                          self.n_items, self.n_pairs, _p(self.elemsE), _p(self.elemsF), self.T, self.nE, self.nF,
+                          self.p, _p(self.rowptr), _p(self.pec_mask() if pec else None), mode, _p(vals), _s())
         else:
             M, K = self.elemental_matrices(sigma)
             omu = 2.0 * math.pi * float(frequency) * MU0
@@ -223,6 +298,12 @@ class DeviceMesh:
                       _p(self.pair_colstart), self.n_pairs, _p(self.elemsE), _p(self.elemsF), self.T, self.nE, self.nF,
                       self.p, _p(self.rowptr), omu, _p(vals), _s())
         return vals
+
+    def pec_rhs(self, b):
+        """b[boundaries] = 0 for every column of b (solver.py:565-567)."""
+        nrhs = 1 if b.ndim == 1 else int(b.shape[1])
+        _lib.call("pg_pec_rhs", _p(self.bnd), self.bnd.numel(), nrhs, _p(b), _s())
+        return b
 
     def locate(self, pts, tol=1e-12):
         pts_t = torch.as_tensor(np.ascontiguousarray(np.atleast_2d(pts), dtype=np.float64), device=self.device)

@@ -114,6 +114,56 @@ def test_pec_matches_oracle():
     assert rel_norm(b.cpu().numpy(), bo) < ELEM_TOL
 
 
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_assembly_df64_and_fused_pec_vs_golden(p):
+    """Double-float arithmetic, PEC fused into the assembly pass, and the
+    record-based pass (bit-identical to the item-list pass)."""
+    g = load("system_n2.npz")
+    pts, tets, sigma = g["points"], g["tets"], g["sigma"]
+    src = json.loads(str(g["src"]))
+    m = _mesh(pts, tets, p)
+    f = src["frequency"]
+    v_df = m.assemble(sigma, f, arithmetic="df64")
+    assert torch.equal(v_df, m.assemble(sigma, f, arithmetic="df64"))          # bitwise reproducible
+    assert torch.equal(v_df, m.assemble(sigma, f, arithmetic="df64", records=False))
+    assert rel_norm(v_df.cpu().numpy(), g[f"p{p}_data"]) < ELEM_TOL
+    v64 = m.assemble(sigma, f)
+    assert torch.equal(v64, m.assemble(sigma, f, records=False))
+    Ar = sp.csr_matrix((g[f"p{p}_data"], g[f"p{p}_indices"], g[f"p{p}_indptr"]), shape=(m.N, m.N))
+    Ao, bo = fem.apply_pec(Ar, g[f"p{p}_b"], g[f"p{p}_bnd"])
+    # fused PEC in FP64 equals assemble + apply_pec bit for bit
+    v_sep = v64.clone()
+    b_sep, _ = m.source_vector(src)
+    m.apply_pec(v_sep, b_sep)
+    for rec in (True, False):
+        assert torch.equal(m.assemble(sigma, f, pec=True, records=rec), v_sep)
+    b, _ = m.source_vector(src)
+    m.pec_rhs(b)
+    assert torch.equal(b, b_sep)
+    assert rel_norm(b.cpu().numpy(), bo) < ELEM_TOL
+    for rec in (True, False):
+        A = _csr(m, m.assemble(sigma, f, arithmetic="df64", pec=True, records=rec))
+        assert abs(A - Ao).max() <= ELEM_TOL * abs(Ao).max()
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_assembly_df64_test_mesh_vs_oracle(p):
+    pts, tets, phys = load_test_mesh()
+    rng = np.random.default_rng(5)
+    s = 10.0 ** rng.uniform(-3, 1, len(tets))
+    sigma = np.stack([s, s * rng.uniform(0.2, 1.0, len(tets))], 1)
+    m = _mesh(pts, tets, p)
+    Ao = _oracle_A(pts, tets, sigma, p, 7.5)
+    v = m.assemble(sigma, 7.5, arithmetic="df64")
+    assert torch.equal(v, m.assemble(sigma, 7.5, arithmetic="df64", records=False))
+    assert rel_norm(v.cpu().numpy(), Ao.data) < ELEM_TOL
+    # each entry to df64 rounding relative to its row scale
+    d = np.abs(v.cpu().numpy() - Ao.data)
+    rowmax = np.maximum.reduceat(np.abs(Ao.data), Ao.indptr[:-1])
+    scale = np.repeat(rowmax, np.diff(Ao.indptr))
+    assert (d <= 1e-12 * scale).all()
+
+
 @pytest.mark.parametrize("ksp,precision", [("gmres", "fp64"), ("gmres", "mixed"), ("cocg", "fp64"),
                                            ("cocg", "mixed"), ("cocg", "df64")])
 def test_solve_and_receivers_vs_reference(precision, ksp):
