@@ -217,6 +217,8 @@ def measured_hbm():
 
 def read_traffic(name):
     """dram bytes per launch recorded in a committed ncu summary, if present."""
+    if name is None:
+        return None
     path = os.path.join(ROOT, "profiles", name)
     try:
         for ln in open(path):
@@ -260,16 +262,25 @@ def run_gpu(args, rank, world, local_rank):
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     launches_per_step = 4   # coefficients, fused assembly + PEC rows/columns, source, PEC on b
 
-    def assemble():
-        mesh.assemble(sigma, freq, out=vals, coef=coef, arithmetic=args.assembly, pec=True,
+    def assemble(v=None):
+        mesh.assemble(sigma, freq, out=vals if v is None else v, coef=coef, arithmetic=args.assembly, pec=True,
                       records=not args.no_records)
 
-    def step():
+    side = torch.cuda.Stream()
+
+    def step(v=None, bv=None):
+        # the RHS (zero, point dipole, PEC rows of b) runs on a second stream
+        # beside the matrix pass; the step ends when both have finished
+        bv = b if bv is None else bv
+        main = torch.cuda.current_stream()
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            bv.zero_()
+            mesh.source_rhs(model.source, src_elem, bv, status=status)
+            mesh.pec_rhs(bv)
         mesh.element_coefficients(sigma, freq, out=coef, check=False, arithmetic=args.assembly)
-        assemble()
-        b.zero_()
-        mesh.source_rhs(model.source, src_elem, b, status=status)
-        mesh.pec_rhs(b)
+        assemble(v)
+        main.wait_stream(side)
 
     for _ in range(args.warmup):
         step()
@@ -324,7 +335,8 @@ def run_gpu(args, rank, world, local_rank):
         roofline = {"bound": "hbm", "kernel": ("k_values_rec<2, df>" if not args.no_records else "k_values_sym_df<2>")
                     + " (fused elemental + CSR assembly + PEC, double-float)",
                     "achieved": round(achieved, 1), "peak": hbm[0], "unit": "GB/s", "frac": round(achieved / hbm[0], 4),
-                    "peak_source": hbm[1], "traffic": read_traffic("assembly_df64_cfg1_ncu.md"),
+                    "peak_source": hbm[1],
+                    "traffic": read_traffic("assembly_records_df64_p2_ncu.md" if not args.no_records else None),
                     "algorithmic_bytes_per_launch": nbytes, "ms_per_launch": round(k_ms, 4),
                     "fp64_equivalent_tflops": round(flops / (k_ms * 1e-3) / 1e12, 4),
                     "fp64_peak_tflops": round(peak64, 4)}
@@ -334,35 +346,60 @@ def run_gpu(args, rank, world, local_rank):
                     + " (fused elemental + CSR assembly + PEC)",
                     "achieved": round(achieved, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
                     "frac": round(achieved / peak64, 4), "peak_source": "measured live (FP64 FMA probe)",
-                    "traffic": read_traffic("assembly_cfg1_ncu.md"),
+                    "traffic": read_traffic("assembly_records_fp64_p2_ncu.md" if not args.no_records else None),
                     "algorithmic_flops_per_launch": flops, "ms_per_launch": round(k_ms, 4),
                     "algorithmic_bytes_per_launch": nbytes}
 
-    # end to end: host buffers in (pinned), A values and b back to the host
+    # end to end: host buffers in (pinned), A values and b back to the host.
+    # Two device / host buffer pairs: the read-back of step k (host link,
+    # ~190 GB/s on GB300) overlaps the assembly of step k + 1.
     nodes_h = torch.from_numpy(np.ascontiguousarray(model.nodes)).pin_memory()
     sigma_h = torch.from_numpy(np.ascontiguousarray(model.sigma)).pin_memory()
-    vals_h = torch.empty(mesh.nnz, dtype=torch.complex128).pin_memory()
-    b_h = torch.empty(mesh.N, dtype=torch.complex128).pin_memory()
+    vals2 = [vals, torch.empty_like(vals)]
+    b2 = [b, torch.empty_like(b)]
+    vals_h = [torch.empty(mesh.nnz, dtype=torch.complex128).pin_memory() for _ in range(2)]
+    b_h = [torch.empty(mesh.N, dtype=torch.complex128).pin_memory() for _ in range(2)]
+    copier = torch.cuda.Stream()
+    copied = [None, None]
 
-    def e2e_step():
+    def e2e_step(k):
+        i = k % 2
+        main = torch.cuda.current_stream()
+        if copied[i] is not None:
+            main.wait_event(copied[i])              # buffer pair i has reached the host
         mesh.nodes.copy_(nodes_h, non_blocking=True)
         sigma.copy_(sigma_h, non_blocking=True)
-        step()
-        vals_h.copy_(vals, non_blocking=True)
-        b_h.copy_(b, non_blocking=True)
+        step(vals2[i], b2[i])
+        ready = torch.cuda.Event()
+        ready.record(main)
+        copier.wait_event(ready)
+        with torch.cuda.stream(copier):
+            vals_h[i].copy_(vals2[i], non_blocking=True)
+            b_h[i].copy_(b2[i], non_blocking=True)
+            copied[i] = torch.cuda.Event()
+            copied[i].record(copier)
 
-    for _ in range(2):
-        e2e_step()
+    def e2e_drain():
+        torch.cuda.current_stream().wait_stream(copier)
+
+    for k in range(2):
+        e2e_step(k)
+    e2e_drain()
     barrier()
     e0.record()
-    for _ in range(args.steps):
-        e2e_step()
+    for k in range(args.steps):
+        e2e_step(k)
+    e2e_drain()
     e1.record()
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
+    if not torch.equal(vals_h[(args.steps - 1) % 2][:1024], vals[:1024].cpu()):
+        raise RuntimeError("end-to-end read-back does not match the device values")
     e2e = {"value": round(world * T / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Melem/s",
            "h2d_bytes_per_step": int(nodes_h.numel() * 8 + sigma_h.numel() * 8),
-           "d2h_bytes_per_step": int(vals_h.numel() * 16 + b_h.numel() * 16), "ms_per_step": round(e2e_ms, 3)}
+           "d2h_bytes_per_step": int(vals.numel() * 16 + b.numel() * 16), "ms_per_step": round(e2e_ms, 3),
+           "pipelined": "read-back of step k overlaps step k + 1 (two buffer pairs)"}
+    del vals2[1], b2[1]
 
     solve = None
     if args.solve_iters > 0 and rank == 0:

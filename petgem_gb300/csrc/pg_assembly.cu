@@ -245,6 +245,71 @@ __global__ void k_coefficients(const double* nodes, const int32_t* elemsN, const
   }
 }
 
+// The per-element coefficients in double-float arithmetic on the FP32 pipes
+// (the FP64 form spends ~180 FP64 operations per element, which on GB300's
+// ~2 FP64 operations per clock per SM made it the second-largest kernel of an
+// assembly pass).  J = x_r - x_0 is formed in FP64 (exact up to rounding of
+// the difference) and split; then, with adj(J) the adjugate (inv J =
+// adj / det):  cK = J J^T / det,  cM = -omega mu adj^T D adj / det.
+__global__ void k_coefficients_dfa(const double* __restrict__ nodes, const int32_t* __restrict__ elemsN,
+                                   const double* __restrict__ sigma, int64_t T, float omu_h, float omu_l,
+                                   float2* __restrict__ coef, int32_t* __restrict__ status) {
+  GRID_STRIDE(e, T) {
+    double x0[3];
+    dfv J[3][3];
+    {
+      const int64_t n0 = elemsN[4 * e];
+      for (int c = 0; c < 3; ++c) x0[c] = nodes[3 * n0 + c];
+      for (int r = 0; r < 3; ++r) {
+        const int64_t n = elemsN[4 * e + r + 1];
+        for (int c = 0; c < 3; ++c) J[r][c] = df_from_double(nodes[3 * n + c] - x0[c]);
+      }
+    }
+    auto cross = [&](int a, int b, int c, int d, int f, int g, int h, int k) {
+      // J[a][b] J[c][d] - J[f][g] J[h][k]
+      return df_sum(df_mul(J[a][b], J[c][d]), df_neg(df_mul(J[f][g], J[h][k])));
+    };
+    dfv A[3][3];   // adjugate, inv J = A / det
+    A[0][0] = cross(1, 1, 2, 2, 1, 2, 2, 1);
+    A[1][0] = cross(1, 2, 2, 0, 1, 0, 2, 2);
+    A[2][0] = cross(1, 0, 2, 1, 1, 1, 2, 0);
+    A[0][1] = cross(0, 2, 2, 1, 0, 1, 2, 2);
+    A[1][1] = cross(0, 0, 2, 2, 0, 2, 2, 0);
+    A[2][1] = cross(0, 1, 2, 0, 0, 0, 2, 1);
+    A[0][2] = cross(0, 1, 1, 2, 0, 2, 1, 1);
+    A[1][2] = cross(0, 2, 1, 0, 0, 0, 1, 2);
+    A[2][2] = cross(0, 0, 1, 1, 0, 1, 1, 0);
+    const dfv det = df_sum(df_sum(df_mul(J[0][0], A[0][0]), df_mul(J[0][1], A[1][0])), df_mul(J[0][2], A[2][0]));
+    float2* cf = coef + 12 * e;
+    if (!(det.h != 0.f) || !isfinite(det.h)) {
+      *status = PG_ERR_DEGENERATE;
+      for (int t = 0; t < 12; ++t) cf[t] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const dfv id = df_rcp(det);
+    const dfv sh = df_from_double(sigma[2 * e]), sv = df_from_double(sigma[2 * e + 1]);
+    const dfv D[3] = {sh, sh, sv};
+    dfv W[3][3];   // W[c][a] = D[c] A[c][a]
+    for (int c = 0; c < 3; ++c)
+      for (int a = 0; a < 3; ++a) W[c][a] = df_mul(D[c], A[c][a]);
+    const dfv m = df_neg(df_mul(dfv{omu_h, omu_l}, id));
+    const int pa[6] = {0, 1, 2, 0, 0, 1};
+    const int pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      dfv g = df_mul(J[pa[t]][0], J[pb[t]][0]);
+      dfv s = df_mul(W[0][pa[t]], A[0][pb[t]]);
+      for (int c = 1; c < 3; ++c) {
+        g = df_sum(g, df_mul(J[pa[t]][c], J[pb[t]][c]));
+        s = df_sum(s, df_mul(W[c][pa[t]], A[c][pb[t]]));
+      }
+      const dfv k = df_mul(g, id), mm = df_mul(s, m);
+      cf[t] = make_float2(k.h, k.l);
+      cf[6 + t] = make_float2(mm.h, mm.l);
+    }
+  }
+}
+
 __device__ __forceinline__ int packed_index(int j, int k, int nd) {
   if (k < j) { int t = j; j = k; k = t; }
   return j * nd - (j * (j - 1)) / 2 + (k - j);
@@ -614,8 +679,10 @@ extern "C" int pg_element_coefficients_df(const double* nodes, const int32_t* el
     pg_set_error("pg_element_coefficients_df: bad argument");
     return PG_ERR_ARG;
   }
-  k_coefficients<<<pg_blocks(n_elems, 256), 256, 0, pg_stream(stream)>>>(
-      nodes, elemsN, sigma, n_elems, omega_mu, reinterpret_cast<float2*>(coef_pairs), status);
+  const float omu_h = (float)omega_mu;
+  const float omu_l = (float)(omega_mu - (double)omu_h);
+  k_coefficients_dfa<<<pg_blocks(n_elems, 256), 256, 0, pg_stream(stream)>>>(
+      nodes, elemsN, sigma, n_elems, omu_h, omu_l, reinterpret_cast<float2*>(coef_pairs), status);
   PG_LAUNCH_CHECK();
   return PG_OK;
 }

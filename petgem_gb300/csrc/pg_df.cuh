@@ -61,3 +61,60 @@ __device__ __forceinline__ double f32_to_f64_exact(float f) {
 __device__ __forceinline__ double df_to_double(float hi, float lo) {
   return __dadd_rn(f32_to_f64_exact(hi), f32_to_f64_exact(lo));
 }
+
+// ---- double-float values as a pair ------------------------------------------
+struct dfv {
+  float h, l;
+};
+
+// (a + b) renormalised, assuming |a| >= |b| (fast two-sum)
+__device__ __forceinline__ dfv df_quick(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return dfv{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dfv df_mul(dfv a, dfv b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return df_quick(p, e);
+}
+
+__device__ __forceinline__ dfv df_sum(dfv a, dfv b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return df_quick(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+
+__device__ __forceinline__ dfv df_neg(dfv a) { return dfv{-a.h, -a.l}; }
+
+// 1 / a: FP32 reciprocal refined by one double-float Newton step
+__device__ __forceinline__ dfv df_rcp(dfv a) {
+  const float r0 = __frcp_rn(a.h);
+  const dfv ar = df_mul(a, dfv{r0, 0.f});
+  const dfv e = df_sum(dfv{1.f, 0.f}, df_neg(ar));          // 1 - a r0, small
+  return df_sum(dfv{r0, 0.f}, df_mul(dfv{r0, 0.f}, e));
+}
+
+// double -> double-float with integer instructions: hi = the leading 24
+// significant bits of v (truncated), lo = the next 24 bits of the remainder
+// (truncated), so hi + lo = v within 2^-48 |v|.  Magnitudes outside
+// [2^-70, 2^100] (including 0, inf, nan) take a conversion instruction.
+__device__ __forceinline__ dfv df_from_double(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const uint32_t hi32 = (uint32_t)(u >> 32), lo32 = (uint32_t)u;
+  const int e = (int)((hi32 >> 20) & 0x7ffu) - 1023;
+  if (e < -70 || e > 100) return dfv{__double2float_rn(v), 0.f};
+  const uint32_t sign = hi32 & 0x80000000u;
+  const uint32_t m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+  const float h = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | m23);
+  const uint32_t r = lo32 & 0x1fffffffu;   // remainder r * 2^(e - 52)
+  float l = 0.f;
+  if (r != 0u) {
+    const int k = 31 - __clz(r);            // leading bit of r, 0..28
+    const uint32_t mant = k >= 23 ? (r >> (k - 23)) : (r << (23 - k));
+    l = __uint_as_float(sign | ((uint32_t)(e - 52 + k + 127) << 23) | (mant & 0x7fffffu));
+  }
+  return dfv{h, l};
+}

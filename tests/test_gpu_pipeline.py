@@ -154,6 +154,12 @@ def test_assembly_df64_test_mesh_vs_oracle(p):
     sigma = np.stack([s, s * rng.uniform(0.2, 1.0, len(tets))], 1)
     m = _mesh(pts, tets, p)
     Ao = _oracle_A(pts, tets, sigma, p, 7.5)
+    # double-float element coefficients against the FP64 ones, per element
+    c64 = m.element_coefficients(sigma, 7.5).cpu().numpy()
+    cdf = m.element_coefficients(sigma, 7.5, arithmetic="df64").cpu().numpy().astype(np.float64)
+    cdf = cdf[..., 0] + cdf[..., 1]
+    err = np.abs(cdf - c64).max(axis=1) / np.abs(c64).max(axis=1)
+    assert err.max() < 1e-13
     v = m.assemble(sigma, 7.5, arithmetic="df64")
     assert torch.equal(v, m.assemble(sigma, 7.5, arithmetic="df64", records=False))
     assert rel_norm(v.cpu().numpy(), Ao.data) < ELEM_TOL
