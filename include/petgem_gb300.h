@@ -329,6 +329,31 @@ int pg_gather_fields(const double* x, const double* nodes, const int32_t* elemsN
                      double omega_mu, double* fields, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Adjoint gradient of a receiver misfit (no petgem counterpart; built from
+ * the elemental mass matrices of hvfem.py:223-316 and the interpolation of
+ * postprocessing.py:566-614).
+ * ---------------------------------------------------------------------- */
+
+/* Transpose of the E part of pg_gather_fields: b[dofs_e(r)] +=
+ * sum_c N^c_j(xi_r) weights[r][c] (weights complex128 [n_pts, 3]; receivers
+ * with elem < 0 are skipped).  Receivers are added in order (deterministic).
+ * Workspace: pg_receiver_adjoint_workspace_bytes(p, n_pts). */
+size_t pg_receiver_adjoint_workspace_bytes(int p, int64_t n_pts);
+int pg_receiver_adjoint(const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo,
+                        const int32_t* dofs, int p, const double* pts, const int32_t* elem, int64_t n_pts,
+                        const double* weights, double* b, void* workspace, size_t workspace_bytes, void* stream);
+
+/* out[e] (complex128 [T]) = y_e^T (-omega mu M_e) x_e, with x_e = x[dofs_e],
+ * y_e = y[dofs_e] and the mass coefficients of pg_element_coefficients
+ * (coef[e][6..11]) against the table-major tables of pg_tuple_tables.  The
+ * gradient of phi = sum |E_rx - d|^2 with respect to m_e = log10 sigma_e is
+ * 2 ln(10) Im(out[e]) for x = u (forward field) and y = lambda (adjoint
+ * field, A lambda = G^T conj(E_rx - d) with PEC rows zeroed). */
+int pg_element_mass_bilinear(const double* coef, const int32_t* tuple_of_elem, const double* tables,
+                             const int32_t* dofs, const double* x, const double* y, int64_t n_elems, int p,
+                             double* out, void* stream);
+
+/* ------------------------------------------------------------------------
  * Krylov (replaces the PETSc KSP of petgem/solver.py:584-594)
  * --------------------------------------------------------------------- */
 

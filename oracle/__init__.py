@@ -19,6 +19,8 @@ function by function, each citing the petgem file:line it follows:
                           interpolation (hvfem.py, solver.py, postprocessing.py).
 * ``oracle.solve``     -- scipy stand-ins for the PETSc KSP solve
                           (solver.py:584-594).
+* ``oracle.adjoint``   -- receiver-misfit gradient (adjoint) and central
+                          finite differences of the oracle forward model.
 
 Parity pinning: the oracle is checked against golden vectors produced by
 running the reference's own functions (``tests/golden/make_golden.py``) and

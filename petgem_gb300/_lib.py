@@ -86,6 +86,9 @@ SIGNATURES = {
     "pg_locate_points": (_INT, [_P, _P, _I64, _P, _I64, _D, _P, _P]),
     "pg_source_rhs": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _P, _D, _D, _P, _P, _P]),
     "pg_gather_fields": (_INT, [_P, _P, _P, _P, _P, _P, _INT, _P, _P, _I64, _D, _P, _P]),
+    "pg_receiver_adjoint_workspace_bytes": (_SZ, [_INT, _I64]),
+    "pg_receiver_adjoint": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _I64, _P, _P, _P, _SZ, _P]),
+    "pg_element_mass_bilinear": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _INT, _P, _P]),
     "pg_spmv_z": (_INT, [_P, _P, _P, _I64, _P, _P, _INT, _P]),
     "pg_spmv_c": (_INT, [_P, _P, _P, _I64, _P, _P, _INT, _P]),
     "pg_gmres_default_opts": (None, [_PO]),

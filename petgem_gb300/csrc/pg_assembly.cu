@@ -1207,3 +1207,100 @@ extern "C" int pg_assemble_records(const void* coef, const int32_t* tuple_of_ele
   PG_LAUNCH_CHECK();
   return PG_OK;
 }
+
+// ---- per-element bilinear form of the mass term (adjoint contraction) --------
+// out[e] = y_e^T (sum_t cM_t R^t) x_e = y_e^T (-omega mu M_e) x_e with x_e, y_e
+// the element's DOF values; one warp per element, packed symmetric entries
+// over the lanes, fixed-order warp reduction.
+namespace {
+
+// inverse of packed_index: row j (the largest with start(j) <= t) and column k
+__device__ __forceinline__ void unpack_index(int t, int nd, int& j, int& k) {
+  const float b = 2.0f * nd + 1.0f;
+  int r = (int)floorf(0.5f * (b - sqrtf(fmaxf(b * b - 8.0f * t, 0.0f))));
+  r = max(0, min(r, nd - 1));
+  while (r > 0 && r * nd - r * (r - 1) / 2 > t) --r;
+  while (r + 1 < nd && (r + 1) * nd - (r + 1) * r / 2 <= t) ++r;
+  j = r;
+  k = r + (t - (r * nd - r * (r - 1) / 2));
+}
+
+template <int P>
+__global__ void __launch_bounds__(256) k_mass_bilinear(const double* __restrict__ coef,
+                                                       const int32_t* __restrict__ tuple_of_elem,
+                                                       const double* __restrict__ tables,
+                                                       const int32_t* __restrict__ dofs, const double2* __restrict__ x,
+                                                       const double2* __restrict__ y, int64_t T,
+                                                       double2* __restrict__ out) {
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  constexpr int NT = ND * (ND + 1) / 2;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < T; e += warps) {
+    const int32_t* de = dofs + e * ND;
+    const double* tb = tables + (int64_t)tuple_of_elem[e] * (12 * NT);
+    double qr[6] = {0, 0, 0, 0, 0, 0}, qi[6] = {0, 0, 0, 0, 0, 0};
+    for (int t = lane; t < NT; t += 32) {
+      int j, k;
+      unpack_index(t, ND, j, k);
+      const double2 yj = y[de[j]], xk = x[de[k]];
+      double sr = yj.x * xk.x - yj.y * xk.y, si = yj.x * xk.y + yj.y * xk.x;
+      if (j != k) {
+        const double2 yk = y[de[k]], xj = x[de[j]];
+        sr += yk.x * xj.x - yk.y * xj.y;
+        si += yk.x * xj.y + yk.y * xj.x;
+      }
+#pragma unroll
+      for (int a = 0; a < 6; ++a) {
+        const double r = tb[a * NT + t];
+        qr[a] = fma(r, sr, qr[a]);
+        qi[a] = fma(r, si, qi[a]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      for (int off = 16; off > 0; off >>= 1) {
+        qr[a] += __shfl_xor_sync(0xffffffffu, qr[a], off);
+        qi[a] += __shfl_xor_sync(0xffffffffu, qi[a], off);
+      }
+    if (lane == 0) {
+      double orr = 0.0, oi = 0.0;
+      for (int a = 0; a < 6; ++a) {
+        const double c = coef[12 * e + 6 + a];
+        orr = fma(c, qr[a], orr);
+        oi = fma(c, qi[a], oi);
+      }
+      out[e] = make_double2(orr, oi);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int pg_element_mass_bilinear(const double* coef, const int32_t* tuple_of_elem, const double* tables,
+                                        const int32_t* dofs, const double* x, const double* y, int64_t n_elems,
+                                        int p, double* out, void* stream) {
+  if (p < 1 || p > 6 || n_elems < 1 || !coef || !tuple_of_elem || !tables || !dofs || !x || !y || !out) {
+    pg_set_error("pg_element_mass_bilinear: bad argument");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  int64_t blocks = (n_elems + 7) / 8;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  const unsigned grid = (unsigned)blocks;
+  const double2* xx = reinterpret_cast<const double2*>(x);
+  const double2* yy = reinterpret_cast<const double2*>(y);
+  double2* o = reinterpret_cast<double2*>(out);
+#define PG_MB(P) k_mass_bilinear<P><<<grid, 256, 0, s>>>(coef, tuple_of_elem, tables, dofs, xx, yy, n_elems, o)
+  switch (p) {
+    case 1: PG_MB(1); break;
+    case 2: PG_MB(2); break;
+    case 3: PG_MB(3); break;
+    case 4: PG_MB(4); break;
+    case 5: PG_MB(5); break;
+    case 6: PG_MB(6); break;
+  }
+#undef PG_MB
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

@@ -264,3 +264,90 @@ extern "C" int pg_gather_fields(const double* x, const double* nodes, const int3
   PG_LAUNCH_CHECK();
   return PG_OK;
 }
+
+// ---- adjoint of the receiver gather (E part) ----------------------------------
+// b[dofs_e(r)] += sum_c N^c_j(xi_r) w[r][c]: the transpose of E = G x, used as
+// the adjoint right-hand side G^T conj(E - d) of a receiver misfit.
+namespace {
+
+template <int P>
+__global__ void k_receiver_weights(const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo,
+                                   const double* pts, const int32_t* elem, int64_t R, const double2* w,
+                                   double2* contrib) {
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < R; r += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t e = elem[r];
+    double2* out = contrib + r * ND;
+    Geo g;
+    if (e < 0 || !load_geo(nodes, elemsN, e, g)) {
+      for (int j = 0; j < ND; ++j) out[j] = make_double2(0.0, 0.0);
+      continue;
+    }
+    double N[3 * ND];
+    phys_basis<P>(g, eo + 6 * (int64_t)e, fo + 4 * (int64_t)e, pts + 3 * r, N, nullptr);
+    const double2 w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+    for (int j = 0; j < ND; ++j) {
+      const double a = N[j], b = N[ND + j], c = N[2 * ND + j];
+      out[j] = make_double2(a * w0.x + b * w1.x + c * w2.x, a * w0.y + b * w1.y + c * w2.y);
+    }
+  }
+}
+
+// one block: receivers in order (deterministic), the element's DOFs in parallel
+template <int P>
+__global__ void k_receiver_scatter(const int32_t* dofs, const int32_t* elem, int64_t R, const double2* contrib,
+                                   double2* b) {
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  for (int64_t r = 0; r < R; ++r) {
+    const int32_t e = elem[r];
+    if (e >= 0)
+      for (int j = threadIdx.x; j < ND; j += blockDim.x) {
+        const int64_t d = dofs[(int64_t)e * ND + j];
+        const double2 c = contrib[r * ND + j];
+        b[d].x += c.x;
+        b[d].y += c.y;
+      }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+extern "C" size_t pg_receiver_adjoint_workspace_bytes(int p, int64_t n_pts) {
+  if (p < 1 || p > 6 || n_pts < 1) return 0;
+  const int64_t nd = p * (p + 2) * (p + 3) / 2;
+  return (size_t)(16 * nd * n_pts);
+}
+
+extern "C" int pg_receiver_adjoint(const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo,
+                                   const int32_t* dofs, int p, const double* pts, const int32_t* elem, int64_t n_pts,
+                                   const double* weights, double* b, void* workspace, size_t workspace_bytes,
+                                   void* stream) {
+  if (n_pts < 1 || p < 1 || p > 6 || !nodes || !elemsN || !eo || !fo || !dofs || !pts || !elem || !weights || !b) {
+    pg_set_error("pg_receiver_adjoint: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (!workspace || workspace_bytes < pg_receiver_adjoint_workspace_bytes(p, n_pts)) {
+    pg_set_error("pg_receiver_adjoint: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  cudaStream_t s = pg_stream(stream);
+  const double2* w = reinterpret_cast<const double2*>(weights);
+  double2* c = reinterpret_cast<double2*>(workspace);
+  double2* bb = reinterpret_cast<double2*>(b);
+  const unsigned grid = pg_blocks(n_pts, 64);
+#define PG_RADJ(P)                                                                             \
+  k_receiver_weights<P><<<grid, 64, 0, s>>>(nodes, elemsN, eo, fo, pts, elem, n_pts, w, c); \
+  k_receiver_scatter<P><<<1, 64, 0, s>>>(dofs, elem, n_pts, c, bb)
+  switch (p) {
+    case 1: PG_RADJ(1); break;
+    case 2: PG_RADJ(2); break;
+    case 3: PG_RADJ(3); break;
+    case 4: PG_RADJ(4); break;
+    case 5: PG_RADJ(5); break;
+    case 6: PG_RADJ(6); break;
+  }
+#undef PG_RADJ
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

@@ -400,6 +400,30 @@ class DeviceMesh:
         keep = (elem >= 0)
         return F[keep], keep
 
+    def receiver_adjoint(self, weights, receivers, b=None):
+        """b += G^T w: the transpose of the E part of receiver_fields, with
+        weights complex128 [R, 3] per (kept or dropped) receiver in the order
+        given; receivers outside the mesh contribute nothing."""
+        pts_t, elem = self.locate(receivers)
+        R = pts_t.shape[0]
+        w = weights.to(torch.complex128).contiguous()
+        if w.shape != (R, 3):
+            raise ValueError(f"weights must be [{R}, 3]")
+        if b is None:
+            b = torch.zeros(self.N, dtype=torch.complex128, device=self.device)
+        ws = _ws(_lib.query("pg_receiver_adjoint_workspace_bytes", self.p, R), self.device)
+        _lib.call("pg_receiver_adjoint", _p(self.nodes), _p(self.elemsN), _p(self.eo), _p(self.fo), _p(self.dofs),
+                  self.p, _p(pts_t), _p(elem), R, _p(w), _p(b), _p(ws), ws.numel(), _s())
+        return b
+
+    def element_mass_bilinear(self, coef, x, y):
+        """out[e] = y_e^T (-omega mu M_e) x_e (complex128 [T]); coef from
+        element_coefficients (FP64) at the frequency of interest."""
+        out = torch.empty(self.T, dtype=torch.complex128, device=self.device)
+        _lib.call("pg_element_mass_bilinear", _p(coef), _p(self.tuple_of_elem), _p(self.tables), _p(self.dofs),
+                  _p(x.contiguous()), _p(y.contiguous()), self.T, self.p, _p(out), _s())
+        return out
+
     def spmv(self, vals, x):
         y = torch.empty_like(x)
         nrhs = 1 if x.ndim == 1 else int(x.shape[1])
