@@ -329,6 +329,57 @@ int pg_gather_fields(const double* x, const double* nodes, const int32_t* elemsN
                      double omega_mu, double* fields, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Magnetotelluric plane-wave right-hand side (petgem/solver.py:318-512).
+ * The 1-D field u(z) (petgem/mt1d.py) is solved on the host between
+ * pg_mt_face_z and pg_mt_rhs.
+ * ---------------------------------------------------------------------- */
+
+/* Boundary faces (one element, face_nelem from pg_topology) in ascending face
+ * order with their element and local face index: petgem's
+ * computeBoundaryFaces + computeBoundaryElements (mesh.py:128-221).
+ * bface / belem int32 and blocal int8 hold up to n_faces entries;
+ * n_bfaces int64 [1] <- the count. */
+size_t pg_boundary_faces_workspace_bytes(int64_t n_faces);
+int pg_boundary_faces(const int32_t* elemsF, const int32_t* face_nelem, int64_t n_elems, int64_t n_faces,
+                      int32_t* bface, int32_t* belem, int8_t* blocal, int64_t* n_bfaces, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* computeFacePlane (mesh.py:324-429): plane int8 [n_bfaces] = bottom 0,
+ * left 1, front 2, right 3, back 4, top 5 of the box bbox = {min_x, max_x,
+ * min_y, max_y, min_z, max_z} (host array); centroid_z f64 [n_bfaces] = z of
+ * the face centroid over the element's local face vertices (solver.py:360).
+ * status int32 [1] <- PG_ERR_UNSUPPORTED for a face on no box side. */
+int pg_face_planes(const double* nodes, const int32_t* elemsN, const int32_t* facesN, const int32_t* bface,
+                   const int32_t* belem, const int8_t* blocal, int64_t n_bfaces, const double* bbox, int8_t* plane,
+                   double* centroid_z, int32_t* status, void* stream);
+
+/* z [n_bfaces * n_rule] of the triangle rule points (rule f64 [n_rule * 3] =
+ * s, t, weight on the triangle (0,0),(1,0),(0,1)) mapped onto each boundary
+ * face (transform2Dto3DInReferenceElement + getRealFromReference). */
+int pg_mt_face_z(const double* nodes, const int32_t* elemsN, const int32_t* belem, const int8_t* blocal,
+                 int64_t n_bfaces, const double* rule, int n_rule, double* z, void* stream);
+
+/* Per-DOF ordered scatter plan of the boundary contributions (face f, local
+ * DOF l): order int32 [n_bfaces * nd], seg_start int32 [n_bfaces * nd + 1],
+ * seg_dof int32 [n_bfaces * nd], n_seg int64 [1]. */
+size_t pg_mt_plan_workspace_bytes(int64_t n_bfaces, int p);
+int pg_mt_plan(const int32_t* dofs, const int32_t* belem, int64_t n_bfaces, int p, int64_t n_dofs, int32_t* order,
+               int32_t* seg_start, int32_t* seg_dof, int64_t* n_seg, void* workspace, size_t workspace_bytes,
+               void* stream);
+
+/* b[:, rhs] += (scale_re + i scale_im) sum_k w_k |det J_2D| ((n x N_l) x n) .
+ * e_k with e_k = u[f, k] times the direction of getNeumannBCface(plane,
+ * polarization) (1 = x, 2 = y); u complex128 [n_bfaces * n_rule]; b complex128
+ * [N * nrhs] (RHS fastest).  Faces are added per DOF in ascending order.
+ * Workspace: pg_mt_rhs_workspace_bytes(n_bfaces, p). */
+size_t pg_mt_rhs_workspace_bytes(int64_t n_bfaces, int p);
+int pg_mt_rhs(const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo, int p,
+              const int32_t* belem, const int8_t* blocal, const int8_t* plane, int64_t n_bfaces, const double* rule,
+              int n_rule, const double* u, int polarization, double scale_re, double scale_im, const int32_t* order,
+              const int32_t* seg_start, const int32_t* seg_dof, int64_t n_seg, double* b, int nrhs, int rhs,
+              void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
  * Adjoint gradient of a receiver misfit (no petgem counterpart; built from
  * the elemental mass matrices of hvfem.py:223-316 and the interpolation of
  * postprocessing.py:566-614).

@@ -86,6 +86,15 @@ SIGNATURES = {
     "pg_locate_points": (_INT, [_P, _P, _I64, _P, _I64, _D, _P, _P]),
     "pg_source_rhs": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _P, _D, _D, _P, _P, _P]),
     "pg_gather_fields": (_INT, [_P, _P, _P, _P, _P, _P, _INT, _P, _P, _I64, _D, _P, _P]),
+    "pg_boundary_faces_workspace_bytes": (_SZ, [_I64]),
+    "pg_boundary_faces": (_INT, [_P, _P, _I64, _I64, _P, _P, _P, _P, _P, _SZ, _P]),
+    "pg_face_planes": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
+    "pg_mt_face_z": (_INT, [_P, _P, _P, _P, _I64, _P, _INT, _P, _P]),
+    "pg_mt_plan_workspace_bytes": (_SZ, [_I64, _INT]),
+    "pg_mt_plan": (_INT, [_P, _P, _I64, _INT, _I64, _P, _P, _P, _P, _P, _SZ, _P]),
+    "pg_mt_rhs_workspace_bytes": (_SZ, [_I64, _INT]),
+    "pg_mt_rhs": (_INT, [_P, _P, _P, _P, _INT, _P, _P, _P, _I64, _P, _INT, _P, _INT, _D, _D, _P, _P, _P, _I64, _P, _INT,
+                         _INT, _P, _SZ, _P]),
     "pg_receiver_adjoint_workspace_bytes": (_SZ, [_INT, _I64]),
     "pg_receiver_adjoint": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _I64, _P, _P, _P, _SZ, _P]),
     "pg_element_mass_bilinear": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _INT, _P, _P]),

@@ -400,6 +400,100 @@ class DeviceMesh:
         keep = (elem >= 0)
         return F[keep], keep
 
+    # ---------------------------------------------------------------- MT excitation
+    def mt_boundary(self):
+        """Boundary faces, their elements / local faces / box sides and the
+        per-DOF scatter plan of the MT right-hand side (once per mesh)."""
+        if getattr(self, "_mt", None) is not None:
+            return self._mt
+        dev, nF = self.device, self.nF
+        bface = torch.empty(nF, dtype=torch.int32, device=dev)
+        belem = torch.empty(nF, dtype=torch.int32, device=dev)
+        blocal = torch.empty(nF, dtype=torch.int8, device=dev)
+        nb = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = _ws(_lib.query("pg_boundary_faces_workspace_bytes", nF), dev)
+        _lib.call("pg_boundary_faces", _p(self.elemsF), _p(self.face_nelem), self.T, nF, _p(bface), _p(belem),
+                  _p(blocal), _p(nb), _p(ws), ws.numel(), _s())
+        n = int(nb.item())
+        bface, belem, blocal = bface[:n].contiguous(), belem[:n].contiguous(), blocal[:n].contiguous()
+        lo = torch.amin(self.nodes, dim=0).cpu().numpy()
+        hi = torch.amax(self.nodes, dim=0).cpu().numpy()
+        bbox = np.array([lo[0], hi[0], lo[1], hi[1], lo[2], hi[2]], dtype=np.float64)
+        plane = torch.empty(n, dtype=torch.int8, device=dev)
+        cz = torch.empty(n, dtype=torch.float64, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("pg_face_planes", _p(self.nodes), _p(self.elemsN), _p(self.facesN), _p(bface), _p(belem),
+                  _p(blocal), n, ctypes.c_void_p(bbox.ctypes.data), _p(plane), _p(cz), _p(st), _s())
+        if int(st.item()) != 0:
+            raise _lib.PetgemError("pg_face_planes", int(st.item()),
+                                   "a boundary face lies on no side of the bounding box (MT needs a box domain)")
+        m = n * self.nd
+        order = torch.empty(m, dtype=torch.int32, device=dev)
+        seg_start = torch.empty(m + 1, dtype=torch.int32, device=dev)
+        seg_dof = torch.empty(m, dtype=torch.int32, device=dev)
+        nseg = torch.zeros(1, dtype=torch.int64, device=dev)
+        ws = _ws(_lib.query("pg_mt_plan_workspace_bytes", n, self.p), dev)
+        _lib.call("pg_mt_plan", _p(self.dofs), _p(belem), n, self.p, self.N, _p(order), _p(seg_start), _p(seg_dof),
+                  _p(nseg), _p(ws), ws.numel(), _s())
+        self._mt = {"bface": bface, "belem": belem, "blocal": blocal, "plane": plane, "centroid_z": cz,
+                    "bbox": bbox, "order": order, "seg_start": seg_start, "seg_dof": seg_dof,
+                    "n_seg": int(nseg.item()), "n": n}
+        return self._mt
+
+    def mt_face_z(self, rule):
+        """z of every (boundary face, rule point): f64 [n_bfaces, n_rule] on the device.
+        rule: (points (n, 2), weights (n,)) on the triangle (0,0),(1,0),(0,1)."""
+        bd = self.mt_boundary()
+        r = self._rule_tensor(rule)
+        z = torch.empty((bd["n"], r.shape[0]), dtype=torch.float64, device=self.device)
+        _lib.call("pg_mt_face_z", _p(self.nodes), _p(self.elemsN), _p(bd["belem"]), _p(bd["blocal"]), bd["n"],
+                  _p(r), r.shape[0], _p(z), _s())
+        return z
+
+    def _rule_tensor(self, rule):
+        pts, w = rule
+        r = np.concatenate([np.asarray(pts, dtype=np.float64).reshape(-1, 2),
+                            np.asarray(w, dtype=np.float64).reshape(-1, 1)], axis=1)
+        return torch.as_tensor(np.ascontiguousarray(r), device=self.device)
+
+    def mt_field(self, sigma, frequency, rule, n_nodes=10 ** 6):
+        """u at every boundary-face rule point (complex [n_bfaces, n_rule]): the
+        1-D MT field of the right-side (x = max) boundary profile
+        (petgem/solver.py:318-395, mt1d.eval_MT1D on the host)."""
+        from . import mt1d
+        bd = self.mt_boundary()
+        z = self.mt_face_z(rule).cpu().numpy()
+        right = (bd["plane"] == 3)
+        cz = bd["centroid_z"][right].cpu().numpy()
+        s = self.sigma_tensor(sigma) if not torch.is_tensor(sigma) else sigma
+        s4 = s[bd["belem"].long()[right], 0].cpu().numpy()
+        omega = 2.0 * math.pi * float(frequency)
+        u = mt1d.eval_MT1D(bd["bbox"][5], bd["bbox"][4], 1.0, 0.0, s4, cz, omega, MU0, int(n_nodes), 1, z)
+        return torch.as_tensor(np.ascontiguousarray(u, dtype=np.complex128), device=self.device)
+
+    def mt_rhs(self, sigma, frequency, polarizations=("x", "y"), rule=None, u=None, n_nodes=10 ** 6):
+        """MT plane-wave right-hand sides b complex128 [N, npol] (one column per
+        polarisation, RHS fastest, ready for a batched solve), petgem's
+        solver.py:318-512.  rule defaults to a triangle rule exact to degree
+        2p + 2; u (the 1-D field at the rule points) is computed when None."""
+        from . import mt1d
+        bd = self.mt_boundary()
+        rule = rule if rule is not None else mt1d.triangle_rule(2 * self.p + 2)
+        if u is None:
+            u = self.mt_field(sigma, frequency, rule, n_nodes)
+        u = u.to(torch.complex128).contiguous()
+        r = self._rule_tensor(rule)
+        pols = [{"x": 1, "y": 2}[str(q)] for q in polarizations]
+        b = torch.zeros((self.N, len(pols)), dtype=torch.complex128, device=self.device)
+        omu = 2.0 * math.pi * float(frequency) * MU0
+        ws = _ws(_lib.query("pg_mt_rhs_workspace_bytes", bd["n"], self.p), self.device)
+        for k, pol in enumerate(pols):
+            _lib.call("pg_mt_rhs", _p(self.nodes), _p(self.elemsN), _p(self.eo), _p(self.fo), self.p, _p(bd["belem"]),
+                      _p(bd["blocal"]), _p(bd["plane"]), bd["n"], _p(r), r.shape[0], _p(u), pol, 0.0, omu,
+                      _p(bd["order"]), _p(bd["seg_start"]), _p(bd["seg_dof"]), bd["n_seg"], _p(b), len(pols), k,
+                      _p(ws), ws.numel(), _s())
+        return b
+
     def receiver_adjoint(self, weights, receivers, b=None):
         """b += G^T w: the transpose of the E part of receiver_fields, with
         weights complex128 [R, 3] per (kept or dropped) receiver in the order

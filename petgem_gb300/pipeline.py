@@ -51,9 +51,6 @@ class Preprocessing:
         Timers()["Preprocessing"].start()
         model, run, output = inputSetup.model, inputSetup.run, inputSetup.output
         mode = _mode(inputSetup)
-        if mode != "csem":
-            raise NotImplementedError("MT mode: the plane-wave boundary RHS (petgem/solver.py:318-512) is not "
-                                      "built on the GPU yet; CSEM is supported")
         data_model = model[mode]
         p = int(run["nord"])
         mesh = gmsh.read(model["mesh"])
@@ -66,11 +63,14 @@ class Preprocessing:
             sigma = np.stack([sh[phys], sv[phys]], axis=1)
         receivers = np.atleast_2d(np.asarray(_read_array(model["receivers"]), dtype=np.float64))
         dm = DeviceMesh(mesh.points, mesh.tets, p)
-        src = dict(data_model["source"])
-        src_elem = dm.locate_source(src)
-        if int(src_elem.item()) < 0:
-            raise ValueError("Source no located in the computational domain. Please, verify source position or "
-                             "improve the mesh quality.")
+        if mode == "csem":
+            src = dict(data_model["source"])
+            src_elem = dm.locate_source(src)
+            if int(src_elem.item()) < 0:
+                raise ValueError("Source no located in the computational domain. Please, verify source position or "
+                                 "improve the mesh quality.")
+        else:
+            dm.mt_boundary()           # boundary faces, box sides (preprocessing.py:314-381)
         bundle = {"nodes": mesh.points, "tets": mesh.tets, "sigma": sigma, "receivers": receivers, "nord": p}
         np.savez(os.path.join(output["directory_scratch"], "gb300_preprocessing.npz"), **bundle)
         _MESHES[output["directory_scratch"]] = (dm, bundle)
@@ -101,14 +101,24 @@ class Solver:
 
     def assembly(self, inputSetup):
         Timers()["Assembly"].start()
-        data_model = inputSetup.model[_mode(inputSetup)]
-        src = dict(data_model["source"])
-        freq = float(src["frequency"])
+        mode = _mode(inputSetup)
+        data_model = inputSetup.model[mode]
         m = self.mesh
-        self.A = m.assemble(self.bundle["sigma"], freq, fused=True)
-        self.b = [torch.zeros(m.N, dtype=torch.complex128, device=m.device)]
-        self.x = [torch.zeros_like(self.b[0])]
-        m.source_vector(src, self.b[0])
+        self.mode = mode
+        if mode == "csem":
+            src = dict(data_model["source"])
+            freq = float(src["frequency"])
+            self.A = m.assemble(self.bundle["sigma"], freq, fused=True)
+            self.b = [torch.zeros(m.N, dtype=torch.complex128, device=m.device)]
+            m.source_vector(src, self.b[0])
+        else:
+            # MT: no PEC; one plane-wave RHS per polarisation (solver.py:318-512)
+            freq = float(data_model["frequency"])
+            self.polarizations = [str(q) for q in data_model["polarization"]]
+            self.A = m.assemble(self.bundle["sigma"], freq, fused=True)
+            B = m.mt_rhs(self.bundle["sigma"], freq, self.polarizations)
+            self.b = [B[:, k].contiguous() for k in range(B.shape[1])]
+        self.x = [torch.zeros_like(bk) for bk in self.b]
         torch.cuda.synchronize()
         Timers()["Assembly"].stop()
 
@@ -116,10 +126,11 @@ class Solver:
         """PEC + KSP solve.  options: dict from parse_petsc_options (petgem
         reads them from the PETSc options database, solver.py:588)."""
         opts = options or {}
-        Timers()["SetBoundaries"].start()
-        self.mesh.apply_pec(self.A, self.b[0])
-        torch.cuda.synchronize()
-        Timers()["SetBoundaries"].stop()
+        if getattr(self, "mode", "csem") == "csem":
+            Timers()["SetBoundaries"].start()
+            self.mesh.apply_pec(self.A, self.b[0])
+            torch.cuda.synchronize()
+            Timers()["SetBoundaries"].stop()
         Timers()["Solver"].start()
         ksp = str(opts.get("ksp_type", "gmres"))
         if ksp not in ("gmres", "cocg"):
@@ -128,16 +139,20 @@ class Solver:
         if pc not in ("jacobi", "sor", "none", "bjacobi"):
             raise ValueError(f"-pc_type {pc}: supported preconditioner is jacobi")
         self.info = []
+        self.ksp = ksp
+        # all polarisations in one batched solve (one SpMM per iteration)
+        B = torch.stack(self.b, dim=1).contiguous() if len(self.b) > 1 else self.b[0]
+        X, info = self.mesh.solve(self.A, B, rtol=float(opts.get("ksp_rtol", 1e-8)),
+                                  restart=int(opts.get("ksp_gmres_restart", 30)),
+                                  max_it=int(opts.get("ksp_max_it", 10000)),
+                                  precision=str(opts.get("pg_precision", "fp64")), ksp=ksp,
+                                  raise_on_fail=False)
         for i in range(len(self.b)):
-            x, info = self.mesh.solve(self.A, self.b[i], rtol=float(opts.get("ksp_rtol", 1e-8)),
-                                      restart=int(opts.get("ksp_gmres_restart", 30)),
-                                      max_it=int(opts.get("ksp_max_it", 10000)),
-                                      precision=str(opts.get("pg_precision", "fp64")), ksp=ksp,
-                                      raise_on_fail=False)
-            self.x[i] = x
+            self.x[i] = X[:, i].contiguous() if X.ndim == 2 else X
             self.info.append(info)
-            Print.master(f"     KSP {ksp}: {info.iterations} iterations, true relative residual {info.relres:.3e}")
-            np.save(os.path.join(inputSetup.output["directory_scratch"], f"x{i}.npy"), x.cpu().numpy())
+            Print.master(f"     KSP {ksp}: {info.iterations} iterations, true relative residual "
+                         f"{info.relres_per_rhs[i] if info.relres_per_rhs is not None else info.relres:.3e}")
+            np.save(os.path.join(inputSetup.output["directory_scratch"], f"x{i}.npy"), self.x[i].cpu().numpy())
         Timers()["Solver"].stop()
 
 
@@ -149,19 +164,23 @@ class Postprocessing:
         model, run, output = inputSetup.model, inputSetup.run, inputSetup.output
         mode = _mode(inputSetup)
         scratch = output["directory_scratch"]
+        npol = int(run["num_polarizations"])
         if solver is not None:
             m, xs, bundle = solver.mesh, solver.x, solver.bundle
         else:
             m, bundle = _MESHES[scratch]
-            xs = [torch.as_tensor(np.load(os.path.join(scratch, "x0.npy")), device=m.device)]
-        freq = float(model[mode]["source"]["frequency"])
-        fields, keep = m.receiver_fields(xs[0], bundle["receivers"], freq)
+            xs = [torch.as_tensor(np.load(os.path.join(scratch, f"x{i}.npy")), device=m.device) for i in range(npol)]
+        freq = float(model[mode]["source"]["frequency"]) if mode == "csem" else float(model[mode]["frequency"])
+        Fs = []
+        for x in xs:
+            fields, keep = m.receiver_fields(x, bundle["receivers"], freq)
+            Fs.append(fields.cpu().numpy())
         dropped = np.nonzero(~keep.cpu().numpy())[0]
         if dropped.size:
             Print.master("        The following receivers were not located and will not be taken into account "
                          + str(dropped))
-        F = fields.cpu().numpy()
-        self.fields = F
+        F = Fs[0]
+        self.fields = F if mode == "csem" else Fs
         elapsed = Timers()["Assembly"].elapsed + Timers()["Solver"].elapsed
         out = {
             "machine/machine": f"{platform.uname().node}. {platform.uname().release}. {platform.uname().processor}",
@@ -175,28 +194,74 @@ class Postprocessing:
             "model/cuda": bool(run.get("cuda", False)),
             "model/vtk": bool(output.get("vtk", False)),
             "model/mode": mode,
-            "model/num-polarizations": int(run["num_polarizations"]),
+            "model/num-polarizations": npol,
             "model/solver": str(getattr(solver, "ksp", "gmres")) if solver else "gmres",
             "model/run-time (s)": float(elapsed),
-            "model/frequency (Hz)": freq,
-            "model/E-fields/x": F[:, 0], "model/E-fields/y": F[:, 1], "model/E-fields/z": F[:, 2],
-            "model/H-fields/x": F[:, 3], "model/H-fields/y": F[:, 4], "model/H-fields/z": F[:, 5],
         }
-        src = model[mode]["source"]
         if run.get("conductivity_from_file"):
             out["model/sigma-file"] = str(model[mode]["sigma"]["file"])
         else:
             out["model/sigma_horizontal (S/m)"] = np.asarray(model[mode]["sigma"]["horizontal"], dtype=np.float64)
             out["model/sigma_vertical (S/m)"] = np.asarray(model[mode]["sigma"]["vertical"], dtype=np.float64)
-        out["model/source_position (m)"] = np.asarray(src["position"], dtype=np.float64)
-        out["model/source_azimuth (deg)"] = src["azimuth"]
-        out["model/source_dip (deg)"] = src["dip"]
-        out["model/source_current (Am)"] = src["current"]
-        out["model/source_length (m)"] = src["length"]
+        out["model/frequency (Hz)"] = freq
+        if mode == "csem":
+            src = model[mode]["source"]
+            out["model/source_position (m)"] = np.asarray(src["position"], dtype=np.float64)
+            out["model/source_azimuth (deg)"] = src["azimuth"]
+            out["model/source_dip (deg)"] = src["dip"]
+            out["model/source_current (Am)"] = src["current"]
+            out["model/source_length (m)"] = src["length"]
+            for c, k in enumerate("xyz"):
+                out[f"model/E-fields/{k}"] = F[:, c]
+                out[f"model/H-fields/{k}"] = F[:, 3 + c]
+        else:
+            pols = [str(q) for q in model[mode]["polarization"]]
+            out["model/polarization"] = np.asarray(pols)
+            for i, q in enumerate(pols):
+                for c, k in enumerate("xyz"):
+                    out[f"model/E-fields_mode_{q}/{k}"] = Fs[i][:, c]
+                    out[f"model/H-fields_mode_{q}/{k}"] = Fs[i][:, 3 + c]
+            if npol == 2:
+                rho, phase, tip, Z = computeImpedance(Fs, 2.0 * np.pi * freq, MU0)
+                self.impedance, self.apparent_resistivity, self.phase, self.tipper = Z, rho, phase, tip
+                for j, k in enumerate(("xx", "xy", "yx", "yy")):
+                    out[f"model/impedance/{k}"] = Z[j]
+                    out[f"model/apparent_resistivity/{k}"] = rho[j]
+                    out[f"model/phase/{k}"] = phase[j]
+                out["model/tipper/x"], out["model/tipper/y"] = tip[0], tip[1]
         name = f"{mode}_petgemV{VERSION}_{datetime.datetime.today().strftime('%Y-%m-%d')}"
         self.output_file = write_results(os.path.join(output["directory"], name), out)
         Timers()["Postprocessing"].stop()
-        return F
+        return F if mode == "csem" else Fs
+
+
+def computeImpedance(fields, omega, mu):
+    """Apparent resistivity, phase, tipper and impedance from two
+    polarisations' receiver fields (R, 6) each (petgem/postprocessing.py:619-688):
+    Z solves E = Z H per receiver, rho_a = |Z|^2 / (omega mu), phase =
+    atan(-Im Z / Re Z) in degrees mod 360, and the tipper T solves
+    Hz = Tx Hx + Ty Hy.  Returns ([rho xx, xy, yx, yy], [phase ...], [Tx, Ty],
+    [Z xx, xy, yx, yy])."""
+    f1, f2 = np.asarray(fields[0]), np.asarray(fields[1])
+    e1x, e1y, h1x, h1y, h1z = f1[:, 0], f1[:, 1], f1[:, 3], f1[:, 4], f1[:, 5]
+    e2x, e2y, h2x, h2y, h2z = f2[:, 0], f2[:, 1], f2[:, 3], f2[:, 4], f2[:, 5]
+    # Cramer's rule on the two polarisations, in the reference's factorisation
+    m1 = h2y * h2x * h1y - h2y * h2y * h1x
+    m2 = h2x * h2x * h1y - h2y * h2x * h1x
+    m3 = e2x * h2x * h1y - h2y * e2x * h1x
+    m4 = h2y * e2y * h1y - h2y * h2y * e1y
+    m5 = h2x * e2y * h1y - h2y * h2x * e1y
+    m6 = h2y * h2x * e1y - e2y * h2y * h1x
+    m7 = h2x * h2x * e1y - e2y * h2x * h1x
+    det = h1x * m1 - h1y * m2
+    Z = [(e1x * m1 - h1y * m3) / det, (h1x * m3 - e1x * m2) / det,
+         (h1x * m4 - h1y * m5) / det, (h1x * m6 - h1y * m7) / det]
+    rho = [np.abs(z) ** 2 / (mu * omega) for z in Z]
+    phase = [np.mod(np.degrees(np.arctan(-z.imag / z.real)), 360.0) for z in Z]
+    c = h1x * h2y
+    ty = (h2z / h2y - (h1z * h2x) / c) / (1.0 - (h1y * h2x) / c)
+    tx = (h1z - ty * h1y) / h1x
+    return rho, phase, [tx, ty], Z
 
 
 def write_results(stem, datasets):
