@@ -349,44 +349,10 @@ class DeviceMesh:
 
     def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
               raise_on_fail=True, ksp="gmres", check_every=50):
-        """Solve A x = b; b complex128 [N] or [N, k] (k in 1,2,4,8,16,32).
-
-        ksp="gmres": right-Jacobi restarted GMRES(restart) (PETSc -ksp_type gmres -pc_type jacobi);
-        ksp="cocg":  Jacobi-scaled COCG for the complex-symmetric A.
-        precision="fp64" (complex128), "mixed" (complex64 matrix/SpMV, FP64 recurrence and
-        refinement) or "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy).
-        Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
-        """
-        nrhs = 1 if b.ndim == 1 else int(b.shape[1])
-        x = torch.zeros_like(b) if x0 is None else x0.clone()
-        prec = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
-        if prec == 2 and ksp != "cocg":
-            raise ValueError("precision='df64' is implemented for ksp='cocg'")
-        res = _lib.GmresResult()
-        rr = (ctypes.c_double * nrhs)()
-        lib = _lib.load()
-        if ksp == "gmres":
-            o = _lib.GmresOpts()
-            lib.pg_gmres_default_opts(ctypes.byref(o))
-            o.restart, o.max_it, o.rtol, o.precision, o.reorth = int(restart), int(max_it), float(rtol), prec, int(reorth)
-            nbytes = _lib.query("pg_gmres_workspace_bytes", self.N, self.nnz, nrhs, ctypes.byref(o))
-            fn = lib.pg_gmres
-        elif ksp == "cocg":
-            o = _lib.CocgOpts()
-            lib.pg_cocg_default_opts(ctypes.byref(o))
-            o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), prec, int(check_every)
-            nbytes = _lib.query("pg_cocg_workspace_bytes", self.N, self.nnz, nrhs, ctypes.byref(o))
-            fn = lib.pg_cocg
-        else:
-            raise ValueError(f"unknown ksp type {ksp!r} (gmres, cocg)")
-        ws = _ws(nbytes + 256, self.device)
-        st = fn(_p(self.rowptr), _p(self.col), _p(vals), self.N, self.nnz, _p(b.contiguous()), _p(x), nrhs,
-                ctypes.byref(o), ctypes.byref(res), ctypes.cast(rr, ctypes.c_void_p), _p(ws), ws.numel(), _s())
-        info = SolveInfo(int(res.iterations), int(res.restarts), float(res.relres), int(st), list(rr))
-        if st != 0 and (raise_on_fail or st != -7):
-            msg = lib.pg_last_error()
-            raise _lib.PetgemError(f"pg_{ksp}", st, msg.decode() if msg else "")
-        return x, info
+        """Solve A x = b for this mesh's CSR pattern (see solve_csr)."""
+        return solve_csr(self.rowptr, self.col, vals, b, x0=x0, rtol=rtol, restart=restart, max_it=max_it,
+                         precision=precision, reorth=reorth, raise_on_fail=raise_on_fail, ksp=ksp,
+                         check_every=check_every)
 
     def receiver_fields(self, x, receivers, frequency):
         """(fields complex128 [R', 6], kept mask) like petgem fieldInterpolator
@@ -523,3 +489,49 @@ class DeviceMesh:
         nrhs = 1 if x.ndim == 1 else int(x.shape[1])
         _lib.call("pg_spmv_z", _p(self.rowptr), _p(self.col), _p(vals), self.N, _p(x.contiguous()), _p(y), nrhs, _s())
         return y
+
+
+def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
+              raise_on_fail=True, ksp="gmres", check_every=50):
+    """Solve A x = b for a CSR matrix on the GPU (rowptr int64 [N+1], col
+    int32 [nnz], vals complex128 [nnz]); b complex128 [N] or [N, k]
+    (k in 1,2,4,8,16,32).  The KSPSolve of petgem/solver.py:584-594.
+
+    ksp="gmres": right-Jacobi restarted GMRES(restart) (PETSc -ksp_type gmres -pc_type jacobi);
+    ksp="cocg":  Jacobi-scaled COCG for complex-symmetric A.
+    precision="fp64" (complex128), "mixed" (complex64 matrix/SpMV, FP64 recurrence and
+    refinement) or "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy).
+    Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
+    """
+    N = int(rowptr.numel()) - 1
+    nnz = int(col.numel())
+    nrhs = 1 if b.ndim == 1 else int(b.shape[1])
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    prec = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
+    if prec == 2 and ksp != "cocg":
+        raise ValueError("precision='df64' is implemented for ksp='cocg'")
+    res = _lib.GmresResult()
+    rr = (ctypes.c_double * nrhs)()
+    lib = _lib.load()
+    if ksp == "gmres":
+        o = _lib.GmresOpts()
+        lib.pg_gmres_default_opts(ctypes.byref(o))
+        o.restart, o.max_it, o.rtol, o.precision, o.reorth = int(restart), int(max_it), float(rtol), prec, int(reorth)
+        nbytes = _lib.query("pg_gmres_workspace_bytes", N, nnz, nrhs, ctypes.byref(o))
+        fn = lib.pg_gmres
+    elif ksp == "cocg":
+        o = _lib.CocgOpts()
+        lib.pg_cocg_default_opts(ctypes.byref(o))
+        o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), prec, int(check_every)
+        nbytes = _lib.query("pg_cocg_workspace_bytes", N, nnz, nrhs, ctypes.byref(o))
+        fn = lib.pg_cocg
+    else:
+        raise ValueError(f"unknown ksp type {ksp!r} (gmres, cocg)")
+    ws = _ws(nbytes + 256, b.device)
+    st = fn(_p(rowptr), _p(col), _p(vals), N, nnz, _p(b.contiguous()), _p(x), nrhs,
+            ctypes.byref(o), ctypes.byref(res), ctypes.cast(rr, ctypes.c_void_p), _p(ws), ws.numel(), _s())
+    info = SolveInfo(int(res.iterations), int(res.restarts), float(res.relres), int(st), list(rr))
+    if st != 0 and (raise_on_fail or st != -7):
+        msg = lib.pg_last_error()
+        raise _lib.PetgemError(f"pg_{ksp}", st, msg.decode() if msg else "")
+    return x, info

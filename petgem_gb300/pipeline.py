@@ -6,7 +6,9 @@ The stages keep the reference's method names, timer names and inputs (the
 params file and PETSc-style KSP options).  Instead of PETSc binary scratch
 files, Preprocessing leaves the mesh resident on the GPU (and saves a small
 ``.npz`` bundle in ``directory_scratch`` so a later process can resume), the
-Solver keeps A, b and x as device tensors, and Postprocessing writes the
+Solver keeps A, b and x as device tensors (and writes x{i}.dat in petgem's
+PETSc binary format; it also starts from petgem's own preprocessing scratch
+files when those are what the scratch directory holds), and Postprocessing writes the
 receiver fields with the reference's HDF5 dataset paths (h5py when
 installed, otherwise the same paths as keys of an ``.npz`` file).
 """
@@ -17,7 +19,7 @@ import platform
 import numpy as np
 import torch
 
-from . import gmsh
+from . import gmsh, petsc_io
 from .common import Print, Timers, parse_petsc_options
 from .engine import MU0, DeviceMesh
 
@@ -90,10 +92,18 @@ class Solver:
         scratch = inputSetup.output["directory_scratch"]
         if scratch in _MESHES:
             self.mesh, self.bundle = _MESHES[scratch]
-        else:
+        elif os.path.exists(os.path.join(scratch, "gb300_preprocessing.npz")):
             d = np.load(os.path.join(scratch, "gb300_preprocessing.npz"))
             self.bundle = {k: d[k] for k in d.files}
             self.mesh = DeviceMesh(self.bundle["nodes"], self.bundle["tets"], int(self.bundle["nord"]))
+            _MESHES[scratch] = (self.mesh, self.bundle)
+        else:
+            # scratch written by petgem's own Preprocessing (PETSc binary files)
+            nodes, tets, sigma = petsc_io.read_petgem_scratch(scratch)
+            receivers = np.atleast_2d(np.asarray(_read_array(inputSetup.model["receivers"]), dtype=np.float64))
+            p = int(inputSetup.run["nord"])
+            self.bundle = {"nodes": nodes, "tets": tets, "sigma": sigma, "receivers": receivers, "nord": p}
+            self.mesh = DeviceMesh(nodes, tets, p)
             _MESHES[scratch] = (self.mesh, self.bundle)
         self.total_num_dofs = self.mesh.N
         self.boundaries = self.mesh.bnd
@@ -152,7 +162,9 @@ class Solver:
             self.info.append(info)
             Print.master(f"     KSP {ksp}: {info.iterations} iterations, true relative residual "
                          f"{info.relres_per_rhs[i] if info.relres_per_rhs is not None else info.relres:.3e}")
-            np.save(os.path.join(inputSetup.output["directory_scratch"], f"x{i}.npy"), self.x[i].cpu().numpy())
+            # x{i}.dat as petgem's Solver writes it (PETSc binary), readable by petgem's Postprocessing
+            petsc_io.write_vec(os.path.join(inputSetup.output["directory_scratch"], f"x{i}.dat"),
+                               self.x[i].cpu().numpy())
         Timers()["Solver"].stop()
 
 
@@ -169,7 +181,8 @@ class Postprocessing:
             m, xs, bundle = solver.mesh, solver.x, solver.bundle
         else:
             m, bundle = _MESHES[scratch]
-            xs = [torch.as_tensor(np.load(os.path.join(scratch, f"x{i}.npy")), device=m.device) for i in range(npol)]
+            xs = [torch.as_tensor(petsc_io.read_vec(os.path.join(scratch, f"x{i}.dat")), device=m.device)
+                  for i in range(npol)]
         freq = float(model[mode]["source"]["frequency"]) if mode == "csem" else float(model[mode]["frequency"])
         Fs = []
         for x in xs:

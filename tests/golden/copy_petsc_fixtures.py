@@ -1,0 +1,27 @@
+"""Copy petgem's PETSc-binary test system (tests/data/matrix-A.dat,
+vector-b.dat, vector-x.dat: the system petgem's tests/test_petsc.py solves
+with KSP, x being the zero initial guess) into tests/golden/ under
+petgem_*.dat names, unchanged.
+
+    python tests/golden/copy_petsc_fixtures.py --ref /root/reference
+"""
+import argparse
+import os
+import shutil
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    for name in ("matrix-A.dat", "vector-b.dat", "vector-x.dat"):
+        src = os.path.join(args.ref, "tests", "data", name)
+        dst = os.path.join(HERE, "petgem_" + name)
+        shutil.copyfile(src, dst)
+        print("copied", src, "->", dst, os.path.getsize(dst), "bytes")
+
+
+if __name__ == "__main__":
+    main()

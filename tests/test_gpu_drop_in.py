@@ -5,6 +5,7 @@ import json
 import os
 
 import numpy as np
+import torch
 import pytest
 import scipy.sparse.linalg as spla
 
@@ -116,3 +117,97 @@ output:
     assert post.fields.shape == F.shape == (5, 6)
     assert rel_norm(post.fields, F) < 1e-6
     assert os.path.exists(post.output_file)
+
+
+def test_petgem_petsc_test_system_solved_by_gpu_gmres():
+    """petgem's tests/test_petsc.py: read its PETSc-binary system and solve it
+    with the GPU KSP (GMRES + Jacobi, zero initial guess from vector-x)."""
+    import os
+
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    from petgem_gb300 import petsc_io
+    from petgem_gb300.engine import solve_csr
+    fix = os.path.join(os.path.dirname(__file__), "golden")
+    rp, col, vals, shape = petsc_io.read_mat(os.path.join(fix, "petgem_matrix-A.dat"))
+    b = petsc_io.read_vec(os.path.join(fix, "petgem_vector-b.dat"))
+    x0 = petsc_io.read_vec(os.path.join(fix, "petgem_vector-x.dat"))
+    dev = torch.device("cuda:0")
+    t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)  # noqa: E731
+    x, info = solve_csr(t(rp, torch.int64), t(col, torch.int32), t(vals, torch.complex128), t(b, torch.complex128),
+                        x0=t(x0, torch.complex128), rtol=1e-10, max_it=20000, ksp="gmres")
+    assert info.status == 0
+    A = sp.csr_matrix((vals, col, rp), shape=shape)
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(A @ xg - b) <= 1.01e-10 * np.linalg.norm(b)
+    xd = spla.spsolve(A.tocsc(), b)
+    assert np.linalg.norm(xg - xd) <= 1e-6 * np.linalg.norm(xd)
+
+
+def test_params_pipeline_mt_vs_oracle(tmp_path):
+    """MT mode through the params file: boundary excitation for both
+    polarisations, one batched solve, receiver fields and impedances against
+    the oracle (petgem's formulation restated, direct solve).  The 1e6-node
+    1-D MT solve is conditioned ~1e12 (two LU solves differ by ~6e-7), so the
+    comparison is at 5e-6."""
+    from oracle import mt
+    from petgem_gb300 import gmsh, mt1d
+    from petgem_gb300.pipeline import computeImpedance, run_kernel
+    g = load("mt_n4.npz")
+    pts, tets = g["nodes"], g["tets"]
+    cz = pts[tets].mean(axis=1)[:, 2]
+    phys = np.where(cz > 0.0, 1, np.where(cz > -1000.0, 2, 3))
+    msh = tmp_path / "mesh.msh"
+    gmsh.write(str(msh), pts, tets, phys)
+    gx = np.linspace(-2000.0, 2000.0, 3)
+    X, Y = np.meshgrid(gx, gx, indexing="ij")
+    rx = np.stack([X.ravel(), Y.ravel(), np.full(9, -20.0)], axis=1)
+    np.save(tmp_path / "rx.npy", rx)
+    params = tmp_path / "params.yaml"
+    params.write_text(f"""model:
+  mode: mt
+  mt:
+    sigma:
+      horizontal: [0.3, 0.1, 0.05]
+      vertical: [0.3, 0.1, 0.05]
+    frequency: 1.0
+    polarization: ['x', 'y']
+  mesh: {msh}
+  receivers: {tmp_path / 'rx.npy'}
+run:
+  nord: 2
+  cuda: True
+output:
+  vtk: False
+  directory: {tmp_path / 'out'}
+  directory_scratch: {tmp_path / 'tmp'}
+""")
+    setup, solver, post = run_kernel(str(params), ["-ksp_type", "cocg", "-ksp_rtol", "1e-11", "-ksp_max_it", "100000"])
+    assert all(i.status == 0 for i in solver.info)
+    p = 2
+    eE, eN = topology.compute_edges(tets)
+    eF, fN = topology.compute_faces(tets)
+    fE = topology.compute_faces_edges(eF, eE, fN.shape[0])
+    eo, fo = topology.element_orientation(tets, eE, eN, eF, fE)
+    dofs, de, df, dv, nd = topology.compute_connectivity_dofs(eE, eF, p)
+    sh = np.array([0.3, 0.1, 0.05])[phys - 1]
+    sigma = np.stack([sh, sh], 1)
+    M, K = fem.element_matrices_batch(pts[tets], eo, fo, sigma, p)
+    A = fem.assemble(M, K, dofs, nd, 1.0)
+    bd = mt.Boundary(pts, tets, eF, fN, fN.shape[0])
+    rp, rw = mt1d.triangle_rule(2 * p + 2)
+    u, _ = mt.mt_field_at_faces(bd, sigma, rp, 2 * np.pi)
+    Fo = []
+    for pol in (1, 2):
+        b = mt.mt_rhs(bd, eo, fo, dofs, nd, p, u, rp, rw, 2 * np.pi, pol)
+        x = spla.spsolve(A.tocsc(), b)
+        Fo.append(fem.interpolate_fields(x, pts, tets, eo, fo, dofs, p, rx, 1.0)[0])
+    for k in range(2):
+        assert rel_norm(post.fields[k], Fo[k]) < 5e-6
+    Zo = mt.impedance(Fo, 2 * np.pi, fem.MU0)[3]
+    assert rel_norm(np.stack(post.impedance), np.stack(Zo)) < 5e-6
+    Zr = computeImpedance(post.fields, 2 * np.pi, fem.MU0)[3]
+    assert rel_norm(np.stack(Zr), np.stack(post.impedance)) == 0.0
+    assert os.path.exists(post.output_file)
+    assert os.path.exists(os.path.join(str(tmp_path / "tmp"), "x1.dat"))
