@@ -464,6 +464,19 @@ int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* vals, int64
             double* x, int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result, double* relres_per_rhs,
             void* workspace, size_t workspace_bytes, void* stream);
 
+/* Several frequencies in one double-float COCG (precision must be 2): column
+ * j solves (Re A0 + i s_j Im A0) x_j = b_j, where vals = A0 = K - i omega_0 mu
+ * M is assembled (PEC applied) at one frequency omega_0 and s_j = omega_j /
+ * omega_0 > 0 (col_scale: host array [nrhs]).  The matrix is read once per
+ * iteration for all columns; each column has its own Jacobi scaling.  b, x
+ * complex128 [n * nrhs] (RHS fastest).  Other arguments as pg_cocg. */
+size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs);
+int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
+                      const double* b, double* x, int nrhs, const double* col_scale, const pg_cocg_opts* opts,
+                      pg_gmres_result* result, double* relres_per_rhs, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
+
 #ifdef __cplusplus
 }
 #endif

@@ -1381,7 +1381,7 @@ __global__ void __launch_bounds__(kThreads) k_df_spmm(const int64_t* __restrict_
 }
 
 // y += alpha p ; r -= alpha q ; partials rho = r^T r (df), w = sum |r|^2 |D| (FP32 estimate)
-template <int K>
+template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, float4* __restrict__ r,
                                                         const float4* __restrict__ pv, const float4* __restrict__ q,
                                                         const float* __restrict__ wd, int64_t n, CgState* st,
@@ -1412,16 +1412,17 @@ __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, 
     y[e] = ye;
     r[e] = re;
     cdf_mac(rho, re, re);
-    ww += (re.x * re.x + re.z * re.z) * wd[e / K];
+    ww += (re.x * re.x + re.z * re.z) * wd[PC ? e : e / K];
   }
   block_reduce_rhs<K>(cdf_to(rho), smem, prho + (int64_t)blockIdx.x * K);
   block_reduce_rhs<K>(make_double2((double)ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) cg_beta_final<K>(prho, pw, gridDim.x, st, ctl, iter, delta, smem);
 }
 
-template <int K>
+template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_df_pupdate(float4* __restrict__ pv, const float4* __restrict__ r, int64_t n,
-                                                         const CgState* st, int iter) {
+                                                         const CgState* st, int iter, float4* __restrict__ ps = nullptr,
+                                                         const float4* __restrict__ Sdf = nullptr) {
   __shared__ float4 bt[kMaxK];
   __shared__ int use[kMaxK];
   if (threadIdx.x < K) {
@@ -1437,7 +1438,13 @@ __global__ void __launch_bounds__(kThreads) k_df_pupdate(float4* __restrict__ pv
     if (use[e % K]) {
       float4 v = r[e];
       cdf_mac(v, bt[e % K], pv[e]);
-      pv[e] = df_norm(v);
+      v = df_norm(v);
+      pv[e] = v;
+      if (PC) {
+        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+        cdf_mac(w, Sdf[e], v);
+        ps[e] = df_norm(w);
+      }
     }
 }
 
@@ -1450,39 +1457,144 @@ __global__ void k_df_scale_matrix(const int64_t* rowptr, const int32_t* col, con
   }
 }
 
-template <int K>
+template <int K, bool PC = false>
 __global__ void k_df_start(const double2* __restrict__ r64, const double2* __restrict__ S, int64_t n, float4* r,
-                           float4* y, float4* pv, int set_p, double2* prho) {
+                           float4* y, float4* pv, int set_p, double2* prho, float4* ps = nullptr) {
   __shared__ double2 smem[(kThreads / 32) * kMaxK];
   const int64_t total = n * K;
   const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
   const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
   double2 rho = make_double2(0.0, 0.0);
   for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
-    const double2 v = cmul(S[e / K], r64[e]);
+    const double2 sc = S[PC ? e : e / K];
+    const double2 v = cmul(sc, r64[e]);
     const float4 vf = cdf_from(v);
     r[e] = vf;
     y[e] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (set_p) pv[e] = vf;
+    if (PC && set_p) ps[e] = cdf_from(cmul(sc, v));
     rho = dadd(rho, cmul(v, v));
   }
   block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
 }
 
-template <int K>
+template <int K, bool PC = false>
 __global__ void k_df_xupdate(const float4* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
   const int64_t total = n * K;
   for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
-    x[e] = dadd(x[e], cmul(S[e / K], cdf_to(y[e])));
+    x[e] = dadd(x[e], cmul(S[PC ? e : e / K], cdf_to(y[e])));
 }
 
-size_t df_layout(const Plan& P, size_t* off /* 14 */) {
+// ---- several frequencies in one solve --------------------------------------
+// Column j solves (Re A0 + i s_j Im A0) x_j = b_j: A0 assembled at omega_0
+// (K - i omega_0 mu M, PEC rows unit), s_j = omega_j / omega_0.  The matrix is
+// read once per iteration for all columns; each column has its own Jacobi
+// scaling S_j = diag(A_j)^(-1/2), applied to the direction (ps = S_j o p, kept
+// by the p update) and to the product's rows.
+
+// S[r * K + j], |D|[r * K + j] for every column
+template <int K>
+__global__ void k_mf_scaling(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n,
+                             const double* scale, double2* S, double* wd, float* wdf, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 d = make_double2(0.0, 0.0);
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      if (col[k] == r) d = val[k];
+    for (int j = 0; j < K; ++j) {
+      const double2 dj = make_double2(d.x, scale[j] * d.y);
+      const double m = hypot(dj.x, dj.y);
+      if (!(m > 0.0)) {
+        *status = 1;
+        S[r * K + j] = make_double2(1.0, 0.0);
+        wd[r * K + j] = 1.0;
+        wdf[r * K + j] = 1.0f;
+        continue;
+      }
+      // principal square root of 1/d
+      const double2 inv = make_double2(dj.x / (m * m), -dj.y / (m * m));
+      const double mi = 1.0 / m;
+      const double re = sqrt(0.5 * (mi + inv.x));
+      const double im = inv.y >= 0.0 ? sqrt(fmax(0.5 * (mi - inv.x), 0.0)) : -sqrt(fmax(0.5 * (mi - inv.x), 0.0));
+      S[r * K + j] = make_double2(re, im);
+      wd[r * K + j] = m;
+      wdf[r * K + j] = (float)m;
+    }
+  }
+}
+
+__global__ void k_mf_df_matrix(const double2* val, int64_t nnz, float4* out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = cdf_from(val[k]);
+}
+
+__global__ void k_mf_sdf(const double2* S, int64_t total, float4* out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = cdf_from(S[e]);
+}
+
+// q = S o (A_j ps), A_j = Re A0 + i s_j Im A0, partial mu = p^T q; last block: alpha
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_mf_spmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                      const float4* __restrict__ val, int64_t n,
+                                                      const float* __restrict__ scale_hl,
+                                                      const float4* __restrict__ Sdf, const float4* __restrict__ pv,
+                                                      const float4* __restrict__ ps, float4* __restrict__ q,
+                                                      double2* partial, CgState* st, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int rhs = threadIdx.x % K;
+  const float sh = scale_hl[2 * rhs], sl = scale_hl[2 * rhs + 1];
+  const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / K;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; r < n; r += rows_per_pass) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t e = rowptr[r + 1];
+    for (int64_t k = rowptr[r]; k < e; ++k) {
+      const float4 a = val[k];
+      // imaginary part times s_j (double-float product)
+      const dfv im = df_mul(dfv{a.z, a.w}, dfv{sh, sl});
+      cdf_mac(acc, make_float4(a.x, a.y, im.h, im.l), ps[(int64_t)col[k] * K + rhs]);
+    }
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    cdf_mac(out, Sdf[r * K + rhs], df_norm(acc));
+    out = df_norm(out);
+    q[r * K + rhs] = out;
+    cdf_mac(mu, pv[r * K + rhs], out);
+  }
+  block_reduce_rhs<K>(cdf_to(mu), smem, partial + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
+}
+
+// r64 = b - A_j x (FP64), one thread per (row, column)
+template <int K>
+__global__ void k_mf_resid(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                           const double2* __restrict__ val, int64_t n, const double* __restrict__ scale,
+                           const double2* __restrict__ x, const double2* __restrict__ b, double2* __restrict__ r64) {
+  const int64_t total = n * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / K;
+    const int j = (int)(e % K);
+    const double sj = scale[j];
+    double ar = 0.0, ai = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const double2 a = val[k];
+      const double2 xv = x[(int64_t)col[k] * K + j];
+      const double im = sj * a.y;
+      ar = fma(a.x, xv.x, fma(-im, xv.y, ar));
+      ai = fma(a.x, xv.y, fma(im, xv.x, ai));
+    }
+    r64[e] = make_double2(b[e].x - ar, b[e].y - ai);
+  }
+}
+
+size_t df_layout(const Plan& P, size_t* off /* 18 */, bool mf = false) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
+  const size_t ns = mf ? (size_t)P.n * P.k : (size_t)P.n;   // scaling entries: per column with several frequencies
   put(0, P.nnz * sizeof(float4));               // At (double-float)
-  put(1, sizeof(double2) * P.n);                // S
-  put(2, sizeof(double) * P.n);                 // |D|
-  put(3, sizeof(float) * P.n);                  // |D| f32
+  put(1, sizeof(double2) * ns);                 // S
+  put(2, sizeof(double) * ns);                  // |D|
+  put(3, sizeof(float) * ns);                   // |D| f32
   put(4, sizeof(float4) * P.n * P.k);           // p
   put(5, sizeof(float4) * P.n * P.k);           // q
   put(6, sizeof(float4) * P.n * P.k);           // r
@@ -1493,13 +1605,23 @@ size_t df_layout(const Plan& P, size_t* off /* 14 */) {
   put(11, sizeof(CgCtl));
   put(12, sizeof(double) * P.k * 3);
   put(13, sizeof(int) * (P.k + 1));
+  put(14, mf ? sizeof(float4) * P.n * P.k : 0);   // ps = S o p
+  put(15, mf ? sizeof(float4) * ns : 0);          // S (double-float)
+  put(16, sizeof(double) * P.k);                  // column frequency scales
+  put(17, sizeof(float) * 2 * P.k);               // the same as (hi, lo)
   return o;
 }
 
 int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
-                const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  size_t off[14];
-  df_layout(P, off);
+                const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
+                const double* col_scale = nullptr) {
+  const bool mf = col_scale != nullptr;
+  size_t off[18];
+  df_layout(P, off, mf);
+  float4* ps = reinterpret_cast<float4*>(ws + off[14]);
+  float4* Sdf = reinterpret_cast<float4*>(ws + off[15]);
+  double* dscale = reinterpret_cast<double*>(ws + off[16]);
+  float* dscale_hl = reinterpret_cast<float*>(ws + off[17]);
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);
@@ -1523,8 +1645,24 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   if (spmv_grid > nb) return PG_ERR_ARG;
 
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
-  k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
-  k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
+  if (mf) {
+    std::vector<float> hl(2 * (size_t)k);
+    for (int i = 0; i < k; ++i) {
+      hl[2 * i] = (float)col_scale[i];
+      hl[2 * i + 1] = (float)(col_scale[i] - (double)hl[2 * i]);
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(dscale, col_scale, sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(dscale_hl, hl.data(), sizeof(float) * 2 * k, cudaMemcpyHostToDevice, s));
+    PG_KSWITCH(k, (k_mf_scaling<K><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, dscale, S, wd, wdf,
+                                                                          dstatus)));
+    k_mf_sdf<<<pg_blocks(P.n * k, 256), 256, 0, s>>>(S, P.n * k, Sdf);
+    k_mf_df_matrix<<<pg_blocks(P.nnz, 256), 256, 0, s>>>(A, P.nnz, At);
+    // the host copy of the scales must outlive the asynchronous copy
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+  } else {
+    k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
+    k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
+  }
   PG_LAUNCH_CHECK();
   std::vector<double> bnorm(k), rn(k), tgt(k);
   std::vector<int> wnt(k);
@@ -1538,6 +1676,13 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     pg_set_error("pg_cocg: zero diagonal entry (Jacobi scaling undefined)");
     return PG_ERR_BREAKDOWN;
   }
+  auto true_residual = [&]() {
+    if (mf) {
+      PG_KSWITCH(k, (k_mf_resid<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(rowptr, col, A, P.n, dscale, x, b, r64)));
+    } else {
+      launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+    }
+  };
   const char* mon_env = getenv("PG_KSP_MONITOR");
   const bool monitor = mon_env && mon_env[0] && mon_env[0] != '0';
   int64_t its = 0, checks = 0, launch_iter = 1;
@@ -1547,7 +1692,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   bool first = true;
   const double delta = 1e-3;   // double-float recurrence: replace after 3 decades
   for (;;) {
-    launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+    true_residual();
     PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
                    k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
     PG_LAUNCH_CHECK();
@@ -1582,12 +1727,25 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
-    PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part),
-                   k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    if (mf) {
+      PG_KSWITCH(k, (k_df_start<K, true><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part, ps)));
+    } else {
+      PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part)));
+    }
+    PG_KSWITCH(k, (k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
     for (int it = 0; it < steps; ++it) {
       const int iter = (int)(launch_iter + it);
+      if (mf) {
+        PG_KSWITCH(k, (k_mf_spmm<K><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, dscale_hl, Sdf, pv, ps, q,
+                                                                   part, st, ctl),
+                       k_df_update<K, true><<<nb, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter,
+                                                                   delta),
+                       k_df_pupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter,
+                                                                                               ps, Sdf)));
+        continue;
+      }
       switch (k) {
         case 1:
           switch (npr > 64 ? 8 : 4) {
@@ -1603,7 +1761,11 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     }
     PG_LAUNCH_CHECK();
     launch_iter += steps;
-    PG_KSWITCH(k, (k_df_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    if (mf) {
+      PG_KSWITCH(k, (k_df_xupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    } else {
+      PG_KSWITCH(k, (k_df_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    }
     std::vector<int> hits(k), hbrk(k);
     for (int i = 0; i < k; ++i) {
       PG_CUDA_TRY(cudaMemcpyAsync(&hits[i], &st[i].its, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1620,7 +1782,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     if (brk) {
       pg_set_error("pg_cocg: breakdown (p^T A p = 0 or r^T r = 0)");
       status = PG_ERR_BREAKDOWN;
-      launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+      true_residual();
       PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
                      k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
       PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
@@ -1740,7 +1902,7 @@ static Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = cg_plan(n, nnz, nrhs, opts);
-  size_t off[14];
+  size_t off[18];
   return (opts->precision == 2 ? df_layout(P, off) : cg_layout(P, off)) + 256;
 }
 
@@ -1766,4 +1928,39 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
   if (P.prec == 0) return run_cocg<double2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
   if (P.prec == 2) return run_cocg_df(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
   return run_cocg<float2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
+}
+
+extern "C" size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs) {
+  if (n < 1 || !valid_k(nrhs)) return 0;
+  pg_cocg_opts o;
+  pg_cocg_default_opts(&o);
+  o.precision = 2;
+  Plan P = cg_plan(n, nnz, nrhs, &o);
+  size_t off[18];
+  return df_layout(P, off, true) + 256;
+}
+
+extern "C" int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
+                                 const double* b, double* x, int nrhs, const double* col_scale,
+                                 const pg_cocg_opts* opts, pg_gmres_result* result, double* relres_per_rhs,
+                                 void* workspace, size_t workspace_bytes, void* stream) {
+  if (!opts || !rowptr || !col || !vals || !b || !x || !col_scale || n < 1 || nnz < n || !valid_k(nrhs) ||
+      !(opts->rtol > 0.0) || opts->precision != 2) {
+    pg_set_error("pg_cocg_multifreq: bad argument (nrhs 1..32 power of two, rtol > 0, precision 2)");
+    return PG_ERR_ARG;
+  }
+  for (int i = 0; i < nrhs; ++i)
+    if (!(col_scale[i] > 0.0) || !isfinite(col_scale[i])) {
+      pg_set_error("pg_cocg_multifreq: column frequency scales must be positive");
+      return PG_ERR_ARG;
+    }
+  const size_t need = pg_cocg_multifreq_workspace_bytes(n, nnz, nrhs);
+  if (!workspace || workspace_bytes < need) {
+    pg_set_error("pg_cocg_multifreq: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  char* ws = reinterpret_cast<char*>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+  Plan P = cg_plan(n, nnz, nrhs, opts);
+  return run_cocg_df(P, rowptr, col, reinterpret_cast<const double2*>(vals), reinterpret_cast<const double2*>(b),
+                     reinterpret_cast<double2*>(x), opts, result, relres_per_rhs, ws, pg_stream(stream), col_scale);
 }
