@@ -28,6 +28,7 @@
 #include <string.h>
 #include <stdio.h>
 
+#include <mutex>
 #include <vector>
 
 #include "pg_common.cuh"
@@ -1093,6 +1094,10 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   int* dstatus = want + P.k;
   const int write_pm = same ? 0 : 1;
   const int k = P.k, nb = P.nb;
+  // vector-update grid: at least ~4 elements per thread, so the per-block
+  // reduction does not dominate on small systems (its last block sums
+  // gridDim.x partials)
+  const int nbu = (int)std::min<int64_t>(nb, std::max<int64_t>(152 * 2, (P.n * P.k + 4 * kThreads - 1) / (4 * kThreads)));
   const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
   const int spmv_grid = 152 * 16;
   if (spmv_grid > nb) return PG_ERR_ARG;  // partial buffers are sized by nb
@@ -1165,7 +1170,7 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     for (int it = 0; it < steps; ++it) {
       const int iter = (int)(launch_iter + it);
       launch_cg_spmv<CM>(P, rowptr, col, At, pm, pv, q, part, st, ctl, npr, spmv_grid, s);
-      PG_KSWITCH(k, (k_cg_update<CM, K><<<nb, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
+      PG_KSWITCH(k, (k_cg_update<CM, K><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
                      k_cg_pupdate<CM, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, pm, r, P.n, st, iter,
                                                                                           write_pm)));
     }
@@ -1266,6 +1271,41 @@ __device__ __forceinline__ void cdf_add(float4& a, float4 b) {
   df_add(a.z, a.w, b.z, b.w);
 }
 
+// Block reductions of double-float values: the warp and block stages add in
+// double-float on the FP32 pipes and only the block total is converted to
+// double (GB300's FP64 pipe runs ~2 operations per clock per SM, so a
+// per-thread conversion plus a double-precision shuffle tree cost more than
+// the vector update they reduce).  Lanes with equal lane % K combine.
+template <int K>
+__device__ void block_reduce_df(float4 v, float4* smf, double2* out) {
+#pragma unroll
+  for (int off = 16; off >= K; off >>= 1) cdf_add(v, shfl_xor4(v, off));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K) smf[warp * K + lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    float4 t = smf[threadIdx.x];
+    for (int w = 1; w < kThreads / 32; ++w) cdf_add(t, smf[w * K + threadIdx.x]);
+    out[threadIdx.x] = cdf_to(t);
+  }
+  __syncthreads();
+}
+
+template <int K>
+__device__ void block_reduce_f(float v, float* smf, double2* out) {
+#pragma unroll
+  for (int off = 16; off >= K; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K) smf[warp * K + lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    float t = smf[threadIdx.x];
+    for (int w = 1; w < kThreads / 32; ++w) t += smf[w * K + threadIdx.x];
+    out[threadIdx.x] = make_double2((double)t, 0.0);
+  }
+  __syncthreads();
+}
+
 // alpha / beta finalisation shared by the df kernels (last block only)
 template <int K>
 __device__ void cg_alpha_final(const double2* partial, int nblocks, CgState* st, CgCtl* ctl, double2* smem) {
@@ -1326,7 +1366,7 @@ __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblock
 }
 
 // q = At p (double-float), partial mu = p^T q; last block: alpha
-template <int G>
+template <int G, int U = 1>
 __global__ void __launch_bounds__(kThreads) k_df_spmv1(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                        const float4* __restrict__ val, int64_t n,
                                                        const float4* __restrict__ pv, float4* __restrict__ q,
@@ -1344,7 +1384,21 @@ __global__ void __launch_bounds__(kThreads) k_df_spmv1(const int64_t* __restrict
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid) {
       const int64_t e = rowptr[r + 1];
-      for (int64_t k = rowptr[r] + lane; k < e; k += G) cdf_mac(acc, val[k], pv[col[k]]);
+      int64_t k = rowptr[r] + lane;
+      if (U == 2) {
+        // two independent accumulators: two gathers in flight per lane
+        float4 acc1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (; k + G < e; k += 2 * G) {
+          const int32_t c0 = col[k], c1 = col[k + G];
+          const float4 v0 = val[k], v1 = val[k + G];
+          cdf_mac(acc, v0, pv[c0]);
+          cdf_mac(acc1, v1, pv[c1]);
+        }
+        if (k < e) cdf_mac(acc, val[k], pv[col[k]]);
+        cdf_add(acc, acc1);
+      } else {
+        for (; k < e; k += G) cdf_mac(acc, val[k], pv[col[k]]);
+      }
     }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) cdf_add(acc, shfl_xor4(acc, off));
@@ -1354,11 +1408,12 @@ __global__ void __launch_bounds__(kThreads) k_df_spmv1(const int64_t* __restrict
       cdf_mac(mu, pv[r], acc);
     }
   }
-  block_reduce_rhs<1>(cdf_to(mu), smem, partial + blockIdx.x);
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<1>(mu, smf, partial + blockIdx.x);
   if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
 }
 
-template <int K>
+template <int K, int U = 1>
 __global__ void __launch_bounds__(kThreads) k_df_spmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                       const float4* __restrict__ val, int64_t n,
                                                       const float4* __restrict__ pv, float4* __restrict__ q,
@@ -1371,12 +1426,26 @@ __global__ void __launch_bounds__(kThreads) k_df_spmm(const int64_t* __restrict_
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; r < n; r += rows_per_pass) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const int64_t e = rowptr[r + 1];
-    for (int64_t k = rowptr[r]; k < e; ++k) cdf_mac(acc, val[k], pv[(int64_t)col[k] * K + rhs]);
+    int64_t k = rowptr[r];
+    if (U == 2) {
+      float4 acc1 = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (; k + 1 < e; k += 2) {
+        const int32_t c0 = col[k], c1 = col[k + 1];
+        const float4 v0 = val[k], v1 = val[k + 1];
+        cdf_mac(acc, v0, pv[(int64_t)c0 * K + rhs]);
+        cdf_mac(acc1, v1, pv[(int64_t)c1 * K + rhs]);
+      }
+      if (k < e) cdf_mac(acc, val[k], pv[(int64_t)col[k] * K + rhs]);
+      cdf_add(acc, acc1);
+    } else {
+      for (; k < e; ++k) cdf_mac(acc, val[k], pv[(int64_t)col[k] * K + rhs]);
+    }
     acc = df_norm(acc);
     q[r * K + rhs] = acc;
     cdf_mac(mu, pv[r * K + rhs], acc);
   }
-  block_reduce_rhs<K>(cdf_to(mu), smem, partial + (int64_t)blockIdx.x * K);
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<K>(mu, smf, partial + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
 }
 
@@ -1414,8 +1483,9 @@ __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, 
     cdf_mac(rho, re, re);
     ww += (re.x * re.x + re.z * re.z) * wd[PC ? e : e / K];
   }
-  block_reduce_rhs<K>(cdf_to(rho), smem, prho + (int64_t)blockIdx.x * K);
-  block_reduce_rhs<K>(make_double2((double)ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  block_reduce_f<K>(ww, reinterpret_cast<float*>(smf), pw + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) cg_beta_final<K>(prho, pw, gridDim.x, st, ctl, iter, delta, smem);
 }
 
@@ -1561,7 +1631,8 @@ __global__ void __launch_bounds__(kThreads) k_mf_spmm(const int64_t* __restrict_
     q[r * K + rhs] = out;
     cdf_mac(mu, pv[r * K + rhs], out);
   }
-  block_reduce_rhs<K>(cdf_to(mu), smem, partial + (int64_t)blockIdx.x * K);
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<K>(mu, smf, partial + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
 }
 
@@ -1612,6 +1683,89 @@ size_t df_layout(const Plan& P, size_t* off /* 18 */, bool mf = false) {
   return o;
 }
 
+// ---- SpMV variant autotuner ------------------------------------------------
+// The double-float product's best lanes-per-row / unrolling depends on the
+// matrix (rows, stored entries per row) and the RHS count.  At the first
+// cycle of a solve each candidate runs 3 times on the actual operands (the
+// product is the first kernel of an iteration and recomputes alpha, so extra
+// runs change no solver state) and the fastest is kept per (n, nnz, k).
+// PG_AUTOTUNE=0 keeps the default variant.
+struct TuneEntry {
+  int64_t n, nnz;
+  int k, variant;
+};
+std::vector<TuneEntry> g_tune;
+std::mutex g_tune_mu;
+
+int tuned_variant(int64_t n, int64_t nnz, int k) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  for (const TuneEntry& t : g_tune)
+    if (t.n == n && t.nnz == nnz && t.k == k) return t.variant;
+  return -1;
+}
+
+void store_variant(int64_t n, int64_t nnz, int k, int v) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune.push_back(TuneEntry{n, nnz, k, v});
+}
+
+bool autotune_enabled() {
+  const char* e = getenv("PG_AUTOTUNE");
+  return !(e && e[0] == '0');
+}
+
+// single RHS: variant = lanes per row G (1..8) * 10 + unroll U
+void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
+                     const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st,
+                     CgCtl* ctl) {
+  switch (variant) {
+    case 21: k_df_spmv1<2, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 22: k_df_spmv1<2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 42: k_df_spmv1<4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 81: k_df_spmv1<8, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 82: k_df_spmv1<8, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    default: k_df_spmv1<4, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+  }
+}
+
+template <int K>
+void launch_df_spmm(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
+                    const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st, CgCtl* ctl) {
+  if (variant == 2)
+    k_df_spmm<K, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else
+    k_df_spmm<K, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+}
+
+// time each candidate (3 runs after 1 warm-up) and return the fastest
+template <typename F>
+int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return cands[0];
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return cands[0];
+  }
+  int best = cands[0];
+  float best_ms = 1e30f;
+  for (int v : cands) {
+    launch(v);
+    cudaEventRecord(a, s);
+    for (int i = 0; i < 3; ++i) launch(v);
+    cudaEventRecord(b, s);
+    if (cudaEventSynchronize(b) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
+
 int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
                 const double* col_scale = nullptr) {
@@ -1640,6 +1794,10 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   int* want = reinterpret_cast<int*>(ws + off[13]);
   int* dstatus = want + P.k;
   const int k = P.k, nb = P.nb;
+  // vector-update grid: at least ~4 elements per thread, so the per-block
+  // reduction does not dominate on small systems (its last block sums
+  // gridDim.x partials)
+  const int nbu = (int)std::min<int64_t>(nb, std::max<int64_t>(152 * 2, (P.n * P.k + 4 * kThreads - 1) / (4 * kThreads)));
   const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
   const int spmv_grid = 152 * 16;
   if (spmv_grid > nb) return PG_ERR_ARG;
@@ -1690,6 +1848,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   const int64_t max_it = o->max_it > 0 ? o->max_it : 100000;
   int chunk = o->check_every > 0 ? o->check_every : 50;
   bool first = true;
+  int variant = 41;
   const double delta = 1e-3;   // double-float recurrence: replace after 3 decades
   for (;;) {
     true_residual();
@@ -1733,6 +1892,27 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part)));
     }
     PG_KSWITCH(k, (k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    if (first && !mf) {
+      variant = tuned_variant(P.n, P.nnz, k);
+      if (variant < 0) {
+        if (autotune_enabled()) {
+          if (k == 1)
+            variant = pick_fastest({41, 42, 22, 82, 21}, [&](int v) {
+              launch_df_spmv1(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl);
+            }, s);
+          else
+            variant = pick_fastest({1, 2}, [&](int v) {
+              PG_KSWITCH(k, (launch_df_spmm<K>(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+            }, s);
+          PG_LAUNCH_CHECK();
+        } else {
+          variant = k == 1 ? 41 : 1;
+        }
+        store_variant(P.n, P.nnz, k, variant);
+      }
+      if (monitor) fprintf(stderr, "pg_cocg(df64): SpMV variant %d for n=%lld nnz=%lld k=%d\n", variant,
+                           (long long)P.n, (long long)P.nnz, k);
+    }
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
     for (int it = 0; it < steps; ++it) {
@@ -1740,23 +1920,17 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       if (mf) {
         PG_KSWITCH(k, (k_mf_spmm<K><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, dscale_hl, Sdf, pv, ps, q,
                                                                    part, st, ctl),
-                       k_df_update<K, true><<<nb, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter,
+                       k_df_update<K, true><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter,
                                                                    delta),
                        k_df_pupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter,
                                                                                                ps, Sdf)));
         continue;
       }
-      switch (k) {
-        case 1:
-          switch (npr > 64 ? 8 : 4) {
-            case 8: k_df_spmv1<8><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, pv, q, part, st, ctl); break;
-            default: k_df_spmv1<4><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, pv, q, part, st, ctl); break;
-          }
-          break;
-        default:
-          PG_KSWITCH(k, (k_df_spmm<K><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, pv, q, part, st, ctl)));
-      }
-      PG_KSWITCH(k, (k_df_update<K><<<nb, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter, delta),
+      if (k == 1)
+        launch_df_spmv1(variant, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl);
+      else
+        PG_KSWITCH(k, (launch_df_spmm<K>(variant, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+      PG_KSWITCH(k, (k_df_update<K><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter, delta),
                      k_df_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter)));
     }
     PG_LAUNCH_CHECK();
