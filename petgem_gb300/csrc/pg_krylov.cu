@@ -708,7 +708,7 @@ struct CgCtl {
   int any_active;      // some RHS still iterating in this cycle
   int nonfinite;
   unsigned counter;    // last-block-done counter (reset by the last block)
-  int pad;
+  int pending;         // double-float path: a p update is due (set by the update, cleared by the product)
 };
 
 template <typename C>
@@ -1339,7 +1339,7 @@ __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblock
   if (threadIdx.x < K) {
     CgState& S = st[threadIdx.x];
     if (S.active) {
-      S.beta_iter = iter;
+      S.beta_iter = 1;   // fresh beta: the next p update applies it once
       S.its += 1;
       S.res = sqrt(w.x);
       if (!isfinite(S.res)) ctl->nonfinite = 1;
@@ -1355,12 +1355,14 @@ __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblock
       else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
     } else {
       S.beta = make_double2(0.0, 0.0);
+      S.beta_iter = 0;
     }
     if (S.active) atomicOr(&any, 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     ctl->any_active = any && !stop;
+    ctl->pending = 1;
     ctl->counter = 0;
   }
 }
@@ -1371,6 +1373,7 @@ __global__ void __launch_bounds__(kThreads) k_df_spmv1(const int64_t* __restrict
                                                        const float4* __restrict__ val, int64_t n,
                                                        const float4* __restrict__ pv, float4* __restrict__ q,
                                                        double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   const int lane = threadIdx.x % G;
@@ -1418,6 +1421,7 @@ __global__ void __launch_bounds__(kThreads) k_df_spmm(const int64_t* __restrict_
                                                       const float4* __restrict__ val, int64_t n,
                                                       const float4* __restrict__ pv, float4* __restrict__ q,
                                                       double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   const int rhs = threadIdx.x % K;
@@ -1491,13 +1495,15 @@ __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, 
 
 template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_df_pupdate(float4* __restrict__ pv, const float4* __restrict__ r, int64_t n,
-                                                         const CgState* st, int iter, float4* __restrict__ ps = nullptr,
+                                                         const CgState* st, const CgCtl* ctl,
+                                                         float4* __restrict__ ps = nullptr,
                                                          const float4* __restrict__ Sdf = nullptr) {
   __shared__ float4 bt[kMaxK];
   __shared__ int use[kMaxK];
+  if (!ctl->pending) return;
   if (threadIdx.x < K) {
     bt[threadIdx.x] = cdf_from(st[threadIdx.x].beta);
-    use[threadIdx.x] = st[threadIdx.x].beta_iter == iter;
+    use[threadIdx.x] = st[threadIdx.x].beta_iter == 1;
   }
   __syncthreads();
   int anyuse = 0;
@@ -1610,6 +1616,7 @@ __global__ void __launch_bounds__(kThreads) k_mf_spmm(const int64_t* __restrict_
                                                       const float4* __restrict__ Sdf, const float4* __restrict__ pv,
                                                       const float4* __restrict__ ps, float4* __restrict__ q,
                                                       double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   const int rhs = threadIdx.x % K;
@@ -1766,6 +1773,8 @@ int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
   return best;
 }
 
+constexpr int kGraphIters = 16;   // iterations per captured CUDA graph
+
 int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
                 const double* col_scale = nullptr) {
@@ -1843,13 +1852,70 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   };
   const char* mon_env = getenv("PG_KSP_MONITOR");
   const bool monitor = mon_env && mon_env[0] && mon_env[0] != '0';
-  int64_t its = 0, checks = 0, launch_iter = 1;
+  int64_t its = 0, checks = 0;
   int status = PG_OK;
   const int64_t max_it = o->max_it > 0 ? o->max_it : 100000;
   int chunk = o->check_every > 0 ? o->check_every : 50;
   bool first = true;
   int variant = 41;
   const double delta = 1e-3;   // double-float recurrence: replace after 3 decades
+  // one iteration: product (alpha), vector update (beta), direction update;
+  // no per-iteration launch arguments, so a run of them can be captured once
+  // in a CUDA graph and replayed
+  auto one_iteration = [&](cudaStream_t ss) {
+    if (mf) {
+      PG_KSWITCH(k, (k_mf_spmm<K><<<spmv_grid, kThreads, 0, ss>>>(rowptr, col, At, P.n, dscale_hl, Sdf, pv, ps, q,
+                                                                  part, st, ctl),
+                     k_df_update<K, true><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, 0,
+                                                                    delta),
+                     k_df_pupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, r, P.n, st, ctl,
+                                                                                              ps, Sdf)));
+      return;
+    }
+    if (k == 1)
+      launch_df_spmv1(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl);
+    else
+      PG_KSWITCH(k, (launch_df_spmm<K>(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+    PG_KSWITCH(k, (k_df_update<K><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, 0, delta),
+                   k_df_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, r, P.n, st, ctl)));
+  };
+  const char* genv = getenv("PG_GRAPHS");
+  const bool use_graphs = !(genv && genv[0] == '0');
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_failed = false;
+  auto build_graph = [&]() {
+    if (graph_failed) return;
+    cudaGraph_t graph = nullptr;
+    bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      for (int g = 0; g < kGraphIters; ++g) one_iteration(cs);
+      ok = cudaStreamEndCapture(cs, &graph) == cudaSuccess && graph != nullptr;
+    }
+    if (ok) ok = cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+      cudaGetLastError();   // capture unavailable: keep launching directly
+      gexec = nullptr;
+      graph_failed = true;
+    }
+  };
+  struct GraphCleanup {
+    cudaStream_t& cs;
+    cudaEvent_t& a;
+    cudaEvent_t& b;
+    cudaGraphExec_t& g;
+    ~GraphCleanup() {
+      if (g) cudaGraphExecDestroy(g);
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      if (cs) cudaStreamDestroy(cs);
+    }
+  } graph_cleanup{cs, ev_in, ev_out, gexec};
   for (;;) {
     true_residual();
     PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
@@ -1915,26 +1981,19 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     }
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
-    for (int it = 0; it < steps; ++it) {
-      const int iter = (int)(launch_iter + it);
-      if (mf) {
-        PG_KSWITCH(k, (k_mf_spmm<K><<<spmv_grid, kThreads, 0, s>>>(rowptr, col, At, P.n, dscale_hl, Sdf, pv, ps, q,
-                                                                   part, st, ctl),
-                       k_df_update<K, true><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter,
-                                                                   delta),
-                       k_df_pupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter,
-                                                                                               ps, Sdf)));
-        continue;
+    int done = 0;
+    if (use_graphs && steps >= kGraphIters) {
+      if (!gexec) build_graph();
+      if (gexec) {
+        // replay the captured iterations on the capture stream, joined to s
+        cudaEventRecord(ev_in, s);
+        cudaStreamWaitEvent(cs, ev_in, 0);
+        for (; done + kGraphIters <= steps; done += kGraphIters) cudaGraphLaunch(gexec, cs);
+        cudaEventRecord(ev_out, cs);
+        cudaStreamWaitEvent(s, ev_out, 0);
       }
-      if (k == 1)
-        launch_df_spmv1(variant, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl);
-      else
-        PG_KSWITCH(k, (launch_df_spmm<K>(variant, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl)));
-      PG_KSWITCH(k, (k_df_update<K><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, iter, delta),
-                     k_df_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, r, P.n, st, iter)));
     }
-    PG_LAUNCH_CHECK();
-    launch_iter += steps;
+    for (; done < steps; ++done) one_iteration(s);    PG_LAUNCH_CHECK();
     if (mf) {
       PG_KSWITCH(k, (k_df_xupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
     } else {
