@@ -379,6 +379,17 @@ int pg_mt_rhs(const double* nodes, const int32_t* elemsN, const int8_t* eo, cons
               const int32_t* seg_start, const int32_t* seg_dof, int64_t n_seg, double* b, int nrhs, int rhs,
               void* workspace, size_t workspace_bytes, void* stream);
 
+/* Nodal E and H for visualisation (petgem/postprocessing.py:173-260): each
+ * element evaluates E and curl E at its vertices pulled 0.01 % towards the
+ * centroid; a node gets the mean over its elements (ascending element order),
+ * H = curl E / (i omega mu).  fields complex128 [n_nodes, 6] (Ex..Hz); a node
+ * in no element gives NaN, as petgem's 0/0 does.
+ * Workspace: pg_node_fields_workspace_bytes(n_elems, n_nodes). */
+size_t pg_node_fields_workspace_bytes(int64_t n_elems, int64_t n_nodes);
+int pg_node_fields(const double* x, const double* nodes, const int32_t* elemsN, const int8_t* eo, const int8_t* fo,
+                   const int32_t* dofs, int p, int64_t n_elems, int64_t n_nodes, double omega_mu, double* fields,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------
  * Adjoint gradient of a receiver misfit (no petgem counterpart; built from
  * the elemental mass matrices of hvfem.py:223-316 and the interpolation of

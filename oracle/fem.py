@@ -168,3 +168,27 @@ def interpolate_fields(x, nodes, elemsN, eo, fo, dofs, p, pts, frequency):
         F[i, 3:] = C[:, :, 0] @ xe
     F[:, 3:] /= 1j * 2.0 * np.pi * frequency * MU0
     return F, el
+
+
+def node_fields(x, nodes, elemsN, eo, fo, dofs, p, frequency, scale=0.9999):
+    """Nodal E and H for visualisation (petgem/postprocessing.py:173-260):
+    per element, E and curl E at the vertices pulled towards the centroid by
+    `scale`; summed per node in element order, divided by the number of
+    elements sharing the node; H = curl E / (i omega mu)."""
+    nn = nodes.shape[0]
+    acc = np.zeros((nn, 6), dtype=np.complex128)
+    cnt = np.zeros(nn)
+    for e in range(elemsN.shape[0]):
+        coords = nodes[elemsN[e]]
+        cen = coords.sum(axis=0) / 4.0
+        pts = cen + (coords - cen) * scale
+        xi = xyz_to_reference(coords, pts)
+        N, C = basis_at(coords, eo[e], fo[e], p, xi)
+        xe = x[dofs[e]]
+        for k in range(4):
+            acc[elemsN[e, k], :3] += N[:, :, k] @ xe
+            acc[elemsN[e, k], 3:] += C[:, :, k] @ xe
+            cnt[elemsN[e, k]] += 1
+    acc /= cnt[:, None]
+    acc[:, 3:] /= 1j * 2.0 * np.pi * frequency * MU0
+    return acc

@@ -95,6 +95,8 @@ SIGNATURES = {
     "pg_mt_rhs_workspace_bytes": (_SZ, [_I64, _INT]),
     "pg_mt_rhs": (_INT, [_P, _P, _P, _P, _INT, _P, _P, _P, _I64, _P, _INT, _P, _INT, _D, _D, _P, _P, _P, _I64, _P, _INT,
                          _INT, _P, _SZ, _P]),
+    "pg_node_fields_workspace_bytes": (_SZ, [_I64, _I64]),
+    "pg_node_fields": (_INT, [_P, _P, _P, _P, _P, _P, _INT, _I64, _I64, _D, _P, _P, _SZ, _P]),
     "pg_receiver_adjoint_workspace_bytes": (_SZ, [_INT, _I64]),
     "pg_receiver_adjoint": (_INT, [_P, _P, _P, _P, _P, _INT, _P, _P, _I64, _P, _P, _P, _SZ, _P]),
     "pg_element_mass_bilinear": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _INT, _P, _P]),

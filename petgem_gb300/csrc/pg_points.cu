@@ -351,3 +351,137 @@ extern "C" int pg_receiver_adjoint(const double* nodes, const int32_t* elemsN, c
   PG_LAUNCH_CHECK();
   return PG_OK;
 }
+
+// ---- nodal fields for visualisation (petgem/postprocessing.py:173-260) ------
+// Every element evaluates E = sum_j x_j N_j and curl E at its four vertices
+// pulled 0.01 % towards the centroid; a node's value is the mean over the
+// elements that share it (summed in ascending element order), and H = curl E /
+// (i omega mu).  One thread per node walks its (element, vertex) list, sorted
+// once per call, so no atomics are needed.
+#include "pg_sort.cuh"
+
+namespace {
+
+__global__ void k_node_keys(const int32_t* elemsN, int64_t T, uint64_t* keys, int32_t* vals) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 4 * T; i += (int64_t)gridDim.x * blockDim.x) {
+    keys[i] = (uint64_t)(uint32_t)elemsN[i];
+    vals[i] = (int32_t)i;
+  }
+}
+
+__global__ void k_node_first(const uint64_t* keys, int64_t m, int64_t n_nodes, int32_t* first) {
+  // first[node] = position of the node's first entry; n_nodes + 1 entries, -1 where absent
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    if (i == 0 || keys[i] != keys[i - 1]) first[keys[i]] = (int32_t)i;
+}
+
+template <int P>
+__device__ void phys_basis_ref(const Geo& g, const int8_t* eo8, const int8_t* fo8, const double xi[3], double* N,
+                               double* C) {
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  int eo[6], fo[4];
+  for (int i = 0; i < 6; ++i) eo[i] = eo8[i];
+  for (int i = 0; i < 4; ++i) fo[i] = fo8[i];
+  double Nr[3 * ND], Cr[3 * ND];
+  pg_shape3d<P>(xi[0], xi[1], xi[2], eo, fo, Nr, Cr, ND);
+  for (int j = 0; j < ND; ++j)
+    for (int a = 0; a < 3; ++a) {
+      N[a * ND + j] = g.inv[a][0] * Nr[j] + g.inv[a][1] * Nr[ND + j] + g.inv[a][2] * Nr[2 * ND + j];
+      C[a * ND + j] = (g.J[0][a] * Cr[j] + g.J[1][a] * Cr[ND + j] + g.J[2][a] * Cr[2 * ND + j]) / g.det;
+    }
+}
+
+template <int P>
+__global__ void k_node_fields(const double2* x, const double* nodes, const int32_t* elemsN, const int8_t* eo,
+                              const int8_t* fo, const int32_t* dofs, const uint64_t* keys, const int32_t* vals,
+                              int64_t m, const int32_t* first, int64_t n_nodes, double omega_mu, double2* out) {
+  constexpr int ND = P * (P + 2) * (P + 3) / 2;
+  const double scale = 0.9999;
+  const double vref[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int64_t nd = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; nd < n_nodes;
+       nd += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc[6];
+    for (int c = 0; c < 6; ++c) acc[c] = make_double2(0.0, 0.0);
+    int cnt = 0;
+    const int32_t f0 = first[nd];
+    for (int64_t i = f0; f0 >= 0 && i < m && keys[i] == (uint64_t)nd; ++i) {
+      const int64_t e = vals[i] / 4;
+      const int v = vals[i] % 4;
+      Geo g;
+      if (!load_geo(nodes, elemsN, e, g)) continue;
+      double xi[3];
+      for (int a = 0; a < 3; ++a) xi[a] = 0.25 + (vref[v][a] - 0.25) * scale;
+      double N[3 * ND], C[3 * ND];
+      phys_basis_ref<P>(g, eo + 6 * e, fo + 4 * e, xi, N, C);
+      for (int j = 0; j < ND; ++j) {
+        const double2 xj = x[dofs[e * ND + j]];
+        for (int a = 0; a < 3; ++a) {
+          acc[a].x += xj.x * N[a * ND + j];
+          acc[a].y += xj.y * N[a * ND + j];
+          acc[3 + a].x += xj.x * C[a * ND + j];
+          acc[3 + a].y += xj.y * C[a * ND + j];
+        }
+      }
+      ++cnt;
+    }
+    const double inv = 1.0 / (double)cnt;   // a node in no element gives NaN, as 0/0 does in petgem
+    double2* o = out + 6 * nd;
+    for (int a = 0; a < 3; ++a) o[a] = make_double2(acc[a].x * inv, acc[a].y * inv);
+    // H = curl E / (i omega mu):  (u + i w) / (i c) = w / c - i u / c
+    for (int a = 3; a < 6; ++a) o[a] = make_double2(acc[a].y * inv / omega_mu, -acc[a].x * inv / omega_mu);
+  }
+}
+
+}  // namespace
+
+extern "C" size_t pg_node_fields_workspace_bytes(int64_t n_elems, int64_t n_nodes) {
+  if (n_elems < 1 || n_nodes < 1) return 0;
+  const int64_t m = 4 * n_elems;
+  return pg_align256(sizeof(uint64_t) * (size_t)m) + pg_align256(sizeof(int32_t) * (size_t)m) +
+         pg_align256(sizeof(int32_t) * (size_t)(n_nodes + 1)) + pg_align256(pg::sort_workspace_bytes(m)) + 512;
+}
+
+extern "C" int pg_node_fields(const double* x, const double* nodes, const int32_t* elemsN, const int8_t* eo,
+                              const int8_t* fo, const int32_t* dofs, int p, int64_t n_elems, int64_t n_nodes,
+                              double omega_mu, double* fields, void* workspace, size_t workspace_bytes,
+                              void* stream) {
+  if (n_elems < 1 || n_nodes < 1 || p < 1 || p > 6 || !x || !nodes || !elemsN || !eo || !fo || !dofs || !fields ||
+      !(omega_mu > 0) || 4 * n_elems >= (1ll << 31)) {
+    pg_set_error("pg_node_fields: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (!workspace || workspace_bytes < pg_node_fields_workspace_bytes(n_elems, n_nodes)) {
+    pg_set_error("pg_node_fields: workspace too small");
+    return PG_ERR_WORKSPACE;
+  }
+  cudaStream_t s = pg_stream(stream);
+  const int64_t m = 4 * n_elems;
+  PgArena ar(workspace, workspace_bytes);
+  uint64_t* keys = ar.take<uint64_t>(m);
+  int32_t* vals = ar.take<int32_t>(m);
+  int32_t* first = ar.take<int32_t>(n_nodes + 1);
+  const size_t sb = pg::sort_workspace_bytes(m);
+  void* sws = ar.take<char>(sb);
+  if (!keys || !vals || !first || !sws) return PG_ERR_WORKSPACE;
+  k_node_keys<<<pg_blocks(m, 256), 256, 0, s>>>(elemsN, n_elems, keys, vals);
+  int st = pg::sort_pairs(keys, vals, m, pg::bits_for((uint64_t)n_nodes), sws, sb, s);
+  if (st) return st;
+  PG_CUDA_TRY(cudaMemsetAsync(first, 0xff, sizeof(int32_t) * (n_nodes + 1), s));
+  k_node_first<<<pg_blocks(m, 256), 256, 0, s>>>(keys, m, n_nodes, first);
+  const double2* xx = reinterpret_cast<const double2*>(x);
+  double2* out = reinterpret_cast<double2*>(fields);
+  const unsigned grid = pg_blocks(n_nodes, 64);
+#define PG_NF(P) \
+  k_node_fields<P><<<grid, 64, 0, s>>>(xx, nodes, elemsN, eo, fo, dofs, keys, vals, m, first, n_nodes, omega_mu, out)
+  switch (p) {
+    case 1: PG_NF(1); break;
+    case 2: PG_NF(2); break;
+    case 3: PG_NF(3); break;
+    case 4: PG_NF(4); break;
+    case 5: PG_NF(5); break;
+    case 6: PG_NF(6); break;
+  }
+#undef PG_NF
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

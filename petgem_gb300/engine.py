@@ -467,6 +467,16 @@ class DeviceMesh:
                       _p(ws), ws.numel(), _s())
         return b
 
+    def node_fields(self, x, frequency):
+        """Nodal E and H (complex128 [n_nodes, 6]) for visualisation
+        (petgem/postprocessing.py:173-260)."""
+        out = torch.empty((self.n_nodes, 6), dtype=torch.complex128, device=self.device)
+        ws = _ws(_lib.query("pg_node_fields_workspace_bytes", self.T, self.n_nodes), self.device)
+        omu = 2.0 * math.pi * float(frequency) * MU0
+        _lib.call("pg_node_fields", _p(x.contiguous()), _p(self.nodes), _p(self.elemsN), _p(self.eo), _p(self.fo),
+                  _p(self.dofs), self.p, self.T, self.n_nodes, omu, _p(out), _p(ws), ws.numel(), _s())
+        return out
+
     def receiver_adjoint(self, weights, receivers, b=None):
         """b += G^T w: the transpose of the E part of receiver_fields, with
         weights complex128 [R, 3] per (kept or dropped) receiver in the order

@@ -243,9 +243,35 @@ class Postprocessing:
                     out[f"model/phase/{k}"] = phase[j]
                 out["model/tipper/x"], out["model/tipper/y"] = tip[0], tip[1]
         name = f"{mode}_petgemV{VERSION}_{datetime.datetime.today().strftime('%Y-%m-%d')}"
+        if output.get("vtk"):
+            self.vtk_file = write_vtk_fields(m, xs, bundle, mode, model[mode], freq,
+                                             os.path.join(output["directory"], name + ".vtk"))
         self.output_file = write_results(os.path.join(output["directory"], name), out)
         Timers()["Postprocessing"].stop()
         return F if mode == "csem" else Fs
+
+
+def write_vtk_fields(m, xs, bundle, mode, data_model, freq, path):
+    """Nodal E and H (GPU node averaging) and the conductivity as a VTK file
+    with petgem's array names (postprocessing.py:173-336); petgem stores the
+    horizontal conductivity in both cell arrays, and so does this file."""
+    from . import vtk
+    pd = {}
+    if mode == "csem":
+        tags = [""]
+    else:
+        pols = [str(q) for q in data_model["polarization"]]
+        tags = ["_mode" + q for q in pols]
+    for x, tag in zip(xs, tags):
+        F = m.node_fields(x, freq).cpu().numpy()
+        for c, name in enumerate(("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")):
+            pd[f"{mode}_{name}_real{tag}"] = F[:, c].real
+        for c, name in enumerate(("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")):
+            pd[f"{mode}_{name}_imag{tag}"] = F[:, c].imag
+    sigma = np.asarray(bundle["sigma"], dtype=np.float64)
+    cd = {"sigma_horizontal": sigma[:, 0], "sigma_vertical": sigma[:, 0]}
+    vtk.write(path, bundle["nodes"], bundle["tets"], pd, cd)
+    return path
 
 
 def computeImpedance(fields, omega, mu):

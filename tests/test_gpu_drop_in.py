@@ -179,12 +179,15 @@ run:
   nord: 2
   cuda: True
 output:
-  vtk: False
+  vtk: True
   directory: {tmp_path / 'out'}
   directory_scratch: {tmp_path / 'tmp'}
 """)
     setup, solver, post = run_kernel(str(params), ["-ksp_type", "cocg", "-ksp_rtol", "1e-11", "-ksp_max_it", "100000"])
     assert all(i.status == 0 for i in solver.info)
+    from petgem_gb300 import vtk
+    _, _, vfields = vtk.read(post.vtk_file)
+    assert "mt_Ex_real_modex" in vfields and "mt_Hz_imag_modey" in vfields and "sigma_horizontal" in vfields
     p = 2
     eE, eN = topology.compute_edges(tets)
     eF, fN = topology.compute_faces(tets)
