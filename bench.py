@@ -481,12 +481,15 @@ def run_solves(args, torch, mesh, model, vals, b):
     xmx, rmx = timed("cocg", "mixed", b, 3000)
     _, rg = timed("gmres", "mixed", b, 300)
     # receiver-field error of each form against a tight FP64 solve
-    xt, _ = mesh.solve(vals, b, rtol=1e-11, precision="fp64", max_it=3 * args.max_it, raise_on_fail=False, ksp="cocg")
+    # reference solution for the receiver errors: FP64 COCG two decades tighter
+    # (at 1e-11 the FP64 recurrence can stall near its attainable accuracy)
+    xt, it_ = mesh.solve(vals, b, rtol=1e-10, precision="fp64", max_it=3 * args.max_it, raise_on_fail=False, ksp="cocg")
+    out["reference_solve"] = {"rtol": 1e-10, "iterations": it_.iterations, "relres": it_.relres, "status": it_.status}
     Ft, _ = mesh.receiver_fields(xt, model.receivers, model.source["frequency"])
     j1 = fcol.index(f0)      # the workspace source at the workload frequency
     for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf)):
         F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
-        r["receiver_rel_err_vs_fp64_1e-11"] = float(torch.linalg.norm(F - Ft) / torch.linalg.norm(Ft))
+        r["receiver_rel_err_vs_fp64_1e-10"] = float(torch.linalg.norm(F - Ft) / torch.linalg.norm(Ft))
     out["fp64"] = r64
     out["df64"] = rdf
     out["df64_batched"] = rdb
