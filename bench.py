@@ -401,6 +401,10 @@ def run_gpu(args, rank, world, local_rank):
            "pipelined": "read-back of step k overlaps step k + 1 (two buffer pairs)"}
     del vals2[1], b2[1]
 
+    cpu_solve = None
+    if rank == 0 and not args.no_cpu_baseline and args.solve == "all":
+        cpu_solve = cpu_solve_rate(mesh, vals, b)
+
     solve = None
     if args.solve_iters > 0 and rank == 0:
         solve = profile_solves(args, torch, mesh, vals, b)
@@ -419,10 +423,35 @@ def run_gpu(args, rank, world, local_rank):
                            "pattern_setup_ms": round(setup_ms, 1), "orientation_tuples": mesh.n_tuples},
                 "roofline": roofline, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
                 "clocks": clk.summary(), "solve": solve}
+        if cpu_solve is not None:
+            if solve and "fp64" in solve:
+                n_it = solve["fp64"]["iterations"]
+                cpu_solve["ms_per_rhs_extrapolated"] = round(cpu_solve["ms_per_iteration"] * n_it, 1)
+                cpu_solve["iterations_from"] = f"the GPU FP64 COCG count ({n_it}, same algorithm)"
+                cpu_solve["gpu_fp64_speedup_per_rhs"] = round(cpu_solve["ms_per_rhs_extrapolated"] /
+                                                              solve["fp64"]["ms_per_rhs"], 1)
+                cpu_solve["gpu_df64_batched_speedup_per_rhs"] = round(cpu_solve["ms_per_rhs_extrapolated"] /
+                                                                      solve["df64_batched"]["ms_per_rhs"], 1)
+            line["cpu_baseline_solve"] = cpu_solve
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     return line
+
+
+def cpu_solve_rate(mesh, vals, b, iters=150):
+    """FP64 COCG (same algorithm, symmetric Jacobi) on all host cores, compiled
+    C + OpenMP (oracle/csrc/cpu_cocg.c): ms per iteration on a bounded run of
+    `iters` iterations of the workload's system."""
+    from oracle import build_cpu
+    rp, col = mesh.rowptr.cpu().numpy(), mesh.col.cpu().numpy()
+    v, bh = vals.cpu().numpy(), b.cpu().numpy()
+    build_cpu.cocg(rp, col, v, bh, 2, 1e-30)          # warm-up (page-in, thread pool)
+    t = time.time()
+    _, its, rel, st = build_cpu.cocg(rp, col, v, bh, iters, 1e-30)
+    dt = time.time() - t
+    return {"ms_per_iteration": round(dt * 1e3 / max(its, 1), 3), "sample_iterations": its,
+            "threads": os.cpu_count() or 1, "kind": "port (compiled C + OpenMP, FP64 COCG + Jacobi)"}
 
 
 def run_solves(args, torch, mesh, model, vals, b):
