@@ -466,6 +466,14 @@ typedef struct pg_cocg_opts {
   double rtol;
   int precision;
   int check_every;
+  /* entity block-Jacobi (block_p 1..6; 0 = diagonal Jacobi): the matrix is
+   * pg_pattern_build's pattern for a mesh with block_edges edges, block_faces
+   * faces and block_volumes elements at order block_p (DOFs numbered entity by
+   * entity); each entity's diagonal block is factored L D L^T and the solver
+   * runs on S A S^T, S = D^-1/2 L^-1 (blocks above 12 DOFs stay diagonal).
+   * Not used by pg_cocg_multifreq. */
+  int block_p;
+  int64_t block_edges, block_faces, block_volumes;
 } pg_cocg_opts;
 
 void pg_cocg_default_opts(pg_cocg_opts* opts);

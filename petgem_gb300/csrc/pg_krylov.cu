@@ -33,6 +33,7 @@
 
 #include "pg_common.cuh"
 #include "pg_df.cuh"
+#include "pg_blockjac.cuh"
 
 namespace {
 
@@ -471,6 +472,7 @@ struct Plan {
   int prec;           // 0 fp64 Arnoldi, 1 fp32 Arnoldi
   int nb;             // reduction blocks
   size_t csize;       // sizeof Arnoldi complex
+  BjInfo bj;          // COCG entity block-Jacobi (bj.p == 0: diagonal Jacobi)
 };
 
 size_t ws_layout(const Plan& P, size_t* off /* 14 */) {
@@ -1028,7 +1030,55 @@ __global__ void k_cg_xupdate(const double2* __restrict__ y, const double2* __res
     x[e] = dadd(x[e], cmul(S[e / K], y[e]));
 }
 
-size_t cg_layout(const Plan& P, size_t* off /* 14 */) {
+// rows of one entity must share their column list (entity-pair pattern);
+// checked through row lengths and first / last columns before block scaling
+__global__ void k_bj_check(const int64_t* rowptr, const int32_t* col, BjInfo B, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < B.n; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t f, so;
+    int na, loc;
+    B.block(r, f, na, loc, so);
+    const int64_t l0 = rowptr[f + 1] - rowptr[f], l = rowptr[r + 1] - rowptr[r];
+    if (l != l0 || l < 1 || col[rowptr[r]] != col[rowptr[f]] || col[rowptr[r + 1] - 1] != col[rowptr[f + 1] - 1])
+      *status = PG_ERR_ARG;
+  }
+}
+
+__global__ void k_fill_one(double2* S, int64_t n) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    S[r] = make_double2(1.0, 0.0);
+}
+
+struct ToCM64 {
+  __device__ double2 operator()(double2 v) const { return v; }
+};
+struct ToCM32 {
+  __device__ float2 operator()(double2 v) const { return make_float2((float)v.x, (float)v.y); }
+};
+struct IdD2 {
+  __device__ double2 operator()(double2 v) const { return v; }
+};
+
+// block-Jacobi setup shared by the COCG drivers: S (diagonal) := 1, the
+// entity factors into Sblk, |D| into wd, At = S A S^T in the solver's precision
+template <typename CM, typename Conv>
+int bj_setup(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, double2* S, double* wd,
+             double2* Sblk, CM* At, Conv conv, int* dstatus, cudaStream_t s) {
+  k_fill_one<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n);
+  k_bj_check<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, P.bj, dstatus);
+  int h = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&h, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) {
+    pg_set_error("pg_cocg: block-Jacobi needs the entity-block pattern (rows of one entity share their columns)");
+    return PG_ERR_ARG;
+  }
+  k_bj_factor<<<pg_blocks(P.n, 128), 128, 0, s>>>(rowptr, col, A, P.bj, Sblk, wd, dstatus);
+  k_bj_scale_matrix<<<pg_blocks(P.n, 128), 128, 0, s>>>(rowptr, col, A, P.bj, Sblk, At, conv);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+size_t cg_layout(const Plan& P, size_t* off /* 20 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   put(0, P.nnz * P.csize);                      // At (matrix precision)
@@ -1045,6 +1095,8 @@ size_t cg_layout(const Plan& P, size_t* off /* 14 */) {
   put(11, sizeof(CgCtl));
   put(12, sizeof(double) * P.k * 3);            // rnorm, target, (spare)
   put(13, sizeof(int) * (P.k + 1));             // want, status
+  put(18, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);     // block-Jacobi factors
+  put(19, P.bj.p ? sizeof(double2) * P.n * P.k : 0);         // S r64
   return o;
 }
 
@@ -1072,8 +1124,11 @@ void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, co
 template <typename CM>
 int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
              const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  size_t off[14];
+  size_t off[20];
   cg_layout(P, off);
+  const bool bj = P.bj.p > 0;
+  double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
+  double2* r64b = reinterpret_cast<double2*>(ws + off[19]);
   CM* At = reinterpret_cast<CM*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);
@@ -1103,8 +1158,17 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   if (spmv_grid > nb) return PG_ERR_ARG;  // partial buffers are sized by nb
 
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
-  k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
-  k_cg_scale_matrix<CM><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
+  if (bj) {
+    int st0;
+    if (sizeof(CM) == sizeof(double2))
+      st0 = bj_setup(P, rowptr, col, A, S, wd, Sblk, reinterpret_cast<double2*>(At), ToCM64(), dstatus, s);
+    else
+      st0 = bj_setup(P, rowptr, col, A, S, wd, Sblk, reinterpret_cast<float2*>(At), ToCM32(), dstatus, s);
+    if (st0) return st0;
+  } else {
+    k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
+    k_cg_scale_matrix<CM><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
+  }
   PG_LAUNCH_CHECK();
   std::vector<double> bnorm(k), rn(k), tgt(k);
   std::vector<int> wnt(k);
@@ -1162,7 +1226,9 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
-    PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, pm, first ? 1 : 0, write_pm, part),
+    if (bj) PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, r64b)));
+    PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, pm, first ? 1 : 0,
+                                                             write_pm, part),
                    k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
@@ -1176,7 +1242,11 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     }
     PG_LAUNCH_CHECK();
     launch_iter += steps;
-    PG_KSWITCH(k, (k_cg_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    if (bj) {
+      PG_KSWITCH(k, (k_bj_apply_t_add<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, y, x, IdD2())));
+    } else {
+      PG_KSWITCH(k, (k_cg_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    }
     std::vector<int> hits(k);
     std::vector<int> hbrk(k);
     for (int i = 0; i < k; ++i) {
@@ -1665,7 +1735,7 @@ __global__ void k_mf_resid(const int64_t* __restrict__ rowptr, const int32_t* __
   }
 }
 
-size_t df_layout(const Plan& P, size_t* off /* 18 */, bool mf = false) {
+size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf = false) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   const size_t ns = mf ? (size_t)P.n * P.k : (size_t)P.n;   // scaling entries: per column with several frequencies
@@ -1687,6 +1757,8 @@ size_t df_layout(const Plan& P, size_t* off /* 18 */, bool mf = false) {
   put(15, mf ? sizeof(float4) * ns : 0);          // S (double-float)
   put(16, sizeof(double) * P.k);                  // column frequency scales
   put(17, sizeof(float) * 2 * P.k);               // the same as (hi, lo)
+  put(18, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);     // block-Jacobi factors
+  put(19, P.bj.p ? sizeof(double2) * P.n * P.k : 0);         // S r64
   return o;
 }
 
@@ -1773,18 +1845,33 @@ int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
   return best;
 }
 
+struct ToDF {
+  __device__ float4 operator()(double2 v) const { return cdf_from(v); }
+};
+
+__global__ void k_wd_to_f32(const double* wd, int64_t n, float* wdf) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    wdf[r] = (float)wd[r];
+}
+struct DfToD2 {
+  __device__ double2 operator()(float4 v) const { return cdf_to(v); }
+};
+
 constexpr int kGraphIters = 16;   // iterations per captured CUDA graph
 
 int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
                 const double* col_scale = nullptr) {
   const bool mf = col_scale != nullptr;
-  size_t off[18];
+  size_t off[20];
   df_layout(P, off, mf);
   float4* ps = reinterpret_cast<float4*>(ws + off[14]);
   float4* Sdf = reinterpret_cast<float4*>(ws + off[15]);
   double* dscale = reinterpret_cast<double*>(ws + off[16]);
   float* dscale_hl = reinterpret_cast<float*>(ws + off[17]);
+  const bool bj = !mf && P.bj.p > 0;
+  double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
+  double2* r64b = reinterpret_cast<double2*>(ws + off[19]);
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);
@@ -1826,6 +1913,10 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     k_mf_df_matrix<<<pg_blocks(P.nnz, 256), 256, 0, s>>>(A, P.nnz, At);
     // the host copy of the scales must outlive the asynchronous copy
     PG_CUDA_TRY(cudaStreamSynchronize(s));
+  } else if (bj) {
+    const int st0 = bj_setup(P, rowptr, col, A, S, wd, Sblk, At, ToDF(), dstatus, s);
+    if (st0) return st0;
+    k_wd_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(wd, P.n, wdf);
   } else {
     k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
     k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
@@ -1955,7 +2046,8 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     if (mf) {
       PG_KSWITCH(k, (k_df_start<K, true><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part, ps)));
     } else {
-      PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part)));
+      if (bj) PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, r64b)));
+      PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, first ? 1 : 0, part)));
     }
     PG_KSWITCH(k, (k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
     if (first && !mf) {
@@ -1996,6 +2088,8 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     for (; done < steps; ++done) one_iteration(s);    PG_LAUNCH_CHECK();
     if (mf) {
       PG_KSWITCH(k, (k_df_xupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
+    } else if (bj) {
+      PG_KSWITCH(k, (k_bj_apply_t_add<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, y, x, DfToD2())));
     } else {
       PG_KSWITCH(k, (k_df_xupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
     }
@@ -2129,13 +2223,16 @@ extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
 static Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
   int nb = pick_blocks(n, nrhs);
   if (nb < 152 * 16) nb = 152 * 16;  // partials also hold the SpMV's per-block sums
-  return Plan{n, nnz, nrhs, 1, o->precision, nb, o->precision == 1 ? sizeof(float2) : sizeof(double2)};
+  Plan P{n, nnz, nrhs, 1, o->precision, nb, o->precision == 1 ? sizeof(float2) : sizeof(double2), BjInfo{}};
+  P.bj = BjInfo{o->block_edges, o->block_faces, o->block_volumes, o->block_p, n};
+  if (o->block_p < 1 || o->block_p > 6) P.bj.p = 0;
+  return P;
 }
 
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = cg_plan(n, nnz, nrhs, opts);
-  size_t off[18];
+  size_t off[20];
   return (opts->precision == 2 ? df_layout(P, off) : cg_layout(P, off)) + 256;
 }
 
@@ -2146,6 +2243,16 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
       opts->precision < 0 || opts->precision > 2) {
     pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1/2)");
     return PG_ERR_ARG;
+  }
+  if (opts->block_p > 0) {
+    const int64_t pp = opts->block_p;
+    const int64_t nb_dofs = opts->block_edges * pp + opts->block_faces * pp * (pp - 1) +
+                            opts->block_volumes * (pp * (pp - 1) * (pp - 2) / 2);
+    if (opts->block_p > 6 || opts->block_edges < 0 || opts->block_faces < 0 || opts->block_volumes < 0 ||
+        nb_dofs != n) {
+      pg_set_error("pg_cocg: block-Jacobi entity counts do not match n");
+      return PG_ERR_ARG;
+    }
   }
   const size_t need = pg_cocg_workspace_bytes(n, nnz, nrhs, opts);
   if (!workspace || workspace_bytes < need) {
@@ -2169,7 +2276,7 @@ extern "C" size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int 
   pg_cocg_default_opts(&o);
   o.precision = 2;
   Plan P = cg_plan(n, nnz, nrhs, &o);
-  size_t off[18];
+  size_t off[20];
   return df_layout(P, off, true) + 256;
 }
 

@@ -117,3 +117,39 @@ def config1(n=32):
 def config2_sources():
     """64 x-directed HEDs at z = 50 m, x evenly spaced in [-1600, 1600]."""
     return [_hed(x=float(x)) for x in np.linspace(-1600.0, 1600.0, 64)]
+
+
+def config2(n=24):
+    """Batched CSEM, p=2, n^3 cubes over [-1000, 1000]^3: two-layer model
+    (3.3 S/m above z=0, 1.0 S/m below); 64 x-HEDs at z = 50 m (config2_sources)
+    at 0.25, 0.5, 1 and 2 Hz; the receivers of config0 (20 on z=0)."""
+    m = csem_two_layer(n, 2, block=False)
+    m.name = f"csem_p2_{n}cubed_batched"
+    m.frequencies = [0.25, 0.5, 1.0, 2.0]
+    m.sources = config2_sources()
+    return m
+
+
+def config4(n=40, seed=5):
+    """MT, p=3, n^3 cubes over [-5000, 5000]^2 x [-5000, 2000] m: air 1e-8 S/m
+    above z=0, 0.1 S/m for -1000 <= z <= 0, 0.01 S/m below, and three
+    ellipsoids (centres and semi-axes 200-800 m, conductivity log-uniform in
+    [0.001, 1] S/m, seeded); 2 polarisations at 0.1 and 1 Hz; 20 x 20
+    receivers on the surface."""
+    lo, hi = (-5000.0, -5000.0, -5000.0), (5000.0, 5000.0, 2000.0)
+    nodes, tets = kuhn_box(n, lo, hi)
+    cen = nodes[tets].mean(axis=1)
+    s = np.where(cen[:, 2] > 0.0, 1e-8, np.where(cen[:, 2] >= -1000.0, 0.1, 0.01))
+    rng = np.random.default_rng(seed)
+    for _ in range(3):
+        c = np.array([rng.uniform(-3000, 3000), rng.uniform(-3000, 3000), rng.uniform(-3500, -800)])
+        ax = rng.uniform(200.0, 800.0, 3)
+        inside = (((cen - c) / ax) ** 2).sum(axis=1) <= 1.0
+        s[inside] = 10.0 ** rng.uniform(-3.0, 0.0)
+    g = np.linspace(-4000.0, 4000.0, 20)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    rx = np.stack([X.ravel(), Y.ravel(), np.full(400, -1.0)], axis=1)
+    m = Model(f"mt_p3_{n}cubed", nodes, tets, np.stack([s, s], axis=1), 3, None, rx)
+    m.frequencies = [0.1, 1.0]
+    m.polarizations = ["x", "y"]
+    return m
