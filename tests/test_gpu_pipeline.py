@@ -235,3 +235,23 @@ def test_source_outside_mesh_raises():
     m = _mesh(mdl.nodes, mdl.tets, 1)
     with pytest.raises(_lib.PetgemError):
         m.source_vector(dict(mdl.source, position=[5000.0, 0.0, 0.0]))
+
+
+@pytest.mark.parametrize("p", [4, 5, 6])
+def test_assembly_high_order_vs_oracle(p):
+    """p = 4..6 (petgem's run.nord range): pattern, FP64 and double-float
+    values against the oracle on a small jittered Kuhn mesh."""
+    from petgem_gb300 import synthetic
+    nodes, tets = synthetic.kuhn_box(2)
+    nodes = synthetic.jitter_interior(nodes, 2, 0.15, 0, (-1000.0,) * 3, (1000.0,) * 3)
+    rng = np.random.default_rng(p)
+    s = 10.0 ** rng.uniform(-2, 0.5, len(tets))
+    sigma = np.stack([s, s * rng.uniform(0.3, 1.0, len(tets))], 1)
+    m = _mesh(nodes, tets, p)
+    Ao = _oracle_A(nodes, tets, sigma, p, 1.5)
+    for ar in ("fp64", "df64"):
+        v = m.assemble(sigma, 1.5, arithmetic=ar)
+        A = _csr(m, v)
+        assert np.array_equal(A.indptr, Ao.indptr) and np.array_equal(A.indices, Ao.indices)
+        assert rel_norm(A.data, Ao.data) < ELEM_TOL
+        assert torch.equal(v, m.assemble(sigma, 1.5, arithmetic=ar, records=False))
