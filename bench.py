@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--assembly", default="df64", choices=["df64", "fp64"],
                     help="arithmetic of the fused assembly (df64: double-float on the FP32 pipes)")
+    ap.add_argument("--config", type=int, default=1, choices=[1, 4],
+                    help="1: the metric's workload (default); 4: the MT configuration (p=3, 40^3): assembly and "
+                         "MT right-hand side timing only")
     ap.add_argument("--no-records", action="store_true",
                     help="assemble from the item list instead of the per-mesh assembly records")
     ap.add_argument("--solve-iters", type=int, default=0,
@@ -582,8 +585,67 @@ def run_reference(args, rank):
             "e2e": {"value": round(v, 6), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_config4(args):
+    """p = 3 MT configuration: 40^3 cubes (384,000 tets, 7.2 M DOFs, 611 M
+    stored entries): mesh setup, assembly (double-float and FP64) and the MT
+    right-hand side of both polarisations.  Its solve (air at 1e-8 S/m, no
+    PEC) is beyond a Jacobi-preconditioned Krylov method and is not timed."""
+    import torch
+    from petgem_gb300 import synthetic
+    from petgem_gb300.engine import DeviceMesh
+    n = args.n if args.n != 32 else 40
+    model = synthetic.config4(n)
+    t0 = time.time()
+    mesh = DeviceMesh(model.nodes, model.tets, 3)
+    mesh.records()
+    mesh.tables_entry_major("df64")
+    torch.cuda.synchronize()
+    setup_ms = (time.time() - t0) * 1e3
+    sigma = mesh.sigma_tensor(model.sigma)
+    out = {}
+    for ar in ("df64", "fp64"):
+        coef = torch.empty((mesh.T, 12, 2) if ar == "df64" else (mesh.T, 12),
+                           dtype=torch.float32 if ar == "df64" else torch.float64, device="cuda")
+        vals = torch.empty(mesh.nnz, dtype=torch.complex128, device="cuda")
+
+        def step():
+            mesh.element_coefficients(sigma, 1.0, out=coef, check=False, arithmetic=ar)
+            mesh.assemble(sigma, 1.0, out=vals, coef=coef, arithmetic=ar)
+        for _ in range(max(args.warmup, 1)):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, min(args.steps, 20))
+        e0.record()
+        for _ in range(steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[ar] = {"ms_per_step": round(ms, 3), "Melem_per_s": round(mesh.T / ms / 1e3, 2)}
+        del coef, vals
+    mesh.mt_rhs(model.sigma, 1.0, ("x", "y"))         # boundary setup + first use
+    torch.cuda.synchronize()
+    t = time.time()
+    mesh.mt_rhs(model.sigma, 1.0, ("x", "y"))
+    torch.cuda.synchronize()
+    out["mt_rhs_two_polarizations_ms"] = round((time.time() - t) * 1e3, 1)
+    return {"metric": "p=3 Melem/s assembled (MT configuration)", "value": out["df64"]["Melem_per_s"],
+            "unit": "Melem/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "df64 (f32 pairs) -> f64", "data": "synthetic",
+            "config": {"workload": f"mt_p3_{n}cubed (box [-5000,5000]^2 x [-5000,2000] m, air / 2 layers / "
+                                   f"3 ellipsoids)", "tets": mesh.T, "dofs": mesh.N, "nnz": mesh.nnz,
+                       "setup_ms": round(setup_ms, 1), "orientation_tuples": mesh.n_tuples,
+                       "device_memory_gb": round(torch.cuda.max_memory_allocated() / 1e9, 1)},
+            "detail": out}
+
+
 def main():
     args = parse()
+    if args.config == 4:
+        if int(os.environ.get("RANK", 0)) == 0:
+            print(json.dumps(run_config4(args)), flush=True)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
