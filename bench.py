@@ -232,6 +232,20 @@ def read_traffic(name):
     return None
 
 
+def replica_throughput(ms_local, steps, units_per_rank, world, dist=None, device="cpu"):
+    """Replicas (one mesh per rank, no data-path collective): the slowest
+    rank's time sets the step time; value = all ranks' elements / that time,
+    in Melem/s.  Returns (ms per step, value)."""
+    import torch
+    ms_max = float(ms_local)
+    if dist is not None and world > 1:
+        tt = torch.tensor([ms_max], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    ms_per_step = ms_max / steps
+    return ms_per_step, world * units_per_rank / (ms_per_step * 1e-3) / 1e6
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     from petgem_gb300 import _lib, synthetic
@@ -306,14 +320,7 @@ def run_gpu(args, rank, world, local_rank):
         e1.record()
         barrier()
         clk.mark_end()
-    ms = e0.elapsed_time(e1)
-    ms_max = ms
-    if dist is not None:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
-    ms_per_step = ms_max / args.steps
-    value = world * T / (ms_per_step * 1e-3) / 1e6
+    ms_per_step, value = replica_throughput(e0.elapsed_time(e1), args.steps, T, world, dist, "cuda")
 
     # dominant kernel: fused assembly, timed alone on the launching stream
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
