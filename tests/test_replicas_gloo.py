@@ -27,7 +27,7 @@ def test_replica_throughput_two_ranks():
     s.bind(("127.0.0.1", 0))
     port = s.getsockname()[1]
     s.close()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
     for r in (0, 1):
