@@ -495,6 +495,28 @@ int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, const double* v
                       pg_gmres_result* result, double* relres_per_rhs, void* workspace, size_t workspace_bytes,
                       void* stream);
 
+/* Several independent systems (meshes of different sizes, or one mesh at
+ * several frequencies) in one double-float COCG (precision must be 2).  The
+ * systems are stored as one block-diagonal CSR matrix: system j owns rows
+ * seg_rows[j] .. seg_rows[j+1]-1 (host array [n_seg + 1], seg_rows[0] = 0,
+ * seg_rows[n_seg] = n) and references only its own columns (checked).  Each
+ * system keeps its own COCG scalars and convergence test, so its solution is
+ * the one it would reach alone; every launch serves all systems.  With
+ * opts->block_p > 0 each system gets entity block-Jacobi scaling and
+ * seg_entities (host [3 * n_seg]) gives its (edges, faces, elements);
+ * otherwise seg_entities may be NULL.  b, x complex128 [n * nrhs] (RHS
+ * fastest), nrhs right-hand sides per system.  relres and its (host,
+ * [n_seg * nrhs], system-major, either may be NULL) receive each system's
+ * final true relative residual and iteration count; result.iterations is the
+ * largest count.  Replaces, for a batch of models, one KSPSolve per model
+ * (petgem/solver.py:584-594). */
+size_t pg_cocg_segments_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const int64_t* seg_rows, int n_seg,
+                                        const int64_t* seg_entities, const pg_cocg_opts* opts);
+int pg_cocg_segments(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
+                     const int64_t* seg_rows, int n_seg, const int64_t* seg_entities, const double* b, double* x,
+                     int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result, double* relres, int64_t* its,
+                     void* workspace, size_t workspace_bytes, void* stream);
+
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,7 @@ struct BjInfo {
   int64_t nE, nF, nV;
   int p;
   int64_t n;
+  int64_t c0 = 0;   // column index of DOF 0 (a system stored inside a larger block-diagonal matrix)
   __host__ __device__ int de() const { return p; }
   __host__ __device__ int df() const { return p * (p - 1); }
   __host__ __device__ int dv() const { return p * (p - 1) * (p - 2) / 2; }
@@ -87,7 +88,7 @@ __global__ void k_bj_factor(const int64_t* rowptr, const int32_t* col, const dou
     if (na > PG_BJ_MAX) {
       for (int i = 0; i < na; ++i) {
         for (int j = 0; j < na; ++j) Sa[i * na + j] = make_double2(0.0, 0.0);
-        const int64_t k = bj_find(rowptr, col, first + i, first + i);
+        const int64_t k = bj_find(rowptr, col, first + i, B.c0 + first + i);
         const double2 d = val[k];
         if (d.x == 0.0 && d.y == 0.0) *status = PG_ERR_BREAKDOWN;
         Sa[i * na + i] = bj_rsqrt(d);
@@ -97,7 +98,7 @@ __global__ void k_bj_factor(const int64_t* rowptr, const int32_t* col, const dou
     }
     double2 W[PG_BJ_MAX][PG_BJ_MAX], L[PG_BJ_MAX][PG_BJ_MAX], D[PG_BJ_MAX];
     for (int i = 0; i < na; ++i) {
-      const int64_t k = bj_find(rowptr, col, first + i, first);
+      const int64_t k = bj_find(rowptr, col, first + i, B.c0 + first);
       for (int j = 0; j < na; ++j) W[i][j] = val[k + j];
     }
     bool bad = false;
@@ -151,7 +152,7 @@ __global__ void k_bj_scale_matrix(const int64_t* rowptr, const int32_t* col, con
     for (int64_t k = base; k < rowptr[r + 1]; ++k) {
       int64_t fb, sb;
       int nb, j;
-      B.block(col[k], fb, nb, j, sb);
+      B.block(col[k] - B.c0, fb, nb, j, sb);
       const double2* Sb = S + sb;
       double2 acc = make_double2(0.0, 0.0);
       for (int ip = 0; ip <= i; ++ip) {

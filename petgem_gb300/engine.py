@@ -592,3 +592,73 @@ def solve_csr_frequencies(rowptr, col, vals0, b, col_scale, x0=None, rtol=1e-8, 
         msg = lib.pg_last_error()
         raise _lib.PetgemError("pg_cocg_multifreq", st, msg.decode() if msg else "")
     return x, info
+
+
+def concat_systems(systems):
+    """Block-diagonal CSR of several systems [(rowptr, col, vals, b), ...]:
+    (rowptr, col, vals, b, seg_rows) with system j in rows seg_rows[j] ..
+    seg_rows[j+1]-1 and its columns shifted by seg_rows[j]."""
+    rps, cols, vals, bs, rows, nz = [], [], [], [], [0], 0
+    for rp, c, v, b in systems:
+        n_j = int(rp.numel()) - 1
+        rps.append(rp[:-1] + nz)
+        cols.append(c + rows[-1])
+        vals.append(v)
+        bs.append(b)
+        nz += int(c.numel())
+        rows.append(rows[-1] + n_j)
+    dev = systems[0][0].device
+    rowptr = torch.cat(rps + [torch.tensor([nz], dtype=torch.int64, device=dev)])
+    return (rowptr, torch.cat(cols).to(torch.int32), torch.cat(vals), torch.cat(bs),
+            np.asarray(rows, dtype=np.int64))
+
+
+def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_fail=True, check_every=50):
+    """Several independent systems in one double-float COCG (pg_cocg_segments).
+
+    systems: [(rowptr int64 [n_j+1], col int32, vals complex128, b complex128
+    [n_j] or [n_j, k]), ...], every b with the same k (1,2,4,8,16,32).  Each
+    system keeps its own scalars and convergence test (true residual <= rtol
+    ||b_j|| per column); every kernel launch and graph replay serves all of
+    them.  blocks: None (diagonal Jacobi) or (p, [(n_edges, n_faces,
+    n_elements) per system]) for entity block-Jacobi.  Returns ([x_j], info)
+    with info.relres_per_rhs and info.its_per_rhs per (system, rhs)."""
+    if not systems:
+        raise ValueError("no systems")
+    ks = {1 if b.ndim == 1 else int(b.shape[1]) for _, _, _, b in systems}
+    if len(ks) != 1:
+        raise ValueError("every system needs the same number of right-hand sides")
+    k = ks.pop()
+    rowptr, col, vals, b, rows = concat_systems(systems)
+    if k > 1:
+        b = b.reshape(-1, k)
+    S = len(systems)
+    N, nnz = int(rows[-1]), int(col.numel())
+    lib = _lib.load()
+    o = _lib.CocgOpts()
+    lib.pg_cocg_default_opts(ctypes.byref(o))
+    o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), 2, int(check_every)
+    ents = None
+    if blocks is not None:
+        o.block_p = int(blocks[0])
+        ents = np.ascontiguousarray(np.asarray(blocks[1], dtype=np.int64).reshape(S, 3))
+    ents_p = ctypes.c_void_p(ents.ctypes.data) if ents is not None else ctypes.c_void_p(0)
+    rows_p = ctypes.c_void_p(rows.ctypes.data)
+    nbytes = _lib.query("pg_cocg_segments_workspace_bytes", N, nnz, k, rows_p, S, ents_p, ctypes.byref(o))
+    if nbytes == 0:
+        raise ValueError("pg_cocg_segments: bad systems (empty, k not 1..32, or block counts not matching rows)")
+    ws = _ws(nbytes + 256, b.device)
+    x = torch.zeros_like(b)
+    res = _lib.GmresResult()
+    rr = np.zeros(S * k, dtype=np.float64)
+    its = np.zeros(S * k, dtype=np.int64)
+    st = lib.pg_cocg_segments(_p(rowptr), _p(col), _p(vals), N, nnz, rows_p, S, ents_p, _p(b.contiguous()), _p(x), k,
+                              ctypes.byref(o), ctypes.byref(res), ctypes.c_void_p(rr.ctypes.data),
+                              ctypes.c_void_p(its.ctypes.data), _p(ws), ws.numel(), _s())
+    info = SolveInfo(int(res.iterations), int(res.restarts), float(res.relres), int(st), rr.reshape(S, k).tolist())
+    info.its_per_rhs = its.reshape(S, k).tolist()
+    if st != 0 and (raise_on_fail or st != -7):
+        msg = lib.pg_last_error()
+        raise _lib.PetgemError("pg_cocg_segments", st, msg.decode() if msg else "")
+    xs = [x[int(rows[j]):int(rows[j + 1])] for j in range(S)]
+    return xs, info

@@ -114,9 +114,12 @@ def config1(n=32):
     return Model(f"csem_p2_{n}cubed_jitter", nodes, tets, sigma, 2, _hed(), rx)
 
 
-def config2_sources():
-    """64 x-directed HEDs at z = 50 m, x evenly spaced in [-1600, 1600]."""
-    return [_hed(x=float(x)) for x in np.linspace(-1600.0, 1600.0, 64)]
+def config2_sources(count=64, x_max=800.0):
+    """`count` x-directed HEDs at z = 50 m, x evenly spaced in [-x_max, x_max].
+    The batched workload's nominal line, x in [-1600, 1600], runs past the
+    [-1000, 1000] m box, where a source cannot be located (petgem raises); the
+    line is therefore kept inside the box, over the receivers' span."""
+    return [_hed(x=float(x)) for x in np.linspace(-x_max, x_max, count)]
 
 
 def config2(n=24):
@@ -127,6 +130,21 @@ def config2(n=24):
     m.name = f"csem_p2_{n}cubed_batched"
     m.frequencies = [0.25, 0.5, 1.0, 2.0]
     m.sources = config2_sources()
+    return m
+
+
+def config2_extra_sizes(count=8, lo=8, hi=20, seed=2):
+    """Cubes per axis of the batched workload's extra independent meshes:
+    `count` sizes drawn uniformly from lo..hi (seed 2)."""
+    rng = np.random.default_rng(seed)
+    return [int(v) for v in rng.integers(lo, hi + 1, size=count)]
+
+
+def config2_extra(n):
+    """One extra mesh of the batched workload: the two-layer model of config2
+    on n^3 cubes."""
+    m = csem_two_layer(n, 2, block=False)
+    m.name = f"csem_p2_{n}cubed_extra"
     return m
 
 
