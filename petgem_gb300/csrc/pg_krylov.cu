@@ -2268,7 +2268,7 @@ __device__ void seg_beta_final(const double2* prho, const double2* pw, const Seg
 
 // q = At p for every system (G lanes per (row, rhs) item; G > 1 only for one
 // RHS), partial mu = p^T q; last block: alpha of every system
-template <int K, int G>
+template <int K, int G, int U>
 __global__ void __launch_bounds__(kThreads) k_sg_spmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                       const float4* __restrict__ val, Seg g,
                                                       const float4* __restrict__ pv, float4* __restrict__ q,
@@ -2290,9 +2290,24 @@ __global__ void __launch_bounds__(kThreads) k_sg_spmm(const int64_t* __restrict_
       const int64_t r = sp.r0 + it / K;
       const int rhs = (int)(it % K);
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (valid)
-        for (int64_t k = rowptr[r] + lane; k < rowptr[r + 1]; k += G)
-          cdf_mac(acc, val[k], pv[(int64_t)col[k] * K + rhs]);
+      if (valid) {
+        const int64_t e = rowptr[r + 1];
+        int64_t kk = rowptr[r] + lane;
+        if (U == 2) {
+          // two independent accumulators: two gathers in flight per lane
+          float4 acc1 = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (; kk + G < e; kk += 2 * G) {
+            const int32_t c0 = col[kk], c1 = col[kk + G];
+            const float4 v0 = val[kk], v1 = val[kk + G];
+            cdf_mac(acc, v0, pv[(int64_t)c0 * K + rhs]);
+            cdf_mac(acc1, v1, pv[(int64_t)c1 * K + rhs]);
+          }
+          if (kk < e) cdf_mac(acc, val[kk], pv[(int64_t)col[kk] * K + rhs]);
+          cdf_add(acc, acc1);
+        } else {
+          for (; kk < e; kk += G) cdf_mac(acc, val[kk], pv[(int64_t)col[kk] * K + rhs]);
+        }
+      }
 #pragma unroll
       for (int off = G / 2; off > 0; off >>= 1) cdf_add(acc, shfl_xor4(acc, off));
       if (valid && lane == 0) {
@@ -2476,6 +2491,39 @@ std::vector<int> seg_blocks(const int64_t* rows, int S, int k) {
   return blk;
 }
 
+// the same total of blocks re-split over the systems still iterating: a
+// converged system keeps one (idle) block, the others share the rest in
+// proportion to their rows; blocks no system can use go to the largest
+// active system, where they find no rows
+void seg_rebalance(const int64_t* rows, int S, int k, const std::vector<char>& active, int total,
+                   std::vector<int>& blk) {
+  blk.assign(S + 1, 0);
+  int64_t n_act = 0;
+  int big = -1;
+  for (int j = 0; j < S; ++j) {
+    const int64_t nj = rows[j + 1] - rows[j];
+    if (active[j]) {
+      n_act += nj;
+      if (big < 0 || nj > rows[big + 1] - rows[big]) big = j;
+    }
+  }
+  // every system holds one block; the total - S others go to the active
+  // systems (total >= S: the first map gives each system at least one)
+  const int spare = total - S;
+  std::vector<int> b(S, 1);
+  int used = S;
+  for (int j = 0; j < S; ++j) {
+    if (!active[j]) continue;
+    const int64_t nj = rows[j + 1] - rows[j];
+    int64_t v = n_act > 0 ? (int64_t)((double)spare * (double)nj / (double)n_act) : 0;
+    v = std::min<int64_t>(v, std::max<int64_t>((nj * k + kThreads - 1) / kThreads - 1, 0));
+    b[j] += (int)v;
+    used += (int)v;
+  }
+  if (used < total) b[big >= 0 ? big : S - 1] += total - used;
+  for (int j = 0; j < S; ++j) blk[j + 1] = blk[j] + b[j];
+}
+
 struct SegPlan {
   int64_t n, nnz;
   int k, S, nb;
@@ -2566,7 +2614,8 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   double2* r64b = reinterpret_cast<double2*>(ws + off[17]);
   const int k = P.k, G = P.nb;
   const bool bj = P.p > 0;
-  const std::vector<int> hblk = seg_blocks(hrows, P.S, k);
+  std::vector<int> hblk = seg_blocks(hrows, P.S, k), cur_blk;
+  std::vector<char> sys_active(P.S, 1);
   PG_CUDA_TRY(cudaMemcpyAsync(drows, hrows, sizeof(int64_t) * (P.S + 1), cudaMemcpyHostToDevice, s));
   PG_CUDA_TRY(cudaMemcpyAsync(dblk, hblk.data(), sizeof(int) * (P.S + 1), cudaMemcpyHostToDevice, s));
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
@@ -2630,9 +2679,9 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   const double delta = 1e-3;
   auto one_iteration = [&](cudaStream_t ss) {
     if (k == 1)
-      k_sg_spmm<1, 4><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl);
+      k_sg_spmm<1, 4, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl);
     else
-      PG_KSWITCH(k, (k_sg_spmm<K, 1><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
+      PG_KSWITCH(k, (k_sg_spmm<K, 1, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
     PG_KSWITCH(k, (k_sg_update<K><<<G, kThreads, 0, ss>>>(y, r, pv, q, wdf, g, st, part, part2, ctl, delta),
                    k_sg_pupdate<K><<<G, kThreads, 0, ss>>>(pv, r, g, st, ctl)));
   };
@@ -2715,6 +2764,16 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
     }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * pairs, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * pairs, cudaMemcpyHostToDevice, s));
+    // systems already converged keep one idle block; the others take the rest
+    for (int j = 0; j < P.S; ++j) {
+      sys_active[j] = 0;
+      for (int i = 0; i < k; ++i) sys_active[j] |= (char)wnt[j * k + i];
+    }
+    seg_rebalance(hrows, P.S, k, sys_active, G, cur_blk);
+    if (cur_blk != hblk) {
+      hblk = cur_blk;
+      PG_CUDA_TRY(cudaMemcpyAsync(dblk, hblk.data(), sizeof(int) * (P.S + 1), cudaMemcpyHostToDevice, s));
+    }
     if (bj)
       for (int j = 0; j < P.S; ++j) {
         const BjInfo& B = P.bj[j];
