@@ -1762,6 +1762,150 @@ size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf = false) {
   return o;
 }
 
+// ---- entity-group products --------------------------------------------------
+// DOFs are numbered entity by entity with p, p(p-1) and p(p-1)(p-2)/2 DOFs per
+// edge, face and volume: all multiples of p, and every entity starts at a
+// multiple of p.  So rows [R i, R i + R) with R = p belong to one entity and
+// share their column list (entity-pair pattern; checked column by column
+// before use).  The group product loads each column index and p value once
+// and uses them for R rows: fewer loads per stored entry and R independent
+// accumulations per lane.
+
+// 0 if rows of every aligned group of R have the first row's column list
+__global__ void k_group_check(const int64_t* rowptr, const int32_t* col, int64_t n, int R, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = r - r % R;
+    if (f == r) continue;
+    const int64_t o = rowptr[r], of = rowptr[f], len = rowptr[r + 1] - o;
+    if (len != rowptr[f + 1] - of) {
+      *status = 1;
+      continue;
+    }
+    for (int64_t k = 0; k < len; ++k)
+      if (col[o + k] != col[of + k]) {
+        *status = 1;
+        break;
+      }
+  }
+}
+
+// one RHS: G lanes per group of R rows, U column steps per loop pass
+template <int R, int G, int U = 1>
+__global__ void __launch_bounds__(kThreads) k_df_spmv_grp(const int64_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col,
+                                                          const float4* __restrict__ val, int64_t n,
+                                                          const float4* __restrict__ pv, float4* __restrict__ q,
+                                                          double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t ngroups = n / R;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t gw = warp_base; gw < ngroups; gw += groups) {
+    const int64_t gi = gw + (gid - warp_base);
+    const bool valid = gi < ngroups;
+    float4 acc[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      const int64_t r0 = gi * R;
+      int64_t off[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+      const int64_t len = rowptr[r0 + 1] - off[0];
+      int64_t k = lane;
+      if (U == 2) {
+        // a second set of accumulators: two column steps in flight per lane
+        float4 acc1[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) acc1[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (; k + G < len; k += 2 * G) {
+          const int32_t c0 = col[off[0] + k], c1 = col[off[0] + k + G];
+          float4 v0[R], v1[R];
+#pragma unroll
+          for (int i = 0; i < R; ++i) {
+            v0[i] = val[off[i] + k];
+            v1[i] = val[off[i] + k + G];
+          }
+          const float4 x0 = pv[c0], x1 = pv[c1];
+#pragma unroll
+          for (int i = 0; i < R; ++i) {
+            cdf_mac(acc[i], v0[i], x0);
+            cdf_mac(acc1[i], v1[i], x1);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) cdf_add(acc[i], acc1[i]);
+      }
+      for (; k < len; k += G) {
+        const float4 x = pv[col[off[0] + k]];
+#pragma unroll
+        for (int i = 0; i < R; ++i) cdf_mac(acc[i], val[off[i] + k], x);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) cdf_add(acc[i], shfl_xor4(acc[i], o));
+    if (valid && lane == 0) {
+      const int64_t r0 = gi * R;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const float4 a = df_norm(acc[i]);
+        q[r0 + i] = a;
+        cdf_mac(mu, pv[r0 + i], a);
+      }
+    }
+  }
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<1>(mu, smf, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
+}
+
+// K RHS: one thread per (group of R rows, rhs)
+template <int K, int R>
+__global__ void __launch_bounds__(kThreads) k_df_spmm_grp(const int64_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col,
+                                                          const float4* __restrict__ val, int64_t n,
+                                                          const float4* __restrict__ pv, float4* __restrict__ q,
+                                                          double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int rhs = threadIdx.x % K;
+  const int64_t items = (n / R) * K;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += stride) {
+    const int64_t r0 = (it / K) * R;
+    int64_t off[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+    const int64_t len = rowptr[r0 + 1] - off[0];
+    float4 acc[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t k = 0; k < len; ++k) {
+      const float4 x = pv[(int64_t)col[off[0] + k] * K + rhs];
+#pragma unroll
+      for (int i = 0; i < R; ++i) cdf_mac(acc[i], val[off[i] + k], x);
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float4 a = df_norm(acc[i]);
+      q[(r0 + i) * K + rhs] = a;
+      cdf_mac(mu, pv[(r0 + i) * K + rhs], a);
+    }
+  }
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<K>(mu, smf, partial + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
+}
+
 // ---- SpMV variant autotuner ------------------------------------------------
 // The double-float product's best lanes-per-row / unrolling depends on the
 // matrix (rows, stored entries per row) and the RHS count.  At the first
@@ -1771,21 +1915,39 @@ size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf = false) {
 // PG_AUTOTUNE=0 keeps the default variant.
 struct TuneEntry {
   int64_t n, nnz;
-  int k, variant;
+  int k, group, variant;
 };
 std::vector<TuneEntry> g_tune;
 std::mutex g_tune_mu;
 
-int tuned_variant(int64_t n, int64_t nnz, int k) {
+int tuned_variant(int64_t n, int64_t nnz, int k, int group) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   for (const TuneEntry& t : g_tune)
-    if (t.n == n && t.nnz == nnz && t.k == k) return t.variant;
+    if (t.n == n && t.nnz == nnz && t.k == k && t.group == group) return t.variant;
   return -1;
 }
 
-void store_variant(int64_t n, int64_t nnz, int k, int v) {
+void store_variant(int64_t n, int64_t nnz, int k, int group, int v) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_tune.push_back(TuneEntry{n, nnz, k, v});
+  g_tune.push_back(TuneEntry{n, nnz, k, group, v});
+}
+
+// PG_SPMV_VARIANT=v forces a product variant when it is valid for the solve
+// (a group variant only when the rows were checked to group by R); -1 otherwise
+int forced_variant(int k, int group) {
+  const char* e = getenv("PG_SPMV_VARIANT");
+  if (!(e && e[0])) return -1;
+  const int v = atoi(e);
+  if (k == 1) {
+    if (v == 21 || v == 22 || v == 41 || v == 42 || v == 81 || v == 82) return v;
+    if (group && (v == 100 * group + 2 || v == 100 * group + 4 || v == 100 * group + 8 || v == 100 * group + 12 ||
+                  v == 100 * group + 14))
+      return v;
+  } else {
+    if (v == 1 || v == 2) return v;
+    if (group && v == 100 * group) return v;
+  }
+  return -1;
 }
 
 bool autotune_enabled() {
@@ -1793,11 +1955,24 @@ bool autotune_enabled() {
   return !(e && e[0] == '0');
 }
 
-// single RHS: variant = lanes per row G (1..8) * 10 + unroll U
+// single RHS: variant = lanes per row G (1..8) * 10 + unroll U, or
+// 100 R + 10 (U - 1) + G for the product over groups of R rows with G lanes
+// per group and unroll U;
+// several RHS: unroll 1 or 2, or 100 R for the group product
 void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
                      const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st,
                      CgCtl* ctl) {
   switch (variant) {
+    case 202: k_df_spmv_grp<2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 204: k_df_spmv_grp<2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 208: k_df_spmv_grp<2, 8><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 302: k_df_spmv_grp<3, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 304: k_df_spmv_grp<3, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 308: k_df_spmv_grp<3, 8><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 212: k_df_spmv_grp<2, 2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 214: k_df_spmv_grp<2, 4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 312: k_df_spmv_grp<3, 2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 314: k_df_spmv_grp<3, 4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 21: k_df_spmv1<2, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 22: k_df_spmv1<2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 42: k_df_spmv1<4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
@@ -1810,7 +1985,11 @@ void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowpt
 template <int K>
 void launch_df_spmm(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
                     const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st, CgCtl* ctl) {
-  if (variant == 2)
+  if (variant == 200)
+    k_df_spmm_grp<K, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else if (variant == 300)
+    k_df_spmm_grp<K, 3><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else if (variant == 2)
     k_df_spmm<K, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
   else
     k_df_spmm<K, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
@@ -1899,6 +2078,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   if (spmv_grid > nb) return PG_ERR_ARG;
 
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  int group = 0;   // rows per entity group for the group product (0: not used)
   if (mf) {
     std::vector<float> hl(2 * (size_t)k);
     for (int i = 0; i < k; ++i) {
@@ -1917,6 +2097,17 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     const int st0 = bj_setup(P, rowptr, col, A, S, wd, Sblk, At, ToDF(), dstatus, s);
     if (st0) return st0;
     k_wd_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(wd, P.n, wdf);
+    if ((P.bj.p == 2 || P.bj.p == 3) && P.n % P.bj.p == 0) {
+      // the group product needs every aligned group of p rows on one column list
+      int* gflag = reinterpret_cast<int*>(part);
+      int hg = 1;
+      PG_CUDA_TRY(cudaMemsetAsync(gflag, 0, sizeof(int), s));
+      k_group_check<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, P.n, P.bj.p, gflag);
+      PG_LAUNCH_CHECK();
+      PG_CUDA_TRY(cudaMemcpyAsync(&hg, gflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaStreamSynchronize(s));
+      group = hg == 0 ? P.bj.p : 0;
+    }
   } else {
     k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
     k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
@@ -2051,22 +2242,29 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     }
     PG_KSWITCH(k, (k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
     if (first && !mf) {
-      variant = tuned_variant(P.n, P.nnz, k);
+      variant = forced_variant(k, group);
+      if (variant < 0) variant = tuned_variant(P.n, P.nnz, k, group);
       if (variant < 0) {
         if (autotune_enabled()) {
-          if (k == 1)
-            variant = pick_fastest({41, 42, 22, 82, 21}, [&](int v) {
+          if (k == 1) {
+            std::vector<int> cands = {41, 42, 22, 82, 21};
+            if (group)
+              for (int gv : {2, 4, 8, 12, 14}) cands.push_back(100 * group + gv);
+            variant = pick_fastest(cands, [&](int v) {
               launch_df_spmv1(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl);
             }, s);
-          else
-            variant = pick_fastest({1, 2}, [&](int v) {
+          } else {
+            std::vector<int> cands = {1, 2};
+            if (group) cands.push_back(100 * group);
+            variant = pick_fastest(cands, [&](int v) {
               PG_KSWITCH(k, (launch_df_spmm<K>(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl)));
             }, s);
+          }
           PG_LAUNCH_CHECK();
         } else {
           variant = k == 1 ? 41 : 1;
         }
-        store_variant(P.n, P.nnz, k, variant);
+        store_variant(P.n, P.nnz, k, group, variant);
       }
       if (monitor) fprintf(stderr, "pg_cocg(df64): SpMV variant %d for n=%lld nnz=%lld k=%d\n", variant,
                            (long long)P.n, (long long)P.nnz, k);

@@ -26,6 +26,7 @@ def _system(n, seed, k=1, p=2):
         m.source_rhs(s, m.locate_source(s), bj)
         b[:, j] = bj
     m.pec_rhs(b)
+    assert bool((torch.linalg.norm(b, dim=0) > 0).all())
     return m, A, (b[:, 0].contiguous() if k == 1 else b)
 
 
