@@ -1196,8 +1196,8 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
                    k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
     PG_LAUNCH_CHECK();
     PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
-    Ctl hctl;
-    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    CgCtl hctl;
+    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, s));
     PG_CUDA_TRY(cudaStreamSynchronize(s));
     if (!first && hctl.nonfinite) {
       pg_set_error("pg_cocg: non-finite residual");
@@ -1866,6 +1866,75 @@ __global__ void __launch_bounds__(kThreads) k_df_spmv_grp(const int64_t* __restr
   if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
 }
 
+// one RHS, G lanes per group of R rows; each lane issues the column, value
+// and p loads of B column steps back to back before using them, so a warp
+// keeps B times more bytes in flight than one step at a time
+template <int R, int G, int B>
+__global__ void __launch_bounds__(kThreads) k_df_spmv_grpb(const int64_t* __restrict__ rowptr,
+                                                           const int32_t* __restrict__ col,
+                                                           const float4* __restrict__ val, int64_t n,
+                                                           const float4* __restrict__ pv, float4* __restrict__ q,
+                                                           double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t ngroups = n / R;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t gw = warp_base; gw < ngroups; gw += groups) {
+    const int64_t gi = gw + (gid - warp_base);
+    const bool valid = gi < ngroups;
+    float4 acc[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      const int64_t r0 = gi * R;
+      int64_t off[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+      const int len = (int)(rowptr[r0 + 1] - off[0]);
+      for (int k0 = lane; k0 < len; k0 += G * B) {
+        int c[B];
+        float4 v[B][R], x[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+          const int k = k0 + j * G;
+          c[j] = k < len ? col[off[0] + k] : 0;
+#pragma unroll
+          for (int i = 0; i < R; ++i) v[j][i] = k < len ? val[off[i] + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) x[j] = k0 + j * G < len ? pv[c[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < B; ++j)
+          if (k0 + j * G < len) {
+#pragma unroll
+            for (int i = 0; i < R; ++i) cdf_mac(acc[i], v[j][i], x[j]);
+          }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) cdf_add(acc[i], shfl_xor4(acc[i], o));
+    if (valid && lane == 0) {
+      const int64_t r0 = gi * R;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const float4 a = df_norm(acc[i]);
+        q[r0 + i] = a;
+        cdf_mac(mu, pv[r0 + i], a);
+      }
+    }
+  }
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<1>(mu, smf, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
+}
+
 // K RHS: one thread per (group of R rows, rhs)
 template <int K, int R>
 __global__ void __launch_bounds__(kThreads) k_df_spmm_grp(const int64_t* __restrict__ rowptr,
@@ -1940,9 +2009,8 @@ int forced_variant(int k, int group) {
   const int v = atoi(e);
   if (k == 1) {
     if (v == 21 || v == 22 || v == 41 || v == 42 || v == 81 || v == 82) return v;
-    if (group && (v == 100 * group + 2 || v == 100 * group + 4 || v == 100 * group + 8 || v == 100 * group + 12 ||
-                  v == 100 * group + 14))
-      return v;
+    const int gv = v - 100 * group;
+    if (group && (gv == 2 || gv == 4 || gv == 8 || gv == 12 || gv == 14 || gv == 32 || gv == 34)) return v;
   } else {
     if (v == 1 || v == 2) return v;
     if (group && v == 100 * group) return v;
@@ -1957,7 +2025,8 @@ bool autotune_enabled() {
 
 // single RHS: variant = lanes per row G (1..8) * 10 + unroll U, or
 // 100 R + 10 (U - 1) + G for the product over groups of R rows with G lanes
-// per group and unroll U;
+// per group and unroll U, 100 R + 30 + G for the group product with 4 column
+// steps batched;
 // several RHS: unroll 1 or 2, or 100 R for the group product
 void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
                      const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st,
@@ -1970,6 +2039,10 @@ void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowpt
     case 304: k_df_spmv_grp<3, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 308: k_df_spmv_grp<3, 8><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 212: k_df_spmv_grp<2, 2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 232: k_df_spmv_grpb<2, 2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 234: k_df_spmv_grpb<2, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 332: k_df_spmv_grpb<3, 2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 334: k_df_spmv_grpb<3, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 214: k_df_spmv_grp<2, 4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 312: k_df_spmv_grp<3, 2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 314: k_df_spmv_grp<3, 4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
@@ -2078,6 +2151,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   if (spmv_grid > nb) return PG_ERR_ARG;
 
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  PG_CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(CgCtl), s));
   int group = 0;   // rows per entity group for the group product (0: not used)
   if (mf) {
     std::vector<float> hl(2 * (size_t)k);
@@ -2141,6 +2215,9 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   bool first = true;
   int variant = 41;
   const double delta = 1e-3;   // double-float recurrence: replace after 3 decades
+  auto launch_single = [&](int v, cudaStream_t ss) {
+    launch_df_spmv1(v, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl);
+  };
   // one iteration: product (alpha), vector update (beta), direction update;
   // no per-iteration launch arguments, so a run of them can be captured once
   // in a CUDA graph and replayed
@@ -2155,7 +2232,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       return;
     }
     if (k == 1)
-      launch_df_spmv1(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl);
+      launch_single(variant, ss);
     else
       PG_KSWITCH(k, (launch_df_spmm<K>(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl)));
     PG_KSWITCH(k, (k_df_update<K><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, 0, delta),
@@ -2204,8 +2281,8 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                    k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
     PG_LAUNCH_CHECK();
     PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
-    Ctl hctl;
-    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    CgCtl hctl;
+    PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, s));
     PG_CUDA_TRY(cudaStreamSynchronize(s));
     if (!first && hctl.nonfinite) {
       pg_set_error("pg_cocg: non-finite residual");
@@ -2249,10 +2326,8 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
           if (k == 1) {
             std::vector<int> cands = {41, 42, 22, 82, 21};
             if (group)
-              for (int gv : {2, 4, 8, 12, 14}) cands.push_back(100 * group + gv);
-            variant = pick_fastest(cands, [&](int v) {
-              launch_df_spmv1(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl);
-            }, s);
+              for (int gv : {2, 4, 8, 12, 14, 32, 34}) cands.push_back(100 * group + gv);
+            variant = pick_fastest(cands, [&](int v) { launch_single(v, s); }, s);
           } else {
             std::vector<int> cands = {1, 2};
             if (group) cands.push_back(100 * group);

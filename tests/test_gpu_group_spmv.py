@@ -1,7 +1,8 @@
 """Double-float products of the COCG: every lanes-per-row / unrolling variant
-and the entity-group product (rows [R i, R i + R) of one mesh entity share
-their columns, R = p) reach the same solution, and the monitor shows the
-forced variant ran."""
+and the entity-group products (rows [R i, R i + R) of one mesh entity share
+their columns, R = p; one column step at a time, unrolled, or 4 steps'
+loads batched) reach the same solution, and the monitor shows the forced
+variant ran."""
 import numpy as np
 import pytest
 import torch
@@ -29,8 +30,9 @@ def _system(p, k):
 
 
 @pytest.mark.parametrize("p,k,variant", [(2, 1, 202), (2, 1, 204), (2, 1, 208), (2, 1, 212), (2, 1, 214),
-                                         (2, 1, 42), (3, 1, 304), (3, 1, 314), (3, 1, 302), (2, 4, 200),
-                                         (2, 4, 2), (3, 8, 300)])
+                                         (2, 1, 232), (2, 1, 234), (2, 1, 42), (3, 1, 304), (3, 1, 314),
+                                         (3, 1, 302), (3, 1, 332), (3, 1, 334), (2, 4, 200), (2, 4, 2),
+                                         (3, 8, 300)])
 def test_df64_product_variants_agree(p, k, variant, monkeypatch, capfd):
     m, A, b = _system(p, k)
     rtol = 1e-10
