@@ -479,7 +479,7 @@ def run_solves(args, torch, mesh, model, vals, b):
         torch.cuda.synchronize()
         dt = time.time() - t
         k = 1 if rhs.ndim == 1 else rhs.shape[1]
-        return x, {"ksp": ksp, "precision": prec, "precond": precond if ksp == "cocg" else "jacobi", "nrhs": k,
+        return x, {"ksp": ksp, "precision": prec, "precond": precond, "nrhs": k,
                    "seconds": round(dt, 3),
                    "ms_per_rhs": round(dt * 1e3 / k, 2), "iterations": info.iterations,
                    "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4),

@@ -432,6 +432,15 @@ typedef struct pg_gmres_opts {
   double rtol;    /* stop when ||b - A x|| <= rtol ||b|| (true residual, FP64) */
   int precision;  /* 0: complex128 Arnoldi; 1: complex64 Arnoldi + complex128 refinement */
   int reorth;     /* 1: classical Gram-Schmidt applied twice (CGS2) */
+  /* entity block-Jacobi (block_p 1..6; 0 = diagonal Jacobi), PETSc -pc_type
+   * bjacobi with one block per edge / face / element: the matrix is
+   * pg_pattern_build's pattern for a mesh with block_edges edges, block_faces
+   * faces and block_volumes elements at order block_p; GMRES runs on A M^-1
+   * (right preconditioning, so the Arnoldi residual is the true one) with
+   * M^-1 = A_aa^-1 per entity block, from A_aa = L D L^T (blocks above 12
+   * DOFs stay diagonal). */
+  int block_p;
+  int64_t block_edges, block_faces, block_volumes;
 } pg_gmres_opts;
 
 typedef struct pg_gmres_result {

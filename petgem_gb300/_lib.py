@@ -19,7 +19,8 @@ _D = ctypes.c_double
 class GmresOpts(ctypes.Structure):
     """pg_gmres_opts (include/petgem_gb300.h)."""
     _fields_ = [("restart", ctypes.c_int), ("max_it", ctypes.c_int), ("rtol", ctypes.c_double),
-                ("precision", ctypes.c_int), ("reorth", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("reorth", ctypes.c_int), ("block_p", ctypes.c_int),
+                ("block_edges", ctypes.c_int64), ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64)]
 
 
 class GmresResult(ctypes.Structure):

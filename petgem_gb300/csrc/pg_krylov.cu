@@ -475,7 +475,7 @@ struct Plan {
   BjInfo bj;          // COCG entity block-Jacobi (bj.p == 0: diagonal Jacobi)
 };
 
-size_t ws_layout(const Plan& P, size_t* off /* 14 */) {
+size_t ws_layout(const Plan& P, size_t* off /* 16 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   put(0, P.nnz * P.csize);                                   // Ahat
@@ -492,7 +492,91 @@ size_t ws_layout(const Plan& P, size_t* off /* 14 */) {
   put(11, sizeof(double) * P.k);                             // target
   put(12, sizeof(int) * P.k);                                // want
   put(13, sizeof(int));                                      // status
+  put(14, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);    // block-Jacobi factors S
+  put(15, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);    // block inverses M^-1
   return o;
+}
+
+// rows of one entity must share their column list (entity-pair pattern);
+// checked through row lengths and first / last columns before block scaling
+__global__ void k_bj_check(const int64_t* rowptr, const int32_t* col, BjInfo B, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < B.n; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t f, so;
+    int na, loc;
+    B.block(r, f, na, loc, so);
+    const int64_t l0 = rowptr[f + 1] - rowptr[f], l = rowptr[r + 1] - rowptr[r];
+    if (l != l0 || l < 1 || col[rowptr[r]] != col[rowptr[f]] || col[rowptr[r + 1] - 1] != col[rowptr[f + 1] - 1])
+      *status = PG_ERR_ARG;
+  }
+}
+
+__global__ void k_fill_one(double2* S, int64_t n) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    S[r] = make_double2(1.0, 0.0);
+}
+
+// GMRES block-Jacobi: Minv_a = A_aa^-1 = S_a^T S_a per entity block
+// (row-major na x na, complex symmetric), from the COCG factors S_a
+__global__ void k_bj_minv(const double2* S, BjInfo B, double2* Minv) {
+  for (int64_t r0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r0 < B.n; r0 += (int64_t)gridDim.x * blockDim.x) {
+    int64_t first, soff;
+    int na, loc;
+    B.block(r0, first, na, loc, soff);
+    if (loc != 0) continue;
+    const double2* Sa = S + soff;
+    double2* Ma = Minv + soff;
+    for (int l = 0; l < na; ++l)
+      for (int j = 0; j < na; ++j) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int t = l > j ? l : j; t < na; ++t) {
+          const double2 u = bj_mul(Sa[t * na + l], Sa[t * na + j]);
+          acc.x += u.x;
+          acc.y += u.y;
+        }
+        Ma[l * na + j] = acc;
+      }
+  }
+}
+
+// out = A M^-1 row by row: the entry at column fb + j of entity b is
+// sum_l A[r, fb + l] Minv_b[l, j] (entity b's columns are contiguous in the row)
+template <typename CM>
+__global__ void k_bj_right_scale(const int64_t* rowptr, const int32_t* col, const double2* val, BjInfo B,
+                                 const double2* Minv, CM* out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < B.n; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      int64_t fb, sb;
+      int nb, j;
+      B.block(col[k] - B.c0, fb, nb, j, sb);
+      const double2* Mb = Minv + sb;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int l = 0; l < nb; ++l) {
+        const double2 t = bj_mul(val[k - j + l], Mb[l * nb + j]);
+        acc.x += t.x;
+        acc.y += t.y;
+      }
+      out[k] = cfrom<CM>(acc);
+    }
+  }
+}
+
+// x[:, c] += Minv t[:, c] (full entity blocks), K columns
+template <int K>
+__global__ void k_bj_minv_apply_add(const double2* Minv, BjInfo B, const double2* t, double2* x) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < B.n * K; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / K;
+    const int c = (int)(e % K);
+    int64_t fa, sa;
+    int na, i;
+    B.block(r, fa, na, i, sa);
+    double2 acc = x[e];
+    for (int l = 0; l < na; ++l) {
+      const double2 u = bj_mul(Minv[sa + i * na + l], t[(fa + l) * K + c]);
+      acc.x += u.x;
+      acc.y += u.y;
+    }
+    x[e] = acc;
+  }
 }
 
 int pick_blocks(int64_t n, int k) {
@@ -542,7 +626,7 @@ void launch_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const
 template <typename C>
 int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
               const pg_gmres_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  size_t off[14];
+  size_t off[16];
   ws_layout(P, off);
   C* Ahat = reinterpret_cast<C*>(ws + off[0]);
   double2* dinv = reinterpret_cast<double2*>(ws + off[1]);
@@ -562,9 +646,30 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   const int64_t stride = P.n * k;
   const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
 
+  const bool bj = P.bj.p > 0;
+  double2* Sblk = reinterpret_cast<double2*>(ws + off[14]);
+  double2* Minv = reinterpret_cast<double2*>(ws + off[15]);
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
-  k_diag_inv<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, dinv, dstatus);
-  k_scale_cols<C><<<pg_blocks(P.nnz, 256), 256, 0, s>>>(col, A, P.nnz, dinv, Ahat);
+  if (bj) {
+    // right preconditioning with the entity blocks' inverses: Ahat = A M^-1
+    k_bj_check<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, P.bj, dstatus);
+    int hchk = 0;
+    PG_CUDA_TRY(cudaMemcpyAsync(&hchk, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hchk) {
+      pg_set_error("pg_gmres: block-Jacobi needs the entity-block pattern (rows of one entity share their columns)");
+      return PG_ERR_ARG;
+    }
+    // |D| of the factorisation is not needed here: dinv serves as its scratch
+    k_bj_factor<<<pg_blocks(P.n, 128), 128, 0, s>>>(rowptr, col, A, P.bj, Sblk, reinterpret_cast<double*>(dinv),
+                                                     dstatus);
+    k_bj_minv<<<pg_blocks(P.n, 128), 128, 0, s>>>(Sblk, P.bj, Minv);
+    k_bj_right_scale<C><<<pg_blocks(P.n, 128), 128, 0, s>>>(rowptr, col, A, P.bj, Minv, Ahat);
+    k_fill_one<<<pg_blocks(P.n, 256), 256, 0, s>>>(dinv, P.n);   // the basis combination is added unscaled
+  } else {
+    k_diag_inv<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, dinv, dstatus);
+    k_scale_cols<C><<<pg_blocks(P.nnz, 256), 256, 0, s>>>(col, A, P.nnz, dinv, Ahat);
+  }
   PG_LAUNCH_CHECK();
 
   // ||b|| per RHS
@@ -577,7 +682,7 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   PG_CUDA_TRY(cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
   PG_CUDA_TRY(cudaStreamSynchronize(s));
   if (hstatus) {
-    pg_set_error("pg_gmres: zero diagonal entry (Jacobi preconditioner undefined)");
+    pg_set_error("pg_gmres: zero diagonal entry or block pivot (Jacobi preconditioner undefined)");
     return PG_ERR_BREAKDOWN;
   }
   for (int i = 0; i < k; ++i) {
@@ -642,9 +747,18 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
       PG_KSWITCH(k, (k_givens<K><<<1, 32 * K, 0, s>>>(npart, nb, j, m, st, ctl, j == steps - 1)));
     }
     PG_LAUNCH_CHECK();
-    PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
-                   k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n, ycoef,
-                                                                                      dinv, x)));
+    if (bj) {
+      // x += M^-1 (V y): the combination into r (free until the next true residual), then the blocks
+      PG_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(double2) * P.n * k, s));
+      PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
+                     k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n,
+                                                                                        ycoef, dinv, r),
+                     k_bj_minv_apply_add<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Minv, P.bj, r, x)));
+    } else {
+      PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
+                     k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n,
+                                                                                        ycoef, dinv, x)));
+    }
     // iterations actually used this cycle (max over RHS)
     std::vector<int> hs(k);
     for (int i = 0; i < k; ++i)
@@ -1028,24 +1142,6 @@ __global__ void k_cg_xupdate(const double2* __restrict__ y, const double2* __res
   const int64_t total = n * K;
   for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
     x[e] = dadd(x[e], cmul(S[e / K], y[e]));
-}
-
-// rows of one entity must share their column list (entity-pair pattern);
-// checked through row lengths and first / last columns before block scaling
-__global__ void k_bj_check(const int64_t* rowptr, const int32_t* col, BjInfo B, int* status) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < B.n; r += (int64_t)gridDim.x * blockDim.x) {
-    int64_t f, so;
-    int na, loc;
-    B.block(r, f, na, loc, so);
-    const int64_t l0 = rowptr[f + 1] - rowptr[f], l = rowptr[r + 1] - rowptr[r];
-    if (l != l0 || l < 1 || col[rowptr[r]] != col[rowptr[f]] || col[rowptr[r + 1] - 1] != col[rowptr[f + 1] - 1])
-      *status = PG_ERR_ARG;
-  }
-}
-
-__global__ void k_fill_one(double2* S, int64_t n) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
-    S[r] = make_double2(1.0, 0.0);
 }
 
 struct ToCM64 {
@@ -3138,11 +3234,17 @@ extern "C" void pg_gmres_default_opts(pg_gmres_opts* o) {
   o->reorth = 0;
 }
 
+static Plan gmres_plan(int64_t n, int64_t nnz, int nrhs, const pg_gmres_opts* o) {
+  Plan P{n, nnz, nrhs, o->restart, o->precision, pick_blocks(n, nrhs),
+         o->precision ? sizeof(float2) : sizeof(double2)};
+  if (o->block_p >= 1 && o->block_p <= 6) P.bj = BjInfo{o->block_edges, o->block_faces, o->block_volumes, o->block_p, n};
+  return P;
+}
+
 extern "C" size_t pg_gmres_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_gmres_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
-  Plan P{n, nnz, nrhs, opts->restart, opts->precision, pick_blocks(n, nrhs),
-         opts->precision ? sizeof(float2) : sizeof(double2)};
-  size_t off[14];
+  Plan P = gmres_plan(n, nnz, nrhs, opts);
+  size_t off[16];
   return ws_layout(P, off) + 256;
 }
 
@@ -3158,14 +3260,23 @@ extern "C" int pg_gmres(const int64_t* rowptr, const int32_t* col, const double*
     pg_set_error("pg_gmres: restart must be 1..64, rtol > 0, precision 0 or 1");
     return PG_ERR_ARG;
   }
+  if (opts->block_p > 0) {
+    const int64_t pp = opts->block_p;
+    const int64_t nb_dofs = opts->block_edges * pp + opts->block_faces * pp * (pp - 1) +
+                            opts->block_volumes * (pp * (pp - 1) * (pp - 2) / 2);
+    if (opts->block_p > 6 || opts->block_edges < 0 || opts->block_faces < 0 || opts->block_volumes < 0 ||
+        nb_dofs != n) {
+      pg_set_error("pg_gmres: block-Jacobi entity counts do not match n");
+      return PG_ERR_ARG;
+    }
+  }
   const size_t need = pg_gmres_workspace_bytes(n, nnz, nrhs, opts);
   if (!workspace || workspace_bytes < need) {
     pg_set_error("pg_gmres: workspace too small");
     return PG_ERR_WORKSPACE;
   }
   char* ws = reinterpret_cast<char*>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
-  Plan P{n, nnz, nrhs, opts->restart, opts->precision, pick_blocks(n, nrhs),
-         opts->precision ? sizeof(float2) : sizeof(double2)};
+  Plan P = gmres_plan(n, nnz, nrhs, opts);
   cudaStream_t s = pg_stream(stream);
   const double2* A = reinterpret_cast<const double2*>(vals);
   const double2* bb = reinterpret_cast<const double2*>(b);

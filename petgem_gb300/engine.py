@@ -350,10 +350,9 @@ class DeviceMesh:
     def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
               raise_on_fail=True, ksp="gmres", check_every=50, precond="block"):
         """Solve A x = b for this mesh's CSR pattern (see solve_csr).
-        precond="block": COCG with entity block-Jacobi (each edge / face /
-        volume's diagonal block factored L D L^T); "jacobi": diagonal.  GMRES
-        always uses diagonal Jacobi."""
-        blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" and ksp == "cocg" else None
+        precond="block": entity block-Jacobi (each edge / face / volume's
+        diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal."""
+        blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" else None
         return solve_csr(self.rowptr, self.col, vals, b, x0=x0, rtol=rtol, restart=restart, max_it=max_it,
                          precision=precision, reorth=reorth, raise_on_fail=raise_on_fail, ksp=ksp,
                          check_every=check_every, blocks=blocks)
@@ -518,13 +517,17 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     int32 [nnz], vals complex128 [nnz]); b complex128 [N] or [N, k]
     (k in 1,2,4,8,16,32).  The KSPSolve of petgem/solver.py:584-594.
 
-    ksp="gmres": right-Jacobi restarted GMRES(restart) (PETSc -ksp_type gmres -pc_type jacobi);
+    ksp="gmres": right-preconditioned restarted GMRES(restart) (PETSc -ksp_type gmres,
+                 -pc_type jacobi, or bjacobi with blocks);
     ksp="cocg":  Jacobi-scaled COCG for complex-symmetric A.
     precision="fp64" (complex128), "mixed" (complex64 matrix/SpMV, FP64 recurrence and
     refinement) or "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy).
     Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
-    blocks=(p, n_edges, n_faces, n_elements): COCG with entity block-Jacobi on a
-    pattern built by DeviceMesh (rows of one entity share their columns).
+    blocks=(p, n_edges, n_faces, n_elements): entity block-Jacobi on a pattern
+    built by DeviceMesh (rows of one entity share their columns): COCG runs on
+    S A S^T (S = D^-1/2 L^-1 per block), GMRES on A M^-1 (M^-1 = A_aa^-1 per
+    block, right preconditioning: PETSc -pc_type bjacobi with one block per
+    edge / face / element).
     """
     N = int(rowptr.numel()) - 1
     nnz = int(col.numel())
@@ -540,6 +543,8 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
         o = _lib.GmresOpts()
         lib.pg_gmres_default_opts(ctypes.byref(o))
         o.restart, o.max_it, o.rtol, o.precision, o.reorth = int(restart), int(max_it), float(rtol), prec, int(reorth)
+        if blocks is not None:
+            o.block_p, o.block_edges, o.block_faces, o.block_volumes = (int(v) for v in blocks)
         nbytes = _lib.query("pg_gmres_workspace_bytes", N, nnz, nrhs, ctypes.byref(o))
         fn = lib.pg_gmres
     elif ksp == "cocg":

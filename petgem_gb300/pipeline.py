@@ -147,7 +147,10 @@ class Solver:
             raise ValueError(f"-ksp_type {ksp}: supported types are gmres and cocg")
         pc = str(opts.get("pc_type", "jacobi"))
         if pc not in ("jacobi", "sor", "none", "bjacobi"):
-            raise ValueError(f"-pc_type {pc}: supported preconditioner is jacobi")
+            raise ValueError(f"-pc_type {pc}: supported preconditioners are jacobi and bjacobi")
+        # bjacobi: one block per edge / face / element; sor (petgem's default,
+        # a sequential sweep) and none run with the entity blocks as well
+        precond = "jacobi" if pc == "jacobi" else "block"
         self.info = []
         self.ksp = ksp
         # all polarisations in one batched solve (one SpMM per iteration)
@@ -156,7 +159,7 @@ class Solver:
                                   restart=int(opts.get("ksp_gmres_restart", 30)),
                                   max_it=int(opts.get("ksp_max_it", 10000)),
                                   precision=str(opts.get("pg_precision", "fp64")), ksp=ksp,
-                                  raise_on_fail=False)
+                                  raise_on_fail=False, precond=precond)
         for i in range(len(self.b)):
             self.x[i] = X[:, i].contiguous() if X.ndim == 2 else X
             self.info.append(info)
