@@ -57,9 +57,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--assembly", default="df64", choices=["df64", "fp64"],
                     help="arithmetic of the fused assembly (df64: double-float on the FP32 pipes)")
-    ap.add_argument("--config", type=int, default=1, choices=[1, 2, 4],
+    ap.add_argument("--config", type=int, default=1, choices=[1, 2, 3, 4],
                     help="1: the metric's workload (default); 2: the batched workload (12 systems x 16 RHS in one "
-                         "solve); 4: the MT configuration (p=3, 40^3): assembly and MT right-hand side timing only")
+                         "solve); 3: the adjoint gradient (24^3) with a finite-difference check; 4: the MT "
+                         "configuration (p=3, 40^3): assembly and MT right-hand side timing only")
     ap.add_argument("--no-records", action="store_true",
                     help="assemble from the item list instead of the per-mesh assembly records")
     ap.add_argument("--solve-iters", type=int, default=0,
@@ -596,6 +597,85 @@ def run_reference(args, rank):
             "e2e": {"value": round(v, 6), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_config3(args):
+    """Adjoint gradient workload: 24^3 cubes (82,944 tets, p = 2), m = log10
+    sigma per element, 100 receivers, misfit sum |E - d|^2 with d = E(m) plus
+    10 % complex Gaussian noise (seed 4).  Times the gradient (forward solve,
+    G^T conj(E - d), adjoint solve, per-element contraction) at rtol 1e-8, then
+    checks it against central differences (step 1e-6) on 20 random elements
+    (seed 7) and on the 4 elements of largest gradient, with solves at 1e-11."""
+    import torch
+    from petgem_gb300 import synthetic
+    from petgem_gb300.adjoint import ReceiverMisfit
+    from petgem_gb300.engine import DeviceMesh
+    n = args.n if args.n != 32 else 24
+    model = synthetic.config3(n)
+    mesh = DeviceMesh(model.nodes, model.tets, 2)
+    m = torch.as_tensor(model.m, dtype=torch.float64, device="cuda")
+    # observed data: the model's own fields with 10 % complex noise
+    probe = ReceiverMisfit(mesh, model.source, model.receivers, np.zeros((len(model.receivers), 3), complex),
+                           rtol=1e-11, precision="df64")
+    _, (_, _, u, r, keep) = probe.evaluate(m)
+    E = r.cpu().numpy()                                   # E - 0 at the kept receivers
+    rng = np.random.default_rng(4)
+    noisy = E * (1.0 + 0.1 * (rng.standard_normal(E.shape) + 1j * rng.standard_normal(E.shape)))
+    d = np.zeros((len(model.receivers), 3), complex)
+    d[keep.cpu().numpy()] = noisy
+    out = {}
+    prob = ReceiverMisfit(mesh, model.source, model.receivers, d, rtol=1e-8, precision="df64")
+    prob.value_and_gradient(m)                            # warm-up (autotuning, allocations)
+    torch.cuda.synchronize()
+    t = time.time()
+    phi, g = prob.value_and_gradient(m)
+    torch.cuda.synchronize()
+    t_grad = time.time() - t
+    its = [i.iterations for i in prob.last_info[-2:]]
+    torch.cuda.synchronize()
+    t = time.time()
+    prob.evaluate(m)
+    torch.cuda.synchronize()
+    t_fwd = time.time() - t
+    out["gradient_seconds"] = round(t_grad, 3)
+    out["forward_seconds"] = round(t_fwd, 3)
+    out["solve_iterations_forward_adjoint"] = its
+    # central differences with tight solves
+    tight = ReceiverMisfit(mesh, model.source, model.receivers, d, rtol=1e-11, precision="df64", max_it=400000)
+    phi_t, g_t = tight.value_and_gradient(m)
+    g_np = g_t.cpu().numpy()
+    h = 1e-6
+    rnd = np.random.default_rng(7).choice(mesh.T, 20, replace=False)
+    top = np.argsort(-np.abs(g_np))[:4]
+
+    def fd(e):
+        mp, mm = m.clone(), m.clone()
+        mp[e] += h
+        mm[e] -= h
+        return (tight.evaluate(mp)[0].item() - tight.evaluate(mm)[0].item()) / (2 * h)
+    fd_rnd = np.array([fd(int(e)) for e in rnd])
+    fd_top = np.array([fd(int(e)) for e in top])
+    err_rnd = float(np.linalg.norm(fd_rnd - g_np[rnd]) / np.linalg.norm(g_np[rnd]))
+    err_top = float(np.max(np.abs(fd_top - g_np[top]) / np.abs(g_np[top])))
+    gmax = float(np.max(np.abs(g_np)))
+    out["fd_check"] = {"step": h, "solve_rtol": 1e-11, "random_elements": 20,
+                       "rel_err_random_normwise": err_rnd,
+                       # the random elements' gradients lie far below the largest: a step of 1e-6 moves phi
+                       # less than the solves' own error there, so their differences are measured against
+                       # the gradient's scale
+                       "max_abs_err_random_over_max_gradient": float(np.max(np.abs(fd_rnd - g_np[rnd]))) / gmax,
+                       "max_abs_gradient_random_over_max_gradient": float(np.max(np.abs(g_np[rnd]))) / gmax,
+                       "top_gradient_elements": 4,
+                       "rel_err_top_max": err_top,
+                       "gradient_at_1e-8_vs_1e-11": float(torch.linalg.norm(g - g_t) / torch.linalg.norm(g_t))}
+    return {"metric": "seconds per adjoint gradient (forward + adjoint solve + contraction), p = 2",
+            "value": round(t_grad, 3), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": round(t_grad * 1e3, 1), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "df64 solves (f32 pairs), FP64 contraction", "data": "synthetic",
+            "config": {"workload": f"adjoint_p2_{n}cubed (m = log10 sigma ~ U[-2, 0.5], seed 3; 100 receivers; "
+                                   f"d = E(m) with 10 % complex noise, seed 4)", "tets": mesh.T, "dofs": mesh.N,
+                       "phi": float(phi)},
+            "detail": out}
+
+
 def run_config4(args):
     """p = 3 MT configuration: 40^3 cubes (384,000 tets, 7.2 M DOFs, 611 M
     stored entries): mesh setup, assembly (double-float and FP64) and the MT
@@ -766,6 +846,10 @@ def main():
     if args.config == 2:
         if int(os.environ.get("RANK", 0)) == 0:
             print(json.dumps(run_config2(args)), flush=True)
+        return
+    if args.config == 3:
+        if int(os.environ.get("RANK", 0)) == 0:
+            print(json.dumps(run_config3(args)), flush=True)
         return
     if args.config == 4:
         if int(os.environ.get("RANK", 0)) == 0:

@@ -1720,6 +1720,26 @@ __global__ void k_df_start(const double2* __restrict__ r64, const double2* __res
   block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
 }
 
+// v[:, c] *= f[c] (FP64 vectors)
+template <int K>
+__global__ void k_scale_cols_d2(double2* v, int64_t n, const double* f) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    v[e] = dscale(f[e % K], v[e]);
+}
+
+// v[:, c] *= f[c] (double-float vectors; f split into hi + lo)
+template <int K>
+__global__ void k_scale_cols_df(float4* v, int64_t n, const double* f) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x) {
+    const double fc = f[e % K];
+    const float fh = __double2float_rn(fc);
+    const float fl = __double2float_rn(fc - (double)fh);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    cdf_mac(acc, v[e], make_float4(fh, fl, 0.f, 0.f));
+    v[e] = df_norm(acc);
+  }
+}
+
 template <int K, bool PC = false>
 __global__ void k_df_xupdate(const float4* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
   const int64_t total = n * K;
@@ -1847,7 +1867,7 @@ size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf = false) {
   put(9, sizeof(double2) * (size_t)P.nb * P.k * 3);
   put(10, sizeof(CgState) * P.k);
   put(11, sizeof(CgCtl));
-  put(12, sizeof(double) * P.k * 3);
+  put(12, sizeof(double) * P.k * 6);              // rnorm, target, column scales, inverses, ratios
   put(13, sizeof(int) * (P.k + 1));
   put(14, mf ? sizeof(float4) * P.n * P.k : 0);   // ps = S o p
   put(15, mf ? sizeof(float4) * ns : 0);          // S (double-float)
@@ -2235,6 +2255,12 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   CgCtl* ctl = reinterpret_cast<CgCtl*>(ws + off[11]);
   double* rnorm = reinterpret_cast<double*>(ws + off[12]);
   double* target = rnorm + P.k;
+  // per-column scales of the double-float recurrence: every cycle starts from
+  // the true residual scaled to unit norm, so r^T r stays far inside the
+  // FP32 exponent range whatever the units of b
+  double* cscale = rnorm + 2 * P.k;
+  double* cinv = rnorm + 3 * P.k;
+  double* clam = rnorm + 4 * P.k;
   int* want = reinterpret_cast<int*>(ws + off[13]);
   int* dstatus = want + P.k;
   const int k = P.k, nb = P.nb;
@@ -2283,7 +2309,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
   }
   PG_LAUNCH_CHECK();
-  std::vector<double> bnorm(k), rn(k), tgt(k);
+  std::vector<double> bnorm(k), rn(k), tgt(k), sc(k), sc_prev(k, 1.0), scal(4 * (size_t)k);
   std::vector<int> wnt(k);
   PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, part), k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
   PG_LAUNCH_CHECK();
@@ -2397,7 +2423,8 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       const double tb = o->rtol * bnorm[i];
       const bool ok = rn[i] <= tb || bnorm[i] == 0.0;
       wnt[i] = ok ? 0 : 1;
-      tgt[i] = 0.5 * tb;
+      sc[i] = rn[i] > 0.0 && isfinite(rn[i]) ? rn[i] : 1.0;
+      tgt[i] = 0.5 * tb / sc[i];
       if (!ok) all = false;
     }
     if (status || all) break;
@@ -2405,8 +2432,24 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       status = PG_ERR_NOT_CONVERGED;
       break;
     }
+    // unit-norm cycle: the residual estimate starts at 1 (0 for an exact
+    // column), p is carried over in the new scale
+    for (int i = 0; i < k; ++i) {
+      scal[i] = rn[i] > 0.0 ? 1.0 : 0.0;
+      scal[k + i] = sc[i];
+      scal[2 * k + i] = 1.0 / sc[i];
+      scal[3 * k + i] = sc_prev[i] / sc[i];
+      sc_prev[i] = sc[i];
+    }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(rnorm, scal.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(cscale, scal.data() + k, sizeof(double) * 3 * k, cudaMemcpyHostToDevice, s));
+    PG_KSWITCH(k, (k_scale_cols_d2<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, P.n, cinv)));
+    if (!first) {
+      PG_KSWITCH(k, (k_scale_cols_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(pv, P.n, clam)));
+      if (mf) PG_KSWITCH(k, (k_scale_cols_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(ps, P.n, clam)));
+    }
     if (mf) {
       PG_KSWITCH(k, (k_df_start<K, true><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part, ps)));
     } else {
@@ -2454,7 +2497,9 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
         cudaStreamWaitEvent(s, ev_out, 0);
       }
     }
-    for (; done < steps; ++done) one_iteration(s);    PG_LAUNCH_CHECK();
+    for (; done < steps; ++done) one_iteration(s);
+    PG_LAUNCH_CHECK();
+    PG_KSWITCH(k, (k_scale_cols_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(y, P.n, cscale)));
     if (mf) {
       PG_KSWITCH(k, (k_df_xupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(y, S, P.n, x)));
     } else if (bj) {
@@ -2829,16 +2874,41 @@ __global__ void k_sg_cycle_init(const double2* prho, Seg g, CgState* st, const d
   }
 }
 
+__device__ __forceinline__ int seg_of_row(const Seg& g, int64_t r) {
+  int lo = 0, hi = g.S - 1;   // largest j with row[j] <= r
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.row[mid] <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// v[r, c] *= f[system(r) * K + c] (FP64 vectors)
+template <int K>
+__global__ void k_sg_scale_d2(double2* v, Seg g, int64_t n, const double* f) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    v[e] = dscale(f[seg_of_row(g, e / K) * K + e % K], v[e]);
+}
+
+// the same for double-float vectors
+template <int K>
+__global__ void k_sg_scale_df(float4* v, Seg g, int64_t n, const double* f) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x) {
+    const double fc = f[seg_of_row(g, e / K) * K + e % K];
+    const float fh = __double2float_rn(fc);
+    const float fl = __double2float_rn(fc - (double)fh);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    cdf_mac(acc, v[e], make_float4(fh, fl, 0.f, 0.f));
+    v[e] = df_norm(acc);
+  }
+}
+
 // every stored column of system j lies in its own rows (block-diagonal)
 __global__ void k_sg_check(const int64_t* rowptr, const int32_t* col, Seg g, int64_t n, int* status) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = g.S - 1;   // system of row r
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (g.row[mid] <= r) lo = mid;
-      else hi = mid - 1;
-    }
-    const int64_t c0 = g.row[lo], c1 = g.row[lo + 1];
+    const int j = seg_of_row(g, r);
+    const int64_t c0 = g.row[j], c1 = g.row[j + 1];
     for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
       if (col[k] < c0 || col[k] >= c1) *status = PG_ERR_ARG;
   }
@@ -2917,7 +2987,7 @@ size_t sg_layout(const SegPlan& P, size_t* off /* 18 */) {
   put(9, sizeof(double2) * (size_t)P.nb * P.k * 3);
   put(10, sizeof(CgState) * pairs);
   put(11, sizeof(CgCtl));
-  put(12, sizeof(double) * pairs * 3);           // rnorm, target
+  put(12, sizeof(double) * pairs * 6);           // rnorm, target, pair scales, inverses, ratios
   put(13, sizeof(int) * (pairs + 1));            // want, status
   put(14, sizeof(int64_t) * (P.S + 1));          // system rows
   put(15, sizeof(int) * (P.S + 1));              // system blocks
@@ -2975,6 +3045,11 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   const int pairs = P.S * P.k;
   double* rnorm = reinterpret_cast<double*>(ws + off[12]);
   double* target = rnorm + pairs;
+  // per-pair scales: every cycle starts from the true residual at unit norm
+  // (r^T r stays inside the FP32 exponent range of the double-float pairs)
+  double* cscale = rnorm + 2 * pairs;
+  double* cinv = rnorm + 3 * pairs;
+  double* clam = rnorm + 4 * pairs;
   int* want = reinterpret_cast<int*>(ws + off[13]);
   int* dstatus = want + pairs;
   int64_t* drows = reinterpret_cast<int64_t*>(ws + off[14]);
@@ -3024,7 +3099,7 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
     k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, Sd, At, wdf, wd);
   }
   PG_LAUNCH_CHECK();
-  std::vector<double> bnorm(pairs), rn(pairs), tgt(pairs);
+  std::vector<double> bnorm(pairs), rn(pairs), tgt(pairs), sc(pairs), sc_prev(pairs, 1.0), scal(4 * (size_t)pairs);
   std::vector<int> wnt(pairs);
   PG_KSWITCH(k, (k_sg_norm2<K><<<G, kThreads, 0, s>>>(b, g, part), k_sg_norm_final<K><<<1, kThreads, 0, s>>>(part, g, rnorm)));
   PG_LAUNCH_CHECK();
@@ -3123,7 +3198,8 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
       const double tb = o->rtol * bnorm[t];
       const bool ok = rn[t] <= tb || bnorm[t] == 0.0;
       wnt[t] = ok ? 0 : 1;
-      tgt[t] = 0.5 * tb;
+      sc[t] = rn[t] > 0.0 && isfinite(rn[t]) ? rn[t] : 1.0;
+      tgt[t] = 0.5 * tb / sc[t];
       if (!ok) all = false;
     }
     if (status || all) break;
@@ -3131,8 +3207,19 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
       status = PG_ERR_NOT_CONVERGED;
       break;
     }
+    for (int t = 0; t < pairs; ++t) {
+      scal[t] = rn[t] > 0.0 ? 1.0 : 0.0;
+      scal[pairs + t] = sc[t];
+      scal[2 * pairs + t] = 1.0 / sc[t];
+      scal[3 * pairs + t] = sc_prev[t] / sc[t];
+      sc_prev[t] = sc[t];
+    }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * pairs, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * pairs, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(rnorm, scal.data(), sizeof(double) * pairs, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(cscale, scal.data() + pairs, sizeof(double) * 3 * pairs, cudaMemcpyHostToDevice, s));
+    PG_KSWITCH(k, (k_sg_scale_d2<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, g, P.n, cinv)));
+    if (!first) PG_KSWITCH(k, (k_sg_scale_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(pv, g, P.n, clam)));
     // systems already converged keep one idle block; the others take the rest
     for (int j = 0; j < P.S; ++j) {
       sys_active[j] = 0;
@@ -3167,6 +3254,7 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
     }
     for (; done < steps; ++done) one_iteration(s);
     PG_LAUNCH_CHECK();
+    PG_KSWITCH(k, (k_sg_scale_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(y, g, P.n, cscale)));
     if (bj) {
       for (int j = 0; j < P.S; ++j) {
         const BjInfo& B = P.bj[j];

@@ -148,6 +148,22 @@ def config2_extra(n):
     return m
 
 
+def config3(n=24):
+    """Adjoint gradient workload, p=2: n^3 cubes x 6 tets over [-1000, 1000]^3;
+    per-element m_e = log10 sigma_e ~ U[-2, 0.5] (seed 3), sigma_h = sigma_v;
+    HED at (0,0,50) 1 Hz; 10x10 receivers on z=0 spanning [-800, 800]^2.
+    The model's `m` holds the log-conductivities."""
+    nodes, tets = kuhn_box(n)
+    m = np.random.default_rng(3).uniform(-2.0, 0.5, len(tets))
+    s = 10.0 ** m
+    g = np.linspace(-800.0, 800.0, 10)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    rx = np.stack([X.ravel(), Y.ravel(), np.zeros(100)], axis=1)
+    model = Model(f"adjoint_p2_{n}cubed", nodes, tets, np.stack([s, s], axis=1), 2, _hed(), rx)
+    model.m = m
+    return model
+
+
 def config4(n=40, seed=5):
     """MT, p=3, n^3 cubes over [-5000, 5000]^2 x [-5000, 2000] m: air 1e-8 S/m
     above z=0, 0.1 S/m for -1000 <= z <= 0, 0.01 S/m below, and three
