@@ -49,6 +49,9 @@ struct BjInfo {
   __host__ __device__ int64_t n_blocks() const { return nE + (df() ? nF : 0) + (dv() ? nV : 0); }
 };
 
+// the kernels below are compiled into every solver translation unit
+namespace {
+
 __device__ __forceinline__ double2 bj_mul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -213,3 +216,5 @@ __global__ void k_bj_apply_t_add(const double2* S, BjInfo B, const YT* y, double
     x[e] = acc;
   }
 }
+
+}  // namespace

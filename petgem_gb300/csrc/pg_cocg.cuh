@@ -1,0 +1,352 @@
+// Shared pieces of the COCG solvers: per-RHS state and control block,
+// last-block reductions, Jacobi and entity block-Jacobi setup, the
+// double-float arithmetic and its reductions, and the solver entry points
+// that cross translation units.
+#pragma once
+#include "pg_krylov.cuh"
+
+namespace {
+
+// ============================================================================
+// COCG: conjugate orthogonal CG for complex-symmetric A (A^T = A, not
+// Hermitian), the short-recurrence Krylov method for the complex symmetric
+// systems of frequency-domain edge-element EM.  Jacobi enters as a symmetric
+// scaling  At = S A S,  S = D^-1/2  (complex principal square root), which
+// keeps At complex symmetric; the iteration solves At y = S r and x += S y.
+// The recurrence works in the Arnoldi-equivalent "compute" precision (complex
+// 128 or 64).  At every host check (every `check_every` iterations) the FP64
+// true residual  r = b - A x  replaces the recurrence residual (reliable
+// update: the search direction p is kept), and convergence is decided on it.
+// Per iteration: SpMV fused with mu = p^T q; alpha; y += alpha p, r -= alpha q
+// fused with rho = r^T r and the true-residual weight sum |r_i|^2 |D_i|; beta;
+// p = r + beta p.  Reductions are fixed-order (deterministic).
+// ============================================================================
+
+struct CgState {
+  double2 rho;     // r^T r (bilinear)
+  double2 alpha, beta;
+  double target;   // absolute true-residual target
+  double res;      // recurrence estimate of the true residual
+  double res0;     // true residual at the start of this cycle
+  int active;      // iterating (not converged)
+  int its;
+  int breakdown;
+  int beta_iter;   // launch index whose beta is current (p is updated once per beta)
+};
+
+struct CgCtl {
+  int any_active;      // some RHS still iterating in this cycle
+  int nonfinite;
+  unsigned counter;    // last-block-done counter (reset by the last block)
+  int pending;         // double-float path: a p update is due (set by the update, cleared by the product)
+};
+
+template <typename C>
+__device__ __forceinline__ double2 bilin(C a, C b) {  // a*b (no conjugate) in double
+  const double2 x = to_d(a), y = to_d(b);
+  return make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+}
+
+// Every block publishes its partial; the block that arrives last (atomic
+// ticket) reduces all partials in block order - a fixed order, so the result
+// does not depend on which block is last.  Nothing waits: no spin.
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return last;
+}
+
+// block-wide fixed-order sum of partial[b * K + rhs] over b, per rhs (K <= 32)
+template <int K>
+__device__ double2 sum_partials(const double2* partial, int nblocks, int rhs, double2* smem) {
+  // thread t handles rhs = t % K, blocks b = t / K, t / K + 256 / K, ...
+  const int my_rhs = threadIdx.x % K;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int b = threadIdx.x / K; b < nblocks; b += kThreads / K) acc = dadd(acc, __ldcg(partial + (int64_t)b * K + my_rhs));
+  block_reduce_rhs<K>(acc, smem, smem + (kThreads / 32) * K);
+  const double2 out = smem[(kThreads / 32) * K + rhs];
+  __syncthreads();
+  return out;
+}
+
+// S = D^-1/2 (principal root), wd = |D|, At = S A S in precision CM
+__global__ void k_cg_scaling(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n, double2* S,
+                             double* wd, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 d = make_double2(0.0, 0.0);
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      if (col[k] == r) d = val[k];
+    const double ad = sqrt(dabs2(d));
+    if (ad == 0.0) {
+      *status = PG_ERR_BREAKDOWN;
+      S[r] = make_double2(1.0, 0.0);
+      wd[r] = 1.0;
+      continue;
+    }
+    const double sr = sqrt(0.5 * (ad + d.x));
+    double si = sqrt(fmax(0.0, 0.5 * (ad - d.x)));
+    if (d.y < 0) si = -si;
+    S[r] = ddiv(make_double2(1.0, 0.0), make_double2(sr, si));
+    wd[r] = ad;
+  }
+}
+
+template <int K>
+__global__ void k_cg_cycle_init(const double2* prho, int nblocks, CgState* st, const double* rnorm,
+                                const double* target, const int* want, CgCtl* ctl, int first) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, rhs = threadIdx.x >> 5;
+  if (rhs < K) {
+    double2 rho = make_double2(0.0, 0.0);
+    for (int b = lane; b < nblocks; b += 32) rho = dadd(rho, prho[(int64_t)b * K + rhs]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) rho = dadd(rho, shfl_xor(rho, off));
+    if (lane == 0) {
+      CgState& S = st[rhs];
+      if (first) {
+        S.its = 0;
+        S.breakdown = 0;
+        S.beta_iter = 0;
+      }
+      S.rho = rho;
+      S.target = target[rhs];
+      S.res = rnorm[rhs];
+      S.res0 = rnorm[rhs];
+      S.active = want[rhs] && rnorm[rhs] > 0.0;
+      S.alpha = S.beta = make_double2(0.0, 0.0);
+      if (S.active) atomicOr(&any, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any;
+    ctl->nonfinite = 0;
+    ctl->counter = 0;
+  }
+}
+
+struct ToCM64 {
+  __device__ double2 operator()(double2 v) const { return v; }
+};
+struct ToCM32 {
+  __device__ float2 operator()(double2 v) const { return make_float2((float)v.x, (float)v.y); }
+};
+struct IdD2 {
+  __device__ double2 operator()(double2 v) const { return v; }
+};
+
+// block-Jacobi setup shared by the COCG drivers: S (diagonal) := 1, the
+// entity factors into Sblk, |D| into wd, At = S A S^T in the solver's precision
+template <typename CM, typename Conv>
+int bj_setup(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, double2* S, double* wd,
+             double2* Sblk, CM* At, Conv conv, int* dstatus, cudaStream_t s) {
+  k_fill_one<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n);
+  k_bj_check<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, P.bj, dstatus);
+  int h = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&h, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h) {
+    pg_set_error("pg_cocg: block-Jacobi needs the entity-block pattern (rows of one entity share their columns)");
+    return PG_ERR_ARG;
+  }
+  k_bj_factor<<<pg_blocks(P.n, 128), 128, 0, s>>>(rowptr, col, A, P.bj, Sblk, wd, dstatus);
+  k_bj_scale_matrix<<<pg_blocks(P.n, 128), 128, 0, s>>>(rowptr, col, A, P.bj, Sblk, At, conv);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}
+
+// ============================================================================
+// df64: FP64-accurate COCG on the FP32 pipes.  Values are double-float pairs
+// (hi + lo, ~48-bit mantissa); a complex number is a float4
+// (re.hi, re.lo, im.hi, im.lo), 16 bytes like complex128.  Products are made
+// error-free with FMA, sums are compensated (two-sum), so every operation
+// costs ~11 FP32 instructions instead of one FP64 instruction - and GB300's
+// FP32 pipe is ~57x faster than its FP64 pipe, which makes the SpMV HBM-bound
+// instead of FP64-bound.  FP64 is kept for the scaling, the true residual, the
+// reliable updates and x.
+// ============================================================================
+
+__device__ __forceinline__ float4 df_norm(float4 v) {
+  const float s = __fadd_rn(v.x, v.y);
+  const float e1 = __fsub_rn(v.y, __fsub_rn(s, v.x));
+  const float t = __fadd_rn(v.z, v.w);
+  const float e2 = __fsub_rn(v.w, __fsub_rn(t, v.z));
+  return make_float4(s, e1, t, e2);
+}
+
+// c += a * b (complex double-float)
+__device__ __forceinline__ void cdf_mac(float4& c, float4 a, float4 b) {
+  df_mac(c.x, c.y, a.x, a.y, b.x, b.y);
+  df_mac(c.x, c.y, -a.z, -a.w, b.z, b.w);
+  df_mac(c.z, c.w, a.x, a.y, b.z, b.w);
+  df_mac(c.z, c.w, a.z, a.w, b.x, b.y);
+}
+
+__device__ __forceinline__ float4 cdf_from(double2 v) {
+  const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
+  return make_float4(rh, __double2float_rn(v.x - (double)rh), ih, __double2float_rn(v.y - (double)ih));
+}
+__device__ __forceinline__ double2 cdf_to(float4 v) {
+  return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+__device__ __forceinline__ float4 shfl_xor4(float4 v, int m) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
+                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
+}
+__device__ __forceinline__ void cdf_add(float4& a, float4 b) {
+  df_add(a.x, a.y, b.x, b.y);
+  df_add(a.z, a.w, b.z, b.w);
+}
+
+// Block reductions of double-float values: the warp and block stages add in
+// double-float on the FP32 pipes and only the block total is converted to
+// double (GB300's FP64 pipe runs ~2 operations per clock per SM, so a
+// per-thread conversion plus a double-precision shuffle tree cost more than
+// the vector update they reduce).  Lanes with equal lane % K combine.
+template <int K>
+__device__ void block_reduce_df(float4 v, float4* smf, double2* out) {
+#pragma unroll
+  for (int off = 16; off >= K; off >>= 1) cdf_add(v, shfl_xor4(v, off));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K) smf[warp * K + lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    float4 t = smf[threadIdx.x];
+    for (int w = 1; w < kThreads / 32; ++w) cdf_add(t, smf[w * K + threadIdx.x]);
+    out[threadIdx.x] = cdf_to(t);
+  }
+  __syncthreads();
+}
+
+template <int K>
+__device__ void block_reduce_f(float v, float* smf, double2* out) {
+#pragma unroll
+  for (int off = 16; off >= K; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K) smf[warp * K + lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    float t = smf[threadIdx.x];
+    for (int w = 1; w < kThreads / 32; ++w) t += smf[w * K + threadIdx.x];
+    out[threadIdx.x] = make_double2((double)t, 0.0);
+  }
+  __syncthreads();
+}
+
+// alpha / beta finalisation shared by the df kernels (last block only)
+template <int K>
+__device__ void cg_alpha_final(const double2* partial, int nblocks, CgState* st, CgCtl* ctl, double2* smem) {
+  const double2 m = sum_partials<K>(partial, nblocks, threadIdx.x < K ? threadIdx.x : 0, smem);
+  if (threadIdx.x < K) {
+    CgState& S = st[threadIdx.x];
+    if (S.active) {
+      if (m.x == 0.0 && m.y == 0.0) {
+        S.breakdown = 1;
+        S.active = 0;
+        S.alpha = make_double2(0.0, 0.0);
+      } else {
+        S.alpha = ddiv(S.rho, m);
+      }
+    } else {
+      S.alpha = make_double2(0.0, 0.0);
+    }
+  }
+  if (threadIdx.x == 0) ctl->counter = 0;
+}
+
+template <int K>
+__device__ void cg_beta_final(const double2* prho, const double2* pw, int nblocks, CgState* st, CgCtl* ctl, int iter,
+                              double delta, double2* smem) {
+  const int my = threadIdx.x < K ? threadIdx.x : 0;
+  const double2 rho = sum_partials<K>(prho, nblocks, my, smem);
+  const double2 w = sum_partials<K>(pw, nblocks, my, smem);
+  __shared__ int any, stop;
+  if (threadIdx.x == 0) { any = 0; stop = 0; }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    CgState& S = st[threadIdx.x];
+    if (S.active) {
+      S.beta_iter = 1;   // fresh beta: the next p update applies it once
+      S.its += 1;
+      S.res = sqrt(w.x);
+      if (!isfinite(S.res)) ctl->nonfinite = 1;
+      if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+        S.breakdown = 1;
+        S.active = 0;
+        S.beta = make_double2(0.0, 0.0);
+      } else {
+        S.beta = ddiv(rho, S.rho);
+      }
+      S.rho = rho;
+      if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
+      else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
+    } else {
+      S.beta = make_double2(0.0, 0.0);
+      S.beta_iter = 0;
+    }
+    if (S.active) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any && !stop;
+    ctl->pending = 1;
+    ctl->counter = 0;
+  }
+}
+
+__global__ void k_df_scale_matrix(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n,
+                                  const double2* S, float4* out, float* wdf, const double* wd) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 sr = S[r];
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) out[k] = cdf_from(cmul(sr, cmul(val[k], S[col[k]])));
+    wdf[r] = (float)wd[r];
+  }
+}
+
+template <int K, bool PC = false>
+__global__ void k_df_xupdate(const float4* __restrict__ y, const double2* __restrict__ S, int64_t n, double2* x) {
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    x[e] = dadd(x[e], cmul(S[PC ? e : e / K], cdf_to(y[e])));
+}
+
+struct ToDF {
+  __device__ float4 operator()(double2 v) const { return cdf_from(v); }
+};
+
+__global__ void k_wd_to_f32(const double* wd, int64_t n, float* wdf) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    wdf[r] = (float)wd[r];
+}
+struct DfToD2 {
+  __device__ double2 operator()(float4 v) const { return cdf_to(v); }
+};
+
+constexpr int kGraphIters = 16;   // iterations per captured CUDA graph
+
+inline Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
+  int nb = pick_blocks(n, nrhs);
+  if (nb < 152 * 16) nb = 152 * 16;  // partials also hold the SpMV's per-block sums
+  Plan P{n, nnz, nrhs, 1, o->precision, nb, o->precision == 1 ? sizeof(float2) : sizeof(double2), BjInfo{}};
+  P.bj = BjInfo{o->block_edges, o->block_faces, o->block_volumes, o->block_p, n};
+  if (o->block_p < 1 || o->block_p > 6) P.bj.p = 0;
+  return P;
+}
+
+}  // namespace
+
+namespace pgk {
+
+// workspace layout of the double-float COCG (mf: several frequencies)
+size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf = false);
+// double-float COCG; col_scale (host [k]) selects the several-frequencies form
+int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
+                const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
+                const double* col_scale = nullptr);
+
+}  // namespace pgk
