@@ -44,3 +44,48 @@ def test_host_queries():
 
 def test_library_is_in_tree():
     assert os.path.dirname(_lib.library_path()) == os.path.dirname(os.path.abspath(_build.__file__))
+
+
+def test_solver_argument_checks_on_host():
+    """Size queries and argument checks of the solvers run on the host,
+    before any device call: bad shapes return 0 bytes / PG_ERR_ARG."""
+    import ctypes
+
+    import numpy as np
+    lib = _lib.load()
+    P = ctypes.c_void_p
+    co = _lib.CocgOpts()
+    lib.pg_cocg_default_opts(ctypes.byref(co))
+    co.precision = 2
+    rows = np.array([0, 10, 30], dtype=np.int64)
+    rp = P(rows.ctypes.data)
+    ok = lib.pg_cocg_segments_workspace_bytes(30, 300, 4, rp, 2, P(0), ctypes.byref(co))
+    assert ok > 0
+    bad = np.array([0, 10, 29], dtype=np.int64)          # does not end at n
+    assert lib.pg_cocg_segments_workspace_bytes(30, 300, 4, P(bad.ctypes.data), 2, P(0), ctypes.byref(co)) == 0
+    down = np.array([0, 20, 10, 30], dtype=np.int64)     # falls
+    assert lib.pg_cocg_segments_workspace_bytes(30, 300, 1, P(down.ctypes.data), 3, P(0), ctypes.byref(co)) == 0
+    assert lib.pg_cocg_segments_workspace_bytes(30, 300, 3, rp, 2, P(0), ctypes.byref(co)) == 0   # k not 2^i
+    # block-Jacobi needs per-system entity counts that add up to each system's rows (p = 2: 2 per edge / face)
+    co.block_p = 2
+    assert lib.pg_cocg_segments_workspace_bytes(30, 300, 1, rp, 2, P(0), ctypes.byref(co)) == 0
+    ents = np.array([3, 2, 0, 5, 5, 0], dtype=np.int64)
+    assert lib.pg_cocg_segments_workspace_bytes(30, 300, 1, rp, 2, P(ents.ctypes.data), ctypes.byref(co)) > ok // 4
+    ents_bad = np.array([4, 2, 0, 5, 5, 0], dtype=np.int64)
+    assert lib.pg_cocg_segments_workspace_bytes(30, 300, 1, rp, 2, P(ents_bad.ctypes.data), ctypes.byref(co)) == 0
+    # pg_cocg_segments only runs the double-float form: checked before the device is touched
+    co.precision = 0
+    res = _lib.GmresResult()
+    st = lib.pg_cocg_segments(P(8), P(8), P(8), 30, 300, rp, 2, P(0), P(8), P(8), 1, ctypes.byref(co),
+                              ctypes.byref(res), P(0), P(0), P(8), 1 << 20, P(0))
+    assert st == -1
+    # GMRES block-Jacobi entity counts must add up to n
+    go = _lib.GmresOpts()
+    lib.pg_gmres_default_opts(ctypes.byref(go))
+    plain = lib.pg_gmres_workspace_bytes(30, 300, 1, ctypes.byref(go))
+    go.block_p, go.block_edges, go.block_faces, go.block_volumes = 2, 5, 10, 0
+    assert lib.pg_gmres_workspace_bytes(30, 300, 1, ctypes.byref(go)) > plain
+    go.block_faces = 11
+    st = lib.pg_gmres(P(8), P(8), P(8), 30, 300, P(8), P(8), 1, ctypes.byref(go), ctypes.byref(res), P(0), P(8),
+                      1 << 30, P(0))
+    assert st == -1
