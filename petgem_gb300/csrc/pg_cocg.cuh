@@ -338,6 +338,64 @@ inline Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
   return P;
 }
 
+// ---- product variants shared by the double-float solvers ------------------
+// The entity-group check and the on-line autotuner: at the first cycle of a
+// solve each candidate product runs 3 times on the actual operands (the
+// product is the first kernel of an iteration and recomputes alpha, so the
+// extra runs change no solver state) and the fastest is kept.
+// PG_AUTOTUNE=0 keeps the default variant.
+// 0 if rows of every aligned group of R have the first row's column list
+__global__ void k_group_check(const int64_t* rowptr, const int32_t* col, int64_t n, int R, int* status) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = r - r % R;
+    if (f == r) continue;
+    const int64_t o = rowptr[r], of = rowptr[f], len = rowptr[r + 1] - o;
+    if (len != rowptr[f + 1] - of) {
+      *status = 1;
+      continue;
+    }
+    for (int64_t k = 0; k < len; ++k)
+      if (col[o + k] != col[of + k]) {
+        *status = 1;
+        break;
+      }
+  }
+}
+
+bool autotune_enabled() {
+  const char* e = getenv("PG_AUTOTUNE");
+  return !(e && e[0] == '0');
+}
+
+// time each candidate (3 runs after 1 warm-up) and return the fastest
+template <typename F>
+int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return cands[0];
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return cands[0];
+  }
+  int best = cands[0];
+  float best_ms = 1e30f;
+  for (int v : cands) {
+    launch(v);
+    cudaEventRecord(a, s);
+    for (int i = 0; i < 3; ++i) launch(v);
+    cudaEventRecord(b, s);
+    if (cudaEventSynchronize(b) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
+
 }  // namespace
 
 namespace pgk {

@@ -316,24 +316,6 @@ __global__ void k_mf_resid(const int64_t* __restrict__ rowptr, const int32_t* __
 // and uses them for R rows: fewer loads per stored entry and R independent
 // accumulations per lane.
 
-// 0 if rows of every aligned group of R have the first row's column list
-__global__ void k_group_check(const int64_t* rowptr, const int32_t* col, int64_t n, int R, int* status) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = r - r % R;
-    if (f == r) continue;
-    const int64_t o = rowptr[r], of = rowptr[f], len = rowptr[r + 1] - o;
-    if (len != rowptr[f + 1] - of) {
-      *status = 1;
-      continue;
-    }
-    for (int64_t k = 0; k < len; ++k)
-      if (col[o + k] != col[of + k]) {
-        *status = 1;
-        break;
-      }
-  }
-}
-
 // one RHS: G lanes per group of R rows, U column steps per loop pass
 template <int R, int G, int U = 1>
 __global__ void __launch_bounds__(kThreads) k_df_spmv_grp(const int64_t* __restrict__ rowptr,
@@ -563,10 +545,6 @@ int forced_variant(int k, int group) {
   return -1;
 }
 
-bool autotune_enabled() {
-  const char* e = getenv("PG_AUTOTUNE");
-  return !(e && e[0] == '0');
-}
 
 // single RHS: variant = lanes per row G (1..8) * 10 + unroll U, or
 // 100 R + 10 (U - 1) + G for the product over groups of R rows with G lanes
@@ -613,34 +591,6 @@ void launch_df_spmm(int variant, int grid, cudaStream_t s, const int64_t* rowptr
     k_df_spmm<K, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
 }
 
-// time each candidate (3 runs after 1 warm-up) and return the fastest
-template <typename F>
-int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
-  cudaEvent_t a, b;
-  if (cudaEventCreate(&a) != cudaSuccess) return cands[0];
-  if (cudaEventCreate(&b) != cudaSuccess) {
-    cudaEventDestroy(a);
-    return cands[0];
-  }
-  int best = cands[0];
-  float best_ms = 1e30f;
-  for (int v : cands) {
-    launch(v);
-    cudaEventRecord(a, s);
-    for (int i = 0; i < 3; ++i) launch(v);
-    cudaEventRecord(b, s);
-    if (cudaEventSynchronize(b) != cudaSuccess) break;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = v;
-    }
-  }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  return best;
-}
 
 }  // namespace
 

@@ -191,6 +191,117 @@ __global__ void __launch_bounds__(kThreads) k_sg_spmm(const int64_t* __restrict_
   if (arrive_last(&ctl->counter)) seg_alpha_final<K>(partial, g, st, ctl);
 }
 
+// one RHS, G lanes per group of R rows (the rows of one mesh entity share
+// their column list); each lane issues the loads of B column steps before
+// using them.  Every system's rows start at a multiple of R.
+template <int R, int G, int B>
+__global__ void __launch_bounds__(kThreads) k_sg_spmv_grpb(const int64_t* __restrict__ rowptr,
+                                                           const int32_t* __restrict__ col,
+                                                           const float4* __restrict__ val, Seg g,
+                                                           const float4* __restrict__ pv, float4* __restrict__ q,
+                                                           double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;
+  if (!ctl->any_active) return;
+  const SegPos sp = seg_pos(g);
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (seg_live<1>(st, sp.j)) {
+    const int64_t ngroups = (sp.r1 - sp.r0) / R;
+    const int lane = threadIdx.x % G;
+    const int64_t groups = ((int64_t)sp.nbj * kThreads) / G;
+    const int64_t gid = ((int64_t)sp.lb * kThreads + threadIdx.x) / G;
+    const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+    for (int64_t gw = warp_base; gw < ngroups; gw += groups) {
+      const int64_t gi = gw + (gid - warp_base);
+      const bool valid = gi < ngroups;
+      const int64_t r0 = sp.r0 + gi * R;
+      float4 acc[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (valid) {
+        int64_t off[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+        const int len = (int)(rowptr[r0 + 1] - off[0]);
+        for (int k0 = lane; k0 < len; k0 += G * B) {
+          int c[B];
+          float4 v[B][R], x[B];
+#pragma unroll
+          for (int j = 0; j < B; ++j) {
+            const int k = k0 + j * G;
+            c[j] = k < len ? col[off[0] + k] : 0;
+#pragma unroll
+            for (int i = 0; i < R; ++i) v[j][i] = k < len ? val[off[i] + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+#pragma unroll
+          for (int j = 0; j < B; ++j) x[j] = k0 + j * G < len ? pv[c[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int j = 0; j < B; ++j)
+            if (k0 + j * G < len) {
+#pragma unroll
+              for (int i = 0; i < R; ++i) cdf_mac(acc[i], v[j][i], x[j]);
+            }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) cdf_add(acc[i], shfl_xor4(acc[i], o));
+      if (valid && lane == 0) {
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const float4 a = df_norm(acc[i]);
+          q[r0 + i] = a;
+          cdf_mac(mu, pv[r0 + i], a);
+        }
+      }
+    }
+  }
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<1>(mu, smf, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) seg_alpha_final<1>(partial, g, st, ctl);
+}
+
+// K RHS: one thread per (group of R rows, rhs)
+template <int K, int R>
+__global__ void __launch_bounds__(kThreads) k_sg_spmm_grp(const int64_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col,
+                                                          const float4* __restrict__ val, Seg g,
+                                                          const float4* __restrict__ pv, float4* __restrict__ q,
+                                                          double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;
+  if (!ctl->any_active) return;
+  const SegPos sp = seg_pos(g);
+  const int rhs = threadIdx.x % K;
+  float4 mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (seg_live<K>(st, sp.j)) {
+    const int64_t items = ((sp.r1 - sp.r0) / R) * K;
+    for (int64_t it = (int64_t)sp.lb * kThreads + threadIdx.x; it < items; it += (int64_t)sp.nbj * kThreads) {
+      const int64_t r0 = sp.r0 + (it / K) * R;
+      int64_t off[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+      const int64_t len = rowptr[r0 + 1] - off[0];
+      float4 acc[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int64_t k = 0; k < len; ++k) {
+        const float4 x = pv[(int64_t)col[off[0] + k] * K + rhs];
+#pragma unroll
+        for (int i = 0; i < R; ++i) cdf_mac(acc[i], val[off[i] + k], x);
+      }
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const float4 a = df_norm(acc[i]);
+        q[(r0 + i) * K + rhs] = a;
+        cdf_mac(mu, pv[(r0 + i) * K + rhs], a);
+      }
+    }
+  }
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<K>(mu, smf, partial + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) seg_alpha_final<K>(partial, g, st, ctl);
+}
+
 // y += alpha p ; r -= alpha q with each system's alpha; partial rho and w
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_sg_update(float4* __restrict__ y, float4* __restrict__ r,
@@ -565,6 +676,56 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
     pg_set_error("pg_cocg_segments: zero diagonal entry (Jacobi scaling undefined)");
     return PG_ERR_BREAKDOWN;
   }
+  // rows of one entity share their columns (checked): the group products apply
+  int group = 0;
+  if (bj && (P.p == 2 || P.p == 3)) {
+    int* gflag = reinterpret_cast<int*>(part);
+    int hg = 1;
+    PG_CUDA_TRY(cudaMemsetAsync(gflag, 0, sizeof(int), s));
+    k_group_check<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, P.n, P.p, gflag);
+    PG_LAUNCH_CHECK();
+    PG_CUDA_TRY(cudaMemcpyAsync(&hg, gflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    group = hg == 0 ? P.p : 0;
+  }
+  // product variants (same numbering as the single-system solver): one RHS
+  // 10 G + U for G lanes per row and unroll U, 100 R + 30 + G for the group
+  // product with G lanes per group and 4 batched column steps; several RHS
+  // U = 1, 2 or 100 R for the group product
+  std::vector<int> cands;
+  if (k == 1) {
+    cands = {42, 41, 22, 82};
+    if (group) {
+      cands.push_back(100 * group + 32);
+      cands.push_back(100 * group + 34);
+    }
+  } else {
+    cands = {2, 1};
+    if (group) cands.push_back(100 * group);
+  }
+  auto launch_prod = [&](int v, cudaStream_t ss) {
+    if (k == 1) {
+      switch (v) {
+        case 41: k_sg_spmm<1, 4, 1><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        case 22: k_sg_spmm<1, 2, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        case 82: k_sg_spmm<1, 8, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        case 232: k_sg_spmv_grpb<2, 2, 4><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        case 234: k_sg_spmv_grpb<2, 4, 4><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        case 332: k_sg_spmv_grpb<3, 2, 4><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        case 334: k_sg_spmv_grpb<3, 4, 4><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+        default: k_sg_spmm<1, 4, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl); break;
+      }
+    } else if (v == 200) {
+      PG_KSWITCH(k, (k_sg_spmm_grp<K, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
+    } else if (v == 300) {
+      PG_KSWITCH(k, (k_sg_spmm_grp<K, 3><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
+    } else if (v == 1) {
+      PG_KSWITCH(k, (k_sg_spmm<K, 1, 1><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
+    } else {
+      PG_KSWITCH(k, (k_sg_spmm<K, 1, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
+    }
+  };
+  int variant = cands[0];
   Plan Pf{P.n, P.nnz, k, 1, 0, 1, sizeof(double2), BjInfo{}};
   const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
   auto true_residual = [&]() { launch_spmv<double2>(Pf, rowptr, col, A, x, r64, b, nullptr, npr, s); };
@@ -577,10 +738,7 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   bool first = true;
   const double delta = 1e-3;
   auto one_iteration = [&](cudaStream_t ss) {
-    if (k == 1)
-      k_sg_spmm<1, 4, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl);
-    else
-      PG_KSWITCH(k, (k_sg_spmm<K, 1, 2><<<G, kThreads, 0, ss>>>(rowptr, col, At, g, pv, q, part, st, ctl)));
+    launch_prod(variant, ss);
     PG_KSWITCH(k, (k_sg_update<K><<<G, kThreads, 0, ss>>>(y, r, pv, q, wdf, g, st, part, part2, ctl, delta),
                    k_sg_pupdate<K><<<G, kThreads, 0, ss>>>(pv, r, g, st, ctl)));
   };
@@ -694,6 +852,19 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
       }
     PG_KSWITCH(k, (k_sg_start<K><<<G, kThreads, 0, s>>>(bj ? r64b : r64, Sd, g, r, y, pv, first ? 1 : 0, part),
                    k_sg_cycle_init<K><<<1, kThreads, 0, s>>>(part, g, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    if (first) {
+      // PG_SPMV_VARIANT forces a candidate; else the fastest on these operands
+      const char* fv = getenv("PG_SPMV_VARIANT");
+      int forced = -1;
+      if (fv && fv[0])
+        for (int c : cands)
+          if (c == atoi(fv)) forced = c;
+      if (forced >= 0) variant = forced;
+      else if (autotune_enabled()) variant = pick_fastest(cands, [&](int v) { launch_prod(v, s); }, s);
+      PG_LAUNCH_CHECK();
+      if (monitor) fprintf(stderr, "pg_cocg_segments: SpMV variant %d for n=%lld nnz=%lld k=%d\n", variant,
+                           (long long)P.n, (long long)P.nnz, k);
+    }
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
     int done = 0;

@@ -90,3 +90,26 @@ def test_segments_converged_system_stays_put():
     assert torch.count_nonzero(xs[1]).item() == 0
     assert info.its_per_rhs[1][0] == 0
     assert _true_relres(m1, A1, xs[0], b1)[0] <= 1.01e-9
+
+
+@pytest.mark.parametrize("k,variant", [(1, 42), (1, 41), (1, 22), (1, 82), (1, 232), (1, 234), (4, 2), (4, 1),
+                                       (4, 200)])
+def test_segments_product_variants_agree(k, variant, monkeypatch, capfd):
+    """Every product shape of the several-systems solve (rows, entity groups
+    with batched loads, several RHS) reaches the same solutions; the monitor
+    shows the forced shape ran."""
+    from petgem_gb300.engine import solve_csr_segments
+    systems = [_system(n, seed=j + 1, k=k) for j, n in enumerate((4, 3))]
+    blocks = (2, [(m.nE, m.nF, m.T) for m, _, _ in systems])
+    sysl = [(m.rowptr, m.col, A, b) for m, A, b in systems]
+    monkeypatch.setenv("PG_KSP_MONITOR", "1")
+    monkeypatch.setenv("PG_SPMV_VARIANT", str(variant))
+    xs, info = solve_csr_segments(sysl, blocks=blocks, rtol=1e-10)
+    assert f"SpMV variant {variant} " in capfd.readouterr().err
+    monkeypatch.setenv("PG_SPMV_VARIANT", "42" if k == 1 else "2")
+    x0, i0 = solve_csr_segments(sysl, blocks=blocks, rtol=1e-10)
+    assert info.status == 0 and i0.status == 0
+    for j, (m, A, b) in enumerate(systems):
+        x = xs[j] if k > 1 else xs[j].reshape(-1)
+        assert max(_true_relres(m, A, x, b)) <= 1.01e-10
+        assert rel_norm(xs[j].cpu().numpy(), x0[j].cpu().numpy()) < 1e-7
