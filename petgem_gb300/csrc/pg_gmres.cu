@@ -1,14 +1,15 @@
 // Restarted GMRES for petgem's complex system A x = b (petgem/solver.py:584-594,
-// PETSc KSP with -ksp_type gmres -pc_type jacobi), for one or several
-// right-hand sides at once.
+// PETSc KSP with -ksp_type gmres and -pc_type jacobi or bjacobi), for one or
+// several right-hand sides at once.
 //
 // Structure (same code for both precisions, templated on the Arnoldi scalar):
 //   loop over restarts:
 //     r = b - A x                    complex128 CSR SpMV/SpMM with the original A
 //     stop when ||r|| <= rtol ||b|| for every RHS (true residual, FP64)
-//     one Arnoldi cycle of m steps on  Ahat = A D^-1  (right Jacobi), in the
-//     Arnoldi precision: complex128 ("fp64") or complex64 ("mixed")
-//     x += D^-1 V y                  FP64 update
+//     one Arnoldi cycle of m steps on  Ahat = A M^-1  (right preconditioning:
+//     M = D, or the entity blocks A_aa), in the Arnoldi precision:
+//     complex128 ("fp64") or complex64 ("mixed")
+//     x += M^-1 V y                  FP64 update
 // In the mixed form every restart is an FP64 iterative-refinement step around
 // a complex64 GMRES(m) cycle; in the plain form both parts are complex128.
 //
