@@ -502,6 +502,57 @@ __global__ void __launch_bounds__(kThreads) k_df_spmm_grp(const int64_t* __restr
   if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
 }
 
+// K RHS (K >= 2): one thread per (group of R rows, pair of RHS c, c + K/2):
+// every column index and matrix value loaded serves two RHS
+template <int K, int R>
+__global__ void __launch_bounds__(kThreads) k_df_spmm_grp2(const int64_t* __restrict__ rowptr,
+                                                           const int32_t* __restrict__ col,
+                                                           const float4* __restrict__ val, int64_t n,
+                                                           const float4* __restrict__ pv, float4* __restrict__ q,
+                                                           double2* partial, CgState* st, CgCtl* ctl) {
+  static_assert(K >= 2, "two RHS per thread");
+  constexpr int H = K / 2;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int ra = threadIdx.x % H, rb = ra + H;
+  const int64_t items = (n / R) * H;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  float4 mua = make_float4(0.f, 0.f, 0.f, 0.f), mub = mua;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += stride) {
+    const int64_t r0 = (it / H) * R;
+    int64_t off[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+    const int64_t len = rowptr[r0 + 1] - off[0];
+    float4 acca[R], accb[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acca[i] = accb[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t k = 0; k < len; ++k) {
+      const int64_t c = col[off[0] + k];
+      const float4 xa = pv[c * K + ra], xb = pv[c * K + rb];
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const float4 v = val[off[i] + k];
+        cdf_mac(acca[i], v, xa);
+        cdf_mac(accb[i], v, xb);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float4 a = df_norm(acca[i]), b = df_norm(accb[i]);
+      q[(r0 + i) * K + ra] = a;
+      q[(r0 + i) * K + rb] = b;
+      cdf_mac(mua, pv[(r0 + i) * K + ra], a);
+      cdf_mac(mub, pv[(r0 + i) * K + rb], b);
+    }
+  }
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  block_reduce_df<H>(mua, smf, partial + (int64_t)blockIdx.x * K);
+  block_reduce_df<H>(mub, smf, partial + (int64_t)blockIdx.x * K + H);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
+}
+
 // ---- SpMV variant autotuner ------------------------------------------------
 // The double-float product's best lanes-per-row / unrolling depends on the
 // matrix (rows, stored entries per row) and the RHS count.  At the first
@@ -540,7 +591,7 @@ int forced_variant(int k, int group) {
     if (group && (gv == 2 || gv == 4 || gv == 8 || gv == 12 || gv == 14 || gv == 32 || gv == 34)) return v;
   } else {
     if (v == 1 || v == 2) return v;
-    if (group && v == 100 * group) return v;
+    if (group && (v == 100 * group || v == 100 * group + 50)) return v;
   }
   return -1;
 }
@@ -549,8 +600,8 @@ int forced_variant(int k, int group) {
 // single RHS: variant = lanes per row G (1..8) * 10 + unroll U, or
 // 100 R + 10 (U - 1) + G for the product over groups of R rows with G lanes
 // per group and unroll U, 100 R + 30 + G for the group product with 4 column
-// steps batched;
-// several RHS: unroll 1 or 2, or 100 R for the group product
+// steps batched; several RHS: unroll 1 or 2, 100 R for the group product, or
+// 100 R + 50 for the group product with two RHS per thread
 void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
                      const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st,
                      CgCtl* ctl) {
@@ -581,7 +632,11 @@ void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowpt
 template <int K>
 void launch_df_spmm(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
                     const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st, CgCtl* ctl) {
-  if (variant == 200)
+  if (K >= 2 && variant == 250)
+    k_df_spmm_grp2<(K >= 2 ? K : 2), 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else if (K >= 2 && variant == 350)
+    k_df_spmm_grp2<(K >= 2 ? K : 2), 3><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else if (variant == 200)
     k_df_spmm_grp<K, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
   else if (variant == 300)
     k_df_spmm_grp<K, 3><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
@@ -865,7 +920,10 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
             variant = pick_fastest(cands, [&](int v) { launch_single(v, s); }, s);
           } else {
             std::vector<int> cands = {1, 2};
-            if (group) cands.push_back(100 * group);
+            if (group) {
+              cands.push_back(100 * group);
+              cands.push_back(100 * group + 50);
+            }
             variant = pick_fastest(cands, [&](int v) {
               PG_KSWITCH(k, (launch_df_spmm<K>(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl)));
             }, s);

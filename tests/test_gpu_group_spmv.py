@@ -32,7 +32,7 @@ def _system(p, k):
 @pytest.mark.parametrize("p,k,variant", [(2, 1, 202), (2, 1, 204), (2, 1, 208), (2, 1, 212), (2, 1, 214),
                                          (2, 1, 232), (2, 1, 234), (2, 1, 42), (3, 1, 304), (3, 1, 314),
                                          (3, 1, 302), (3, 1, 332), (3, 1, 334), (2, 4, 200), (2, 4, 2),
-                                         (3, 8, 300)])
+                                         (3, 8, 300), (2, 4, 250), (2, 16, 250), (3, 8, 350)])
 def test_df64_product_variants_agree(p, k, variant, monkeypatch, capfd):
     m, A, b = _system(p, k)
     rtol = 1e-10
