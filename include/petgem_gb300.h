@@ -480,7 +480,8 @@ typedef struct pg_cocg_opts {
    * faces and block_volumes elements at order block_p (DOFs numbered entity by
    * entity); each entity's diagonal block is factored L D L^T and the solver
    * runs on S A S^T, S = D^-1/2 L^-1 (blocks above 12 DOFs stay diagonal).
-   * Not used by pg_cocg_multifreq. */
+   * Not used by pg_cocg_multifreq; pg_cocg_segments takes block_p from here
+   * and each system's entity counts from its seg_entities argument. */
   int block_p;
   int64_t block_edges, block_faces, block_volumes;
 } pg_cocg_opts;

@@ -1,9 +1,10 @@
 """Oracle: scipy stand-ins for the PETSc KSP solve (petgem/solver.py:584-594).
 
 Test infrastructure only (see ``oracle/__init__.py``).  PETSc is third-party
-and absent; the reference configures ``-ksp_type gmres -pc_type jacobi
--ksp_rtol 1e-8``, restated here with scipy's GMRES and a Jacobi
-preconditioner, and a direct solve for tight golden solutions.
+and absent; the benchmark's solve is ``-ksp_type gmres -pc_type jacobi
+-ksp_rtol 1e-8`` (petgem's examples use ``-pc_type sor``), restated here with
+scipy's GMRES and a Jacobi preconditioner, and a direct solve for tight
+golden solutions.
 """
 import numpy as np
 import scipy.sparse as sp
