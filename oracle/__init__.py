@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the shipped package imports this
 package: only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg
-of ``bench.py`` may use it, and only as the checker (or as the timed CPU
-baseline), never as the implementation being measured.
+of ``bench.py`` may use it, and only as the reference results that outputs
+are compared with (or as the timed CPU baseline), never as the
+implementation being measured.
 
 The oracle is a plain numpy/scipy restatement of the reference algorithms,
 function by function, each citing the petgem file:line it follows:

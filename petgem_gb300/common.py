@@ -256,8 +256,8 @@ class InputParameters:
 
 def parse_petsc_options(argv_or_path):
     """KSP options of the subset petgem's options files use (-ksp_type,
-    -ksp_rtol, -ksp_max_it, -ksp_gmres_restart, -pc_type) plus this build's
-    -pg_precision {fp64,mixed} and -pg_nrhs.  Accepts an options file path or
+    -ksp_rtol, -ksp_max_it, -ksp_gmres_restart, -pc_type) plus this library's
+    -pg_precision {fp64,mixed,df64} and -pg_nrhs.  Accepts an options file path or
     an argv list containing -options_file."""
     tokens = []
     if isinstance(argv_or_path, str):
