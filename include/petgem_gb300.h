@@ -526,6 +526,13 @@ int pg_cocg_segments(const int64_t* rowptr, const int32_t* col, const double* va
                      const int64_t* seg_rows, int n_seg, const int64_t* seg_entities, const double* b, double* x,
                      int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result, double* relres, int64_t* its,
                      void* workspace, size_t workspace_bytes, void* stream);
+/* Host-only inspection helper, no petgem counterpart: the block map
+ * pg_cocg_segments launches with (host arrays).  blk[j] .. blk[j+1]-1 are the
+ * blocks of system j: with active == NULL the first map (blocks in
+ * proportion to rows, at least one each); else the map after a residual
+ * check with active[j] != 0 for the systems still iterating (same total, one
+ * block per converged system). */
+int pg_segments_block_map(const int64_t* seg_rows, int n_seg, int nrhs, const unsigned char* active, int* blk);
 
 
 #ifdef __cplusplus

@@ -969,3 +969,26 @@ extern "C" int pg_cocg_segments(const int64_t* rowptr, const int32_t* col, const
                       reinterpret_cast<const double2*>(b), reinterpret_cast<double2*>(x), opts, result, relres, its,
                       ws, pg_stream(stream));
 }
+
+extern "C" int pg_segments_block_map(const int64_t* seg_rows, int n_seg, int nrhs, const unsigned char* active,
+                                     int* blk) {
+  if (!seg_rows || !blk || n_seg < 1 || !valid_k(nrhs) || seg_rows[0] != 0) {
+    pg_set_error("pg_segments_block_map: bad argument");
+    return PG_ERR_ARG;
+  }
+  for (int j = 0; j < n_seg; ++j)
+    if (seg_rows[j + 1] < seg_rows[j]) {
+      pg_set_error("pg_segments_block_map: seg_rows must not fall");
+      return PG_ERR_ARG;
+    }
+  std::vector<int> b = seg_blocks(seg_rows, n_seg, nrhs);
+  if (active) {
+    std::vector<char> act(n_seg);
+    for (int j = 0; j < n_seg; ++j) act[j] = active[j] ? 1 : 0;
+    std::vector<int> r;
+    seg_rebalance(seg_rows, n_seg, nrhs, act, b[n_seg], r);
+    b = r;
+  }
+  for (int j = 0; j <= n_seg; ++j) blk[j] = b[j];
+  return PG_OK;
+}

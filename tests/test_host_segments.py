@@ -45,3 +45,63 @@ def test_batched_workload_meshes_and_sources():
     xs = np.array([s["position"][0] for s in srcs])
     # every source lies inside the [-1000, 1000] m box of the two-layer meshes
     assert np.all(np.abs(xs) <= 1000.0) and np.all(np.diff(xs) > 0)
+
+
+def _block_map(rows, k, active=None):
+    import ctypes
+    from petgem_gb300 import _lib
+    lib = _lib.load()
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    S = rows.size - 1
+    blk = np.zeros(S + 1, dtype=np.int32)
+    act = None if active is None else np.ascontiguousarray(active, dtype=np.uint8)
+    st = lib.pg_segments_block_map(ctypes.c_void_p(rows.ctypes.data), S, k,
+                                   ctypes.c_void_p(0 if act is None else act.ctypes.data),
+                                   ctypes.c_void_p(blk.ctypes.data))
+    assert st == 0
+    return blk
+
+
+def test_segment_block_map_invariants():
+    """The launch's block map (host code of pg_cocg_segments): every system
+    holds at least one block, shares follow the rows, and the re-split after
+    a residual check keeps the grid size, gives converged systems one block
+    and hands the rest to the systems still iterating."""
+    rng = np.random.default_rng(0)
+    for trial in range(300):
+        S = int(rng.integers(1, 40))
+        k = int(rng.choice([1, 2, 4, 8, 16, 32]))
+        sizes = rng.integers(0, 2_000_000 if trial % 2 else 300, S)
+        rows = np.concatenate([[0], np.cumsum(sizes)])
+        if rows[-1] == 0:
+            continue
+        blk = _block_map(rows, k)
+        counts = np.diff(blk)
+        assert blk[0] == 0 and counts.min() >= 1
+        total = int(blk[-1])
+        act = rng.random(S) < 0.5
+        r = _block_map(rows, k, act)
+        rc = np.diff(r)
+        assert r[0] == 0 and int(r[-1]) == total and rc.min() >= 1
+        if act.any() and (~act).any():
+            assert np.all(rc[~act] == 1)
+        # no system gets more blocks than it has (row, rhs) items to spread over, except the largest active one
+        cap = np.maximum((sizes * k + 255) // 256, 1)
+        big = np.argmax(np.where(act, sizes, -1)) if act.any() else S - 1
+        over = np.nonzero(rc > cap)[0]
+        assert set(over.tolist()) <= {int(big)}
+    # proportional shares on a large, even case
+    rows = np.array([0, 1_000_000, 3_000_000], dtype=np.int64)
+    c = np.diff(_block_map(rows, 1))
+    assert abs(c[1] / c[0] - 2.0) < 0.01
+
+
+def test_segment_block_map_rejects_bad_rows():
+    import ctypes
+    from petgem_gb300 import _lib
+    lib = _lib.load()
+    rows = np.array([0, 10, 5], dtype=np.int64)
+    blk = np.zeros(3, dtype=np.int32)
+    st = lib.pg_segments_block_map(ctypes.c_void_p(rows.ctypes.data), 2, 1, ctypes.c_void_p(0),
+                                   ctypes.c_void_p(blk.ctypes.data))
+    assert st == -1
