@@ -511,6 +511,24 @@ class DeviceMesh:
         return y
 
 
+def _check_csr(name, rowptr, col, vals, b):
+    """CSR system on the GPU: rowptr int64 [N+1], col int32 [nnz], vals
+    complex128 [nnz], b complex128 [N] or [N, k]; raises ValueError before
+    anything reaches the library."""
+    if rowptr.dtype != torch.int64 or col.dtype != torch.int32:
+        raise ValueError(f"{name}: rowptr must be int64 and col int32 (got {rowptr.dtype}, {col.dtype})")
+    if vals.dtype != torch.complex128 or b.dtype != torch.complex128:
+        raise ValueError(f"{name}: vals and b must be complex128 (got {vals.dtype}, {b.dtype})")
+    if rowptr.ndim != 1 or col.ndim != 1 or vals.ndim != 1 or b.ndim not in (1, 2):
+        raise ValueError(f"{name}: rowptr, col, vals must be 1-D and b [N] or [N, k]")
+    if col.numel() != vals.numel() or b.shape[0] != rowptr.numel() - 1:
+        raise ValueError(f"{name}: sizes disagree (rows {rowptr.numel() - 1}, b {tuple(b.shape)}, "
+                         f"col {col.numel()}, vals {vals.numel()})")
+    devs = {t.device for t in (rowptr, col, vals, b)}
+    if len(devs) != 1 or next(iter(devs)).type != "cuda":
+        raise ValueError(f"{name}: every array must be on the same CUDA device (got {sorted(map(str, devs))})")
+
+
 def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
               raise_on_fail=True, ksp="gmres", check_every=50, blocks=None):
     """Solve A x = b for a CSR matrix on the GPU (rowptr int64 [N+1], col
@@ -529,6 +547,7 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     block, right preconditioning: PETSc -pc_type bjacobi with one block per
     edge / face / element).
     """
+    _check_csr(f"solve_csr({ksp})", rowptr, col, vals, b)
     N = int(rowptr.numel()) - 1
     nnz = int(col.numel())
     nrhs = 1 if b.ndim == 1 else int(b.shape[1])
@@ -573,10 +592,11 @@ def solve_csr_frequencies(rowptr, col, vals0, b, col_scale, x0=None, rtol=1e-8, 
     [N, k], k in 1,2,4,8,16,32) is solved with (Re A0 + i s_j Im A0), where
     vals0 = A0 = K - i omega_0 mu M (PEC applied) and s_j = omega_j / omega_0.
     One matrix read per iteration serves every column."""
-    N = int(rowptr.numel()) - 1
-    nnz = int(col.numel())
     if b.ndim != 2:
         raise ValueError("b must be [N, k]")
+    _check_csr("solve_csr_frequencies", rowptr, col, vals0, b)
+    N = int(rowptr.numel()) - 1
+    nnz = int(col.numel())
     k = int(b.shape[1])
     sc = np.ascontiguousarray(np.asarray(col_scale, dtype=np.float64).reshape(-1))
     if sc.size != k:
@@ -630,6 +650,8 @@ def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_
     with info.relres_per_rhs and info.its_per_rhs per (system, rhs)."""
     if not systems:
         raise ValueError("no systems")
+    for j, (rp, c, v, bj) in enumerate(systems):
+        _check_csr(f"solve_csr_segments(system {j})", rp, c, v, bj)
     ks = {1 if b.ndim == 1 else int(b.shape[1]) for _, _, _, b in systems}
     if len(ks) != 1:
         raise ValueError("every system needs the same number of right-hand sides")

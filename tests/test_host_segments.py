@@ -105,3 +105,26 @@ def test_segment_block_map_rejects_bad_rows():
     st = lib.pg_segments_block_map(ctypes.c_void_p(rows.ctypes.data), 2, 1, ctypes.c_void_p(0),
                                    ctypes.c_void_p(blk.ctypes.data))
     assert st == -1
+
+
+def test_csr_solvers_reject_bad_arrays_before_the_library():
+    """dtype, shape and device checks of the CSR solve entry points run on the
+    host and raise ValueError (no device needed)."""
+    import pytest
+    from petgem_gb300.engine import solve_csr, solve_csr_frequencies, solve_csr_segments
+    rp = torch.tensor([0, 1, 2], dtype=torch.int64)
+    col = torch.tensor([0, 1], dtype=torch.int32)
+    vals = torch.ones(2, dtype=torch.complex128)
+    b = torch.ones(2, dtype=torch.complex128)
+    with pytest.raises(ValueError, match="CUDA device"):
+        solve_csr(rp, col, vals, b)                          # host tensors
+    with pytest.raises(ValueError, match="int64"):
+        solve_csr(rp.to(torch.int32), col, vals, b)
+    with pytest.raises(ValueError, match="complex128"):
+        solve_csr(rp, col, vals.to(torch.complex64), b, ksp="cocg")
+    with pytest.raises(ValueError, match="sizes disagree"):
+        solve_csr(rp, col, vals, torch.ones(3, dtype=torch.complex128))
+    with pytest.raises(ValueError, match="CUDA device"):
+        solve_csr_frequencies(rp, col, vals, b.reshape(2, 1), [1.0])
+    with pytest.raises(ValueError, match=r"system 0\): rowptr must be int64"):
+        solve_csr_segments([(rp, col.to(torch.int64), vals, b), (rp, col, vals, b)])
