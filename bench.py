@@ -43,6 +43,12 @@ def workload(n):
     return WORKLOAD if n == 32 else f"csem_p2_{n}cubed_jittered_logsigma ({6 * n ** 3:,} tets)"
 
 
+def workload_config(n, tets, dofs, nnz):
+    """`config` of both arms (the same keys and values for the same workload)."""
+    return {"workload": workload(n), "p": 2, "tets": int(tets), "dofs": int(dofs), "nnz": int(nnz),
+            "l2": "working set per step > 129 MB L2 (A values alone 16 B x nnz)"}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -55,12 +61,14 @@ def parse():
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of a baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--assembly", default="df64", choices=["df64", "fp64"],
-                    help="arithmetic of the fused assembly (df64: double-float on the FP32 pipes)")
-    ap.add_argument("--config", type=int, default=1, choices=[1, 2, 3, 4],
-                    help="1: the metric's workload (default); 2: the batched workload (12 systems x 16 RHS in one "
-                         "solve); 3: the adjoint gradient (24^3) with a finite-difference check; 4: the MT "
-                         "configuration (p=3, 40^3): assembly and MT right-hand side timing only")
+    ap.add_argument("--assembly", default="fp64", choices=["df64", "fp64"],
+                    help="arithmetic of the headline assembly (fp64, the reference's arithmetic; df64: "
+                         "double-float on the FP32 pipes, reported beside it as assembly_df64)")
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4],
+                    help="1: the metric's workload (default); 0: plain FP64 CSEM p=1 16^3 with petgem's "
+                         "GMRES(30)+Jacobi, checked against the oracle; 2: the batched workload (12 systems x 16 RHS "
+                         "in one solve); 3: the adjoint gradient (24^3) with finite-difference checks; 4: the MT "
+                         "configuration (p=3, 40^3)")
     ap.add_argument("--no-records", action="store_true",
                     help="assemble from the item list instead of the per-mesh assembly records")
     ap.add_argument("--solve-iters", type=int, default=0,
@@ -88,7 +96,29 @@ def cpu_prepare(model):
     fE = topology.compute_faces_edges(eF, eE, fN.shape[0])
     eo, fo = topology.element_orientation(tets, eE, eN, eF, fE)
     dofs, _, _, _, N = topology.compute_connectivity_dofs(eE, eF, model.p)
-    return {"coords": model.nodes[tets], "eo": eo, "fo": fo, "dofs": dofs, "N": N}
+    return {"coords": model.nodes[tets], "eo": eo, "fo": fo, "dofs": dofs, "N": N,
+            "nnz": pattern_nnz(eE, eF, model.p)}
+
+
+def pattern_nnz(elemsE, elemsF, p):
+    """Stored entries of A before PEC: every pair of mesh entities (edge,
+    face, volume) that share an element couples all their DOFs."""
+    T = elemsE.shape[0]
+    nE, nF = int(elemsE.max()) + 1, int(elemsF.max()) + 1
+    ents = [elemsE.astype(np.int64), nE + elemsF.astype(np.int64)]
+    nd = [np.full(6, p), np.full(4, p * (p - 1))]
+    if p >= 3:
+        ents.append((nE + nF + np.arange(T, dtype=np.int64))[:, None])
+        nd.append(np.array([p * (p - 1) * (p - 2) // 2]))
+    ent = np.concatenate(ents, axis=1)
+    ndof = np.concatenate(nd)
+    keep = ndof > 0
+    ent, ndof = ent[:, keep], ndof[keep]
+    n_ent = nE + nF + T
+    keys = (ent[:, :, None] * n_ent + ent[:, None, :]).reshape(-1)
+    w = (ndof[:, None] * ndof[None, :]).reshape(-1)
+    uk, first = np.unique(keys, return_index=True)
+    return int(np.tile(w, T)[first].sum())
 
 
 def cpu_assembly_rate(model, seconds, cores, prep=None, pool=None):
@@ -280,13 +310,13 @@ def run_gpu(args, rank, world, local_rank):
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     launches_per_step = 4   # coefficients, fused assembly + PEC rows/columns, source, PEC on b
 
-    def assemble(v=None):
-        mesh.assemble(sigma, freq, out=vals if v is None else v, coef=coef, arithmetic=args.assembly, pec=True,
-                      records=not args.no_records)
+    def assemble(v=None, ar=None, cf=None):
+        mesh.assemble(sigma, freq, out=vals if v is None else v, coef=coef if cf is None else cf,
+                      arithmetic=ar or args.assembly, pec=True, records=not args.no_records)
 
     side = torch.cuda.Stream()
 
-    def step(v=None, bv=None):
+    def step(v=None, bv=None, ar=None, cf=None):
         # the RHS (zero, point dipole, PEC rows of b) runs on a second stream
         # beside the matrix pass; the step ends when both have finished
         bv = b if bv is None else bv
@@ -296,8 +326,9 @@ def run_gpu(args, rank, world, local_rank):
             bv.zero_()
             mesh.source_rhs(model.source, src_elem, bv, status=status)
             mesh.pec_rhs(bv)
-        mesh.element_coefficients(sigma, freq, out=coef, check=False, arithmetic=args.assembly)
-        assemble(v)
+        mesh.element_coefficients(sigma, freq, out=coef if cf is None else cf, check=False,
+                                  arithmetic=ar or args.assembly)
+        assemble(v, ar, cf)
         main.wait_stream(side)
 
     for _ in range(args.warmup):
@@ -360,6 +391,48 @@ def run_gpu(args, rank, world, local_rank):
                     "traffic": read_traffic("assembly_records_fp64_p2_ncu.md" if not args.no_records else None),
                     "algorithmic_flops_per_launch": flops, "ms_per_launch": round(k_ms, 4),
                     "algorithmic_bytes_per_launch": nbytes}
+
+    # the double-float form beside the FP64 headline: same step, (hi, lo)
+    # FP32-pair products on the FP32 pipes; its dominant kernel is bound by
+    # load traffic, so its roofline is the HBM copy rate
+    assembly_df64 = None
+    if not df and not args.no_records:
+        mesh.tables_entry_major("df64")
+        coef_df = torch.empty((T, 12, 2), dtype=torch.float32, device="cuda")
+        vals_df = torch.empty_like(vals)
+        for _ in range(args.warmup):
+            step(vals_df, None, "df64", coef_df)
+        barrier()
+        e0.record()
+        for _ in range(args.steps):
+            step(vals_df, None, "df64", coef_df)
+        e1.record()
+        barrier()
+        ms_df = e0.elapsed_time(e1) / args.steps
+        k0.record()
+        for _ in range(args.steps):
+            assemble(vals_df, "df64", coef_df)
+        k1.record()
+        torch.cuda.synchronize()
+        kdf = k0.elapsed_time(k1) / args.steps
+        hbm = measured_hbm()
+        ach = nbytes / (kdf * 1e-3) / 1e9
+        # entrywise against the FP64 values, relative to each row's largest entry
+        rowmax = torch.zeros(mesh.N, dtype=torch.float64, device="cuda")
+        rows = torch.repeat_interleave(torch.arange(mesh.N, device="cuda"), mesh.rowptr[1:] - mesh.rowptr[:-1])
+        rowmax.scatter_reduce_(0, rows, vals.abs(), reduce="amax")
+        dev_rel = float(((vals_df - vals).abs() / rowmax[rows]).max())
+        del rows, rowmax
+        assembly_df64 = {"Melem_per_s": round(world * T / (ms_df * 1e-3) / 1e6, 3), "ms_per_step": round(ms_df, 4),
+                         "dtype": "df64 (f32 pairs) -> f64",
+                         "kernel": "k_values_rec<2, df> (fused elemental + CSR assembly + PEC, double-float)",
+                         "ms_per_launch": round(kdf, 4),
+                         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm[0], "unit": "GB/s",
+                                      "frac": round(ach / hbm[0], 4), "peak_source": hbm[1],
+                                      "traffic": read_traffic("assembly_records_df64_p2_ncu.md"),
+                                      "algorithmic_bytes_per_launch": nbytes},
+                         "max_entry_dev_vs_fp64_over_row_max": dev_rel}
+        del vals_df, coef_df
 
     # end to end: host buffers in (pinned), A values and b back to the host.
     # Two device / host buffer pairs: the read-back of step k (host link,
@@ -426,14 +499,13 @@ def run_gpu(args, rank, world, local_rank):
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Melem/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
-                "higher_is_better": True, "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if not df else "df64 (f32 pairs) -> f64", "data": "synthetic (seeded Kuhn-cube mesh, jittered; log-uniform sigma)",
-                "config": {"workload": workload(args.n), "p": 2, "tets": T, "dofs": mesh.N, "nnz": mesh.nnz,
-                           "parallelism": "replicas" if world > 1 else "single GPU",
-                           "l2": "working set per step > 1 GB (A values alone 876 MB) > 129 MB L2",
-                           "pattern_setup_ms": round(setup_ms, 1), "orientation_tuples": mesh.n_tuples},
+                "config": workload_config(args.n, T, mesh.N, mesh.nnz),
+                "setup": {"parallelism": "replicas" if world > 1 else "single GPU",
+                          "pattern_setup_ms": round(setup_ms, 1), "orientation_tuples": mesh.n_tuples},
                 "roofline": roofline, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
-                "clocks": clk.summary(), "solve": solve}
+                "clocks": clk.summary(), "assembly_df64": assembly_df64, "solve": solve}
         if cpu_solve is not None:
             if solve and "fp64_diagonal_jacobi" in solve:
                 n_it = solve["fp64_diagonal_jacobi"]["iterations"]
@@ -591,10 +663,126 @@ def run_reference(args, rank):
               f"elements per step, {cores} processes")
     return {"metric": METRIC, "value": round(v, 6), "unit": "Melem/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": {"workload": workload(args.n), "p": 2},
+            "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.n, len(model.tets), prep["N"], prep["nnz"]),
             "cpu_baseline": {"value": round(v, 6), "unit": "Melem/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 6), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_config0(args):
+    """Plain FP64 CSEM, Nedelec p = 1: 16^3 cubes x 6 tets (24,576 tets,
+    31,024 DOFs), seawater 3.3 / sediment 1.0 S/m with a 0.01 S/m block,
+    x-HED at (0,0,50) m, 1 Hz, 20 receivers on z = 0.  Times the FP64
+    assembly (coefficients + fused elemental/CSR assembly + PEC) and petgem's
+    own KSP, restarted GMRES(30) with Jacobi in complex128, to a 1e-8 true
+    relative residual (ms per RHS).  The CPU leg builds the same system with
+    the oracle (petgem's elemental loop and COO assembly restated), times
+    scipy's GMRES(30) + Jacobi on it (the PETSc KSP stand-in), and checks the
+    GPU's matrix, right-hand side and receiver fields against it and against
+    a direct solve."""
+    import torch
+    from petgem_gb300 import synthetic
+    from petgem_gb300.engine import DeviceMesh
+    model = synthetic.config0()
+    f = model.source["frequency"]
+    pool = None
+    if not args.no_cpu_baseline:                     # spawn workers before the first GPU call
+        pool = mp.get_context("spawn").Pool(os.cpu_count() or 1)
+    t0 = time.time()
+    mesh = DeviceMesh(model.nodes, model.tets, 1)
+    mesh.records()
+    mesh.tables_entry_major("fp64")
+    torch.cuda.synchronize()
+    setup_ms = (time.time() - t0) * 1e3
+    sigma = mesh.sigma_tensor(model.sigma)
+    coef = torch.empty((mesh.T, 12), dtype=torch.float64, device="cuda")
+    vals = torch.empty(mesh.nnz, dtype=torch.complex128, device="cuda")
+
+    def step():
+        mesh.element_coefficients(sigma, f, out=coef, check=False)
+        mesh.assemble(sigma, f, out=vals, coef=coef, pec=True)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(args.steps, 1)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    asm_ms = e0.elapsed_time(e1) / steps
+    b, _ = mesh.source_vector(model.source)
+    mesh.pec_rhs(b)
+
+    def solve(ksp, precond, prec="fp64"):
+        mesh.solve(vals, b, rtol=1e-8, ksp=ksp, precond=precond, precision=prec, max_it=60, raise_on_fail=False)
+        torch.cuda.synchronize()                     # warm-up: workspace, autotuning
+        t = time.time()
+        x, info = mesh.solve(vals, b, rtol=1e-8, ksp=ksp, precond=precond, precision=prec, restart=30,
+                             max_it=args.max_it, raise_on_fail=False)
+        torch.cuda.synchronize()
+        dt = time.time() - t
+        F, _ = mesh.receiver_fields(x, model.receivers, f)
+        return x, F, {"ksp": ksp, "precond": precond, "precision": prec, "ms_per_rhs": round(dt * 1e3, 2),
+                      "iterations": info.iterations, "relres": info.relres, "converged": info.status == 0}
+    x, F, gm = solve("gmres", "jacobi")
+    gm["restart"] = 30
+    others = {}
+    for name, ksp, pc, prec in (("cocg_fp64_block", "cocg", "block", "fp64"),
+                                ("cocg_df64_block", "cocg", "block", "df64"),
+                                ("gmres30_fp64_block", "gmres", "block", "fp64")):
+        _, Fo, r = solve(ksp, pc, prec)
+        r["receiver_E_rel_diff_vs_gmres"] = float(torch.linalg.norm(Fo[:, :3] - F[:, :3]) /
+                                                  torch.linalg.norm(F[:, :3]))
+        others[name] = r
+    cpu = None
+    if pool is not None:
+        from oracle import solve as osolve
+        from oracle import system
+        try:
+            t = time.time()
+            S = system.csem_system(model.nodes, model.tets, model.sigma, 1, model.source, pool=pool)
+            t_asm = time.time() - t
+        finally:
+            pool.close()
+            pool.join()
+        A = S["A"]
+        rp, cl = mesh.rowptr.cpu().numpy(), mesh.col.cpu().numpy()
+        same_pattern = bool(np.array_equal(rp, A.indptr) and np.array_equal(cl, A.indices))
+        v = vals.cpu().numpy()
+        t = time.time()
+        xc, its, rel = osolve.gmres_jacobi(A, S["b"], 1e-8, 30)
+        t_gm = time.time() - t
+        xd = osolve.direct(A, S["b"])
+        Fd, _ = system.receiver_fields(S, xd, model.nodes, model.tets, 1, model.receivers, f)
+        Fc, _ = system.receiver_fields(S, xc, model.nodes, model.tets, 1, model.receivers, f)
+        Fg = F.cpu().numpy()
+        rel_e = lambda a, r: float(np.linalg.norm(a[:, :3] - r[:, :3]) / np.linalg.norm(r[:, :3]))
+        cpu = {"kind": "port", "cores": os.cpu_count() or 1,
+               "sample": "the whole system: oracle elemental matrices (all cores) + COO assembly + PEC, then "
+                         "scipy GMRES(30) + Jacobi (PETSc KSP stand-in, one core)",
+               "assembly_seconds": round(t_asm, 3), "gmres_ms_per_rhs": round(t_gm * 1e3, 1),
+               "gmres_iterations": its, "gmres_relres": rel,
+               "check": {"pattern_bit_exact": same_pattern,
+                         "values_rel_diff": float(np.linalg.norm(v - A.data) / np.linalg.norm(A.data))
+                         if same_pattern else None,
+                         "b_rel_diff": float(np.linalg.norm(b.cpu().numpy() - S["b"]) / np.linalg.norm(S["b"])),
+                         "gpu_receiver_E_rel_err_vs_oracle_direct": rel_e(Fg, Fd),
+                         "gpu_receiver_EH_rel_err_vs_oracle_direct": float(np.linalg.norm(Fg - Fd) /
+                                                                           np.linalg.norm(Fd)),
+                         "cpu_gmres_receiver_E_rel_err_vs_oracle_direct": rel_e(Fc, Fd)}}
+    return {"metric": "ms/RHS to 1e-8 residual, plain FP64 GMRES(30)+Jacobi (p=1 CSEM)", "value": gm["ms_per_rhs"],
+            "unit": "ms/RHS", "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 3),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Kuhn-cube mesh, two layers and a resistive block)",
+            "config": {"workload": "csem_p1_16cubed_two_layer_block (24,576 tets, 31,024 DOFs)", "p": 1,
+                       "tets": mesh.T, "dofs": mesh.N, "nnz": mesh.nnz, "receivers": len(model.receivers)},
+            "setup_ms": round(setup_ms, 1),
+            "assembly": {"ms_per_step": round(asm_ms, 4), "Melem_per_s": round(mesh.T / asm_ms / 1e3, 2),
+                         "arithmetic": "fp64"},
+            "solve": gm, "other_solvers": others, "cpu_baseline": cpu}
 
 
 def run_config3(args):
@@ -653,6 +841,16 @@ def run_config3(args):
         return (tight.evaluate(mp)[0].item() - tight.evaluate(mm)[0].item()) / (2 * h)
     fd_rnd = np.array([fd(int(e)) for e in rnd])
     fd_top = np.array([fd(int(e)) for e in top])
+    # directional derivative along a seeded random direction over all
+    # elements: grad . v against (phi(m + h v) - phi(m - h v)) / 2h
+    v = torch.as_tensor(np.random.default_rng(8).standard_normal(mesh.T), device="cuda")
+    dphi = float(torch.dot(g_t, v))
+    directional = {"direction": "v ~ N(0, 1) per element, seed 8", "grad_dot_v": dphi}
+    for hd in (1e-4, 1e-5):
+        fdd = (tight.evaluate(m + hd * v)[0].item() - tight.evaluate(m - hd * v)[0].item()) / (2 * hd)
+        directional[f"rel_err_h{hd:g}"] = abs(fdd - dphi) / abs(dphi)
+    directional["passed_1e-5"] = bool(min(directional["rel_err_h0.0001"], directional["rel_err_h1e-05"]) <= 1e-5)
+    out["directional_check"] = directional
     err_rnd = float(np.linalg.norm(fd_rnd - g_np[rnd]) / np.linalg.norm(g_np[rnd]))
     err_top = float(np.max(np.abs(fd_top - g_np[top]) / np.abs(g_np[top])))
     gmax = float(np.max(np.abs(g_np)))
@@ -843,6 +1041,10 @@ def run_config2(args):
 
 def main():
     args = parse()
+    if args.config == 0:
+        if int(os.environ.get("RANK", 0)) == 0:
+            print(json.dumps(run_config0(args)), flush=True)
+        return
     if args.config == 2:
         if int(os.environ.get("RANK", 0)) == 0:
             print(json.dumps(run_config2(args)), flush=True)

@@ -167,7 +167,9 @@ int pg_select_equal(const int32_t* values, int64_t n, int32_t target, int32_t* o
  * up the array's device address with that device current; make that first
  * call before any stream capture.  All calls share the one array: calls that
  * overlap on the GPU (concurrent streams, or several host threads) race and
- * must be serialised by the caller. */
+ * must be serialised by the caller.  The looked-up address is kept for the
+ * life of the process; after cudaDeviceReset of a device, do not call this
+ * function on that device again. */
 #define PG_NOALLOC_MAX_N 262144
 int64_t pg_select_equal_noalloc_max_n(void);
 int pg_select_equal_noalloc(const int32_t* values, int64_t n, int32_t target, int32_t* out, int64_t* count,

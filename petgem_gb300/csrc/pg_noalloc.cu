@@ -18,20 +18,20 @@
 
 namespace {
 
-// Scratch layout of pg_select_equal for n entries: flags + positions
-// (int32 each, 256-byte aligned) + scan partials + a 512-byte tail.
-constexpr size_t align256c(size_t b) { return (b + 255) & ~(size_t)255; }
-constexpr size_t select_bytes(int64_t n) {
-  return align256c(sizeof(int32_t) * (size_t)n) * 2 + align256c(sizeof(int64_t) * (size_t)((n + 2047) / 2048)) +
-         512;
-}
+// Sized by the same compile-time formula that pg_select_workspace_bytes
+// returns, so the two cannot drift apart.
 constexpr int64_t kMaxN = PG_NOALLOC_MAX_N;
-constexpr size_t kScratchBytes = select_bytes(kMaxN);
+constexpr size_t kScratchBytes = pg::select_workspace_bytes_for(kMaxN);
+static_assert(kScratchBytes % 256 == 0 && kScratchBytes < ((size_t)4 << 20),
+              "the static scratch should stay a modest, 256-byte multiple");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // Device address of g_noalloc_scratch, looked up once per device with that
 // device current (the host-side symbol is a stand-in, not a device address).
+// The cached address belongs to the device's primary context: after
+// cudaDeviceReset it is stale, so a process that resets a device must not
+// call pg_select_equal_noalloc on that device again.
 constexpr int kMaxDevices = 64;
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;

@@ -8,7 +8,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;  // keys per block per pass
-constexpr int kScanChunk = 2048;          // elements per block in scans
+// kScanChunk (elements per block in scans) is declared in pg_sort.cuh
 
 template <typename T>
 __global__ void k_reduce_chunks(const T* in, int64_t n, T* partial) {
@@ -158,10 +158,7 @@ __global__ void k_scatter(const uint64_t* __restrict__ kin, const int32_t* __res
 
 }  // namespace
 
-size_t scan_workspace_bytes(int64_t n) {
-  const int64_t nb = (n + kScanChunk - 1) / kScanChunk;
-  return pg_align256(sizeof(int64_t) * (nb > 0 ? nb : 1));
-}
+size_t scan_workspace_bytes(int64_t n) { return scan_workspace_bytes_for(n); }
 
 int scan_exclusive_i32(const int32_t* in, int32_t* out, int64_t n, int32_t* total, void* ws, size_t ws_bytes,
                        cudaStream_t s) {

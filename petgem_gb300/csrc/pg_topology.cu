@@ -424,9 +424,7 @@ extern "C" int pg_flag_edges_of_pairs(const int32_t* edgesNodes, int64_t nE, con
   return PG_OK;
 }
 
-extern "C" size_t pg_select_workspace_bytes(int64_t n) {
-  return pg_align256(sizeof(int32_t) * n) * 2 + pg::scan_workspace_bytes(n) + 512;
-}
+extern "C" size_t pg_select_workspace_bytes(int64_t n) { return pg::select_workspace_bytes_for(n); }
 
 extern "C" int pg_select_equal(const int32_t* values, int64_t n, int32_t target, int32_t* out, int64_t* count,
                                void* workspace, size_t workspace_bytes, void* stream) {

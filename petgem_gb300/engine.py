@@ -524,9 +524,24 @@ def _check_csr(name, rowptr, col, vals, b):
     if col.numel() != vals.numel() or b.shape[0] != rowptr.numel() - 1:
         raise ValueError(f"{name}: sizes disagree (rows {rowptr.numel() - 1}, b {tuple(b.shape)}, "
                          f"col {col.numel()}, vals {vals.numel()})")
+    # the library reads rowptr, col and vals through their data pointers
+    for nm, t in (("rowptr", rowptr), ("col", col), ("vals", vals)):
+        if not t.is_contiguous():
+            raise ValueError(f"{name}: {nm} must be contiguous")
     devs = {t.device for t in (rowptr, col, vals, b)}
     if len(devs) != 1 or next(iter(devs)).type != "cuda":
         raise ValueError(f"{name}: every array must be on the same CUDA device (got {sorted(map(str, devs))})")
+
+
+def _new_x(name, b, x0):
+    """The solution buffer: row-major [N] or [N, k] like b (the kernels write
+    x through its data pointer), zero or a contiguous copy of x0."""
+    if x0 is None:
+        return torch.zeros(tuple(b.shape), dtype=b.dtype, device=b.device)
+    if tuple(x0.shape) != tuple(b.shape) or x0.dtype != b.dtype or x0.device != b.device:
+        raise ValueError(f"{name}: x0 must match b (shape {tuple(b.shape)}, {b.dtype}, {b.device}); got "
+                         f"{tuple(x0.shape)}, {x0.dtype}, {x0.device}")
+    return x0.contiguous().clone()
 
 
 def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
@@ -551,7 +566,7 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     N = int(rowptr.numel()) - 1
     nnz = int(col.numel())
     nrhs = 1 if b.ndim == 1 else int(b.shape[1])
-    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    x = _new_x(f"solve_csr({ksp})", b, x0)
     prec = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
     if prec == 2 and ksp != "cocg":
         raise ValueError("precision='df64' is implemented for ksp='cocg'")
@@ -601,7 +616,7 @@ def solve_csr_frequencies(rowptr, col, vals0, b, col_scale, x0=None, rtol=1e-8, 
     sc = np.ascontiguousarray(np.asarray(col_scale, dtype=np.float64).reshape(-1))
     if sc.size != k:
         raise ValueError("one frequency scale per column")
-    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    x = _new_x("solve_csr_frequencies", b, x0)
     lib = _lib.load()
     o = _lib.CocgOpts()
     lib.pg_cocg_default_opts(ctypes.byref(o))
@@ -675,7 +690,7 @@ def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_
     if nbytes == 0:
         raise ValueError("pg_cocg_segments: bad systems (empty, k not 1..32, or block counts not matching rows)")
     ws = _ws(nbytes + 256, b.device)
-    x = torch.zeros_like(b)
+    x = _new_x("solve_csr_segments", b, None)
     res = _lib.GmresResult()
     rr = np.zeros(S * k, dtype=np.float64)
     its = np.zeros(S * k, dtype=np.int64)

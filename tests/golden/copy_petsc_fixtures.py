@@ -3,7 +3,7 @@ vector-b.dat, vector-x.dat: the system petgem's tests/test_petsc.py solves
 with KSP, x being the zero initial guess) into tests/golden/ under
 petgem_*.dat names, unchanged.
 
-    python tests/golden/copy_petsc_fixtures.py --ref /root/reference
+    python tests/golden/copy_petsc_fixtures.py --ref <petgem checkout>   (or PETGEM_REF=<petgem checkout>)
 """
 import argparse
 import os
@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PETGEM_REF"), required="PETGEM_REF" not in os.environ,
+                    help="path of a petgem source checkout (default: $PETGEM_REF)")
     args = ap.parse_args()
     for name in ("matrix-A.dat", "vector-b.dat", "vector-x.dat"):
         src = os.path.join(args.ref, "tests", "data", name)

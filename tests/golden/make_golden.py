@@ -2,7 +2,7 @@
 
 Run in the build container, where the petgem sources are available:
 
-    python tests/golden/make_golden.py --ref /root/reference
+    python tests/golden/make_golden.py --ref <petgem checkout>   (or PETGEM_REF=<petgem checkout>)
 
 petgem needs petsc4py, mpi4py, PyYAML, colorama, singleton_decorator, h5py
 and meshio at import time; none of them is used by the functions called
@@ -149,7 +149,8 @@ def source_ref(hvfem, points, tets, topo, dofs, p, src, ndof):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PETGEM_REF"), required="PETGEM_REF" not in os.environ,
+                    help="path of a petgem source checkout (default: $PETGEM_REF)")
     args = ap.parse_args()
     hvfem, mesh = shim(args.ref)
     from petgem_gb300 import gmsh, synthetic

@@ -3,7 +3,7 @@ petgem's own functions in the order of its MT assembly branch.
 
 Run in the build container, where the petgem sources are available:
 
-    python tests/golden/make_mt_golden.py --ref /root/reference
+    python tests/golden/make_mt_golden.py --ref <petgem checkout>   (or PETGEM_REF=<petgem checkout>)
 
 petgem's MT right-hand side is built inside Solver.assembly
 (petgem/solver.py:318-512), which needs PETSc objects; here the same
@@ -111,7 +111,8 @@ def reference_mt_rhs(hvfem, mesh, mt1d, nodes, tets, sigma, p, freq, pols=(1, 2)
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PETGEM_REF"), required="PETGEM_REF" not in os.environ,
+                    help="path of a petgem source checkout (default: $PETGEM_REF)")
     args = ap.parse_args()
     hvfem, mesh = shim(args.ref)
     from petgem import mt1d

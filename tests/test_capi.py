@@ -42,6 +42,20 @@ def test_host_queries():
     assert o.restart == 30 and abs(o.rtol - 1e-8) < 1e-20 and o.precision == 0
 
 
+def test_noalloc_limit_matches_header_and_select_workspace():
+    """The allocation-free select's limit is the header's PG_NOALLOC_MAX_N,
+    and the workspace formula its static scratch is sized by is the one
+    pg_select_workspace_bytes reports (one compile-time function in
+    csrc/pg_sort.cuh): 2 int32 arrays + one int64 partial per 2,048 + 512."""
+    lib = _lib.load()
+    m = re.search(r"#define\s+PG_NOALLOC_MAX_N\s+(\d+)", open(HEADER).read())
+    n = int(m.group(1))
+    assert _lib.query("pg_select_equal_noalloc_max_n") == n
+    a256 = lambda b: (b + 255) // 256 * 256
+    for k in (1, 2047, 2048, 2049, 100_000, n):
+        assert _lib.query("pg_select_workspace_bytes", k) == 2 * a256(4 * k) + a256(8 * max(1, -(-k // 2048))) + 512
+
+
 def test_library_is_in_tree():
     assert os.path.dirname(_lib.library_path()) == os.path.dirname(os.path.abspath(_build.__file__))
 

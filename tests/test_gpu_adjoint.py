@@ -52,6 +52,20 @@ def test_gradient_vs_gpu_finite_differences():
         assert abs(fd - grad[e].item()) <= 1e-5 * abs(grad).max().item()
 
 
+def test_directional_derivative_over_all_elements():
+    """grad . v against central differences of phi along a seeded random
+    direction v that moves every element at once (a check whose size does
+    not depend on which elements happen to be picked)."""
+    g, mesh, prob = _setup(rtol=1e-12)
+    m0 = torch.tensor(g["m0"], dtype=torch.float64, device=mesh.device)
+    _, grad = prob.value_and_gradient(m0)
+    v = torch.as_tensor(np.random.default_rng(8).standard_normal(mesh.T), device=mesh.device)
+    dphi = float(torch.dot(grad, v))
+    for h in (1e-4, 1e-5):
+        fd = (prob.evaluate(m0 + h * v)[0] - prob.evaluate(m0 - h * v)[0]).item() / (2 * h)
+        assert abs(fd - dphi) <= 1e-5 * abs(dphi), (h, fd, dphi)
+
+
 def test_receiver_adjoint_is_the_transpose_of_the_gather():
     g, mesh, prob = _setup()
     rng = np.random.default_rng(11)

@@ -128,3 +128,25 @@ def test_csr_solvers_reject_bad_arrays_before_the_library():
         solve_csr_frequencies(rp, col, vals, b.reshape(2, 1), [1.0])
     with pytest.raises(ValueError, match=r"system 0\): rowptr must be int64"):
         solve_csr_segments([(rp, col.to(torch.int64), vals, b), (rp, col, vals, b)])
+
+
+def test_csr_solvers_need_contiguous_arrays_and_a_row_major_solution():
+    """The library reads rowptr / col / vals and writes x through their data
+    pointers: strided inputs are rejected, and the solution buffer is
+    row-major even when b is a transposed view."""
+    import pytest
+    from petgem_gb300.engine import _new_x, solve_csr
+    rp = torch.tensor([0, 1, 2], dtype=torch.int64)
+    col = torch.tensor([0, 1], dtype=torch.int32)
+    vals = torch.ones(4, dtype=torch.complex128)[::2]          # strided view
+    b = torch.ones(2, dtype=torch.complex128)
+    with pytest.raises(ValueError, match="vals must be contiguous"):
+        solve_csr(rp, col, vals, b)
+    bt = torch.arange(8, dtype=torch.float64).to(torch.complex128).reshape(4, 2).t()   # [2, 4], not row-major
+    assert not bt.is_contiguous()
+    x = _new_x("t", bt, None)
+    assert x.shape == bt.shape and x.is_contiguous() and bool((x == 0).all())
+    x = _new_x("t", bt, bt)
+    assert x.is_contiguous() and torch.equal(x, bt)
+    with pytest.raises(ValueError, match="x0 must match b"):
+        _new_x("t", bt, torch.zeros(4, 2, dtype=torch.complex128))
