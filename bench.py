@@ -552,11 +552,15 @@ def run_solves(args, torch, mesh, model, vals, b):
         torch.cuda.synchronize()
         dt = time.time() - t
         k = 1 if rhs.ndim == 1 else rhs.shape[1]
-        return x, {"ksp": ksp, "precision": prec, "precond": precond, "nrhs": k,
-                   "seconds": round(dt, 3),
-                   "ms_per_rhs": round(dt * 1e3 / k, 2), "iterations": info.iterations,
-                   "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4),
-                   "relres": info.relres, "converged": info.status == 0}
+        out = {"ksp": ksp, "precision": prec, "precond": precond, "nrhs": k,
+               "seconds": round(dt, 3),
+               "ms_per_rhs": round(dt * 1e3 / k, 2), "iterations": info.iterations,
+               "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4),
+               "relres": info.relres, "converged": info.status == 0}
+        if prec == "ir32":
+            out["refinement_steps"] = info.restarts
+            out["iterations_are"] = "complex64 inner iterations (max over RHS)"
+        return x, out
 
     # column 0: the workload's own HED; columns 1..: x-HEDs of the batched configuration
     srcs = [model.source] + synthetic.config2_sources(count=args.nrhs - 1)
@@ -572,6 +576,9 @@ def run_solves(args, torch, mesh, model, vals, b):
     _, r64j = timed("cocg", "fp64", b, args.max_it, precond="jacobi")
     xdf, rdf = timed("cocg", "df64", b, args.max_it)
     Xdb, rdb = timed("cocg", "df64", B.contiguous(), args.max_it)
+    # complex64 inner solves + FP64 iterative refinement (one RHS, then the 16-RHS batch)
+    xir, rir = timed("cocg", "ir32", b, 4 * args.max_it)
+    Xib, rib = timed("cocg", "ir32", B.contiguous(), 4 * args.max_it)
     # several frequencies in one solve: 4 frequencies x 8 sources (32 columns)
     freqs = [0.25, 0.5, 1.0, 2.0]
     f0 = model.source["frequency"]
@@ -606,7 +613,8 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["reference_solve"] = {"rtol": 1e-10, "iterations": it_.iterations, "relres": it_.relres, "status": it_.status}
     Ft, _ = mesh.receiver_fields(xt, model.receivers, model.source["frequency"])
     j1 = fcol.index(f0)      # the workspace source at the workload frequency
-    for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf)):
+    for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf),
+                 (xir, rir), (Xib[:, 0].contiguous(), rib)):
         F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
         r["receiver_rel_err_vs_fp64_1e-10"] = float(torch.linalg.norm(F - Ft) / torch.linalg.norm(Ft))
     out["fp64"] = r64
@@ -615,10 +623,15 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["df64_batched"] = rdb
     out["mixed"] = rmx
     out["df64_multifrequency"] = rmf
+    out["ir32"] = rir
+    out["ir32_batched"] = rib
     out["gmres30_mixed_300its"] = rg
-    out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; mixed = complex64 "
-                   "matrix/SpMV + FP64 recurrence, which cannot reach 1e-8 at this conditioning (eps32*kappa ~ 1)")
+    out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; ir32 = complex64 "
+                   "inner COCG solves (matrix, vectors, products in FP32), each restarted from the FP64 true residual, "
+                   "inside FP64 iterative refinement; mixed = complex64 matrix/SpMV + FP64 recurrence with reliable "
+                   "updates, which stalls at this conditioning (capped)")
     out["speedup_df64_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rdb["ms_per_rhs"], 1e-9), 2)
+    out["speedup_ir32_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rib["ms_per_rhs"], 1e-9), 2)
 
     return out
 
@@ -629,6 +642,7 @@ def profile_solves(args, torch, mesh, vals, b):
     B = torch.stack([b] * args.nrhs, 1).contiguous()
     for name, ksp, prec, rhs in (("cocg_fp64", "cocg", "fp64", b), ("cocg_df64", "cocg", "df64", b),
                                  ("cocg_df64_batched", "cocg", "df64", B), ("cocg_mixed", "cocg", "mixed", b),
+                                 ("cocg_ir32", "cocg", "ir32", b), ("cocg_ir32_batched", "cocg", "ir32", B),
                                  ("cocg_mixed_batched", "cocg", "mixed", B), ("gmres_mixed", "gmres", "mixed", b),
                                  ("gmres_fp64", "gmres", "fp64", b)):
         torch.cuda.synchronize()

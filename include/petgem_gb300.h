@@ -470,8 +470,12 @@ int pg_gmres(const int64_t* rowptr, const int32_t* col, const double* vals, int6
  * precision 0: complex128 throughout; 1: complex64 matrix and SpMV with a
  * complex128 recurrence and FP64 reliable updates; 2 ("df64"): matrix and
  * recurrence in double-float (FP32 hi + lo pairs, ~48-bit mantissa) computed
- * on the FP32 pipes, FP64 reliable updates.  The true FP64 residual is checked every check_every
- * iterations (doubling up to 400) and decides convergence. */
+ * on the FP32 pipes, FP64 reliable updates; 3 ("ir32"): FP64 iterative
+ * refinement of the true residual around complex64 inner COCG solves (matrix,
+ * vectors and products all complex64), each restarted from the current FP64
+ * residual and run until its residual estimate has dropped by inner_rtol.
+ * The true FP64 residual is checked every check_every iterations (doubling up
+ * to 400; for precision 3 at every refinement step) and decides convergence. */
 typedef struct pg_cocg_opts {
   int max_it;
   double rtol;
@@ -486,6 +490,9 @@ typedef struct pg_cocg_opts {
    * and each system's entity counts from its seg_entities argument. */
   int block_p;
   int64_t block_edges, block_faces, block_volumes;
+  /* precision 3: relative residual reduction each complex64 inner solve aims
+   * for (0 or outside (0, 1): 1e-2) */
+  double inner_rtol;
 } pg_cocg_opts;
 
 void pg_cocg_default_opts(pg_cocg_opts* opts);

@@ -33,7 +33,7 @@ class CocgOpts(ctypes.Structure):
     """pg_cocg_opts (include/petgem_gb300.h)."""
     _fields_ = [("max_it", ctypes.c_int), ("rtol", ctypes.c_double), ("precision", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("block_p", ctypes.c_int), ("block_edges", ctypes.c_int64),
-                ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64)]
+                ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64), ("inner_rtol", ctypes.c_double)]
 
 
 _PO = ctypes.POINTER(GmresOpts)

@@ -456,7 +456,9 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
 }  // namespace
 
 using pgk::df_layout;
+using pgk::ir_layout;
 using pgk::run_cocg_df;
+using pgk::run_cocg_ir;
 extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
   if (!o) return;
   memset(o, 0, sizeof(*o));
@@ -464,12 +466,14 @@ extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
   o->rtol = 1e-8;
   o->precision = 0;
   o->check_every = 50;
+  o->inner_rtol = 1e-2;
 }
 
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = cg_plan(n, nnz, nrhs, opts);
   size_t off[20];
+  if (opts->precision == 3) return ir_layout(P, off) + 256;
   return (opts->precision == 2 ? df_layout(P, off) : cg_layout(P, off)) + 256;
 }
 
@@ -477,8 +481,8 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
                        const double* b, double* x, int nrhs, const pg_cocg_opts* opts, pg_gmres_result* result,
                        double* relres_per_rhs, void* workspace, size_t workspace_bytes, void* stream) {
   if (!opts || !rowptr || !col || !vals || !b || !x || n < 1 || nnz < n || !valid_k(nrhs) || !(opts->rtol > 0.0) ||
-      opts->precision < 0 || opts->precision > 2) {
-    pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1/2)");
+      opts->precision < 0 || opts->precision > 3) {
+    pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1/2/3)");
     return PG_ERR_ARG;
   }
   if (opts->block_p > 0) {
@@ -504,6 +508,7 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
   double2* xx = reinterpret_cast<double2*>(x);
   if (P.prec == 0) return run_cocg<double2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
   if (P.prec == 2) return run_cocg_df(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
+  if (P.prec == 3) return run_cocg_ir(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
   return run_cocg<float2>(P, rowptr, col, A, bb, xx, opts, result, relres_per_rhs, ws, s);
 }
 

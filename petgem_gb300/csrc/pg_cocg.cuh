@@ -407,4 +407,10 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
                 const double* col_scale = nullptr);
 
+// workspace layout and driver of the complex64-inner / FP64-refinement COCG
+size_t ir_layout(const Plan& P, size_t* off /* 16 */);
+int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b,
+                double2* x, const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws,
+                cudaStream_t s);
+
 }  // namespace pgk

@@ -395,9 +395,11 @@ __global__ void __launch_bounds__(kThreads) k_df_spmv_grp(const int64_t* __restr
 
 // one RHS, G lanes per group of R rows; each lane issues the column, value
 // and p loads of B column steps back to back before using them, so a warp
-// keeps B times more bytes in flight than one step at a time
-template <int R, int G, int B>
-__global__ void __launch_bounds__(kThreads) k_df_spmv_grpb(const int64_t* __restrict__ rowptr,
+// keeps B times more bytes in flight than one step at a time.  MB > 1 asks
+// the compiler for MB resident blocks per SM (fewer registers per thread,
+// more warps to hide the p gathers).
+template <int R, int G, int B, int MB = 1>
+__global__ void __launch_bounds__(kThreads, MB) k_df_spmv_grpb(const int64_t* __restrict__ rowptr,
                                                            const int32_t* __restrict__ col,
                                                            const float4* __restrict__ val, int64_t n,
                                                            const float4* __restrict__ pv, float4* __restrict__ q,
@@ -588,7 +590,9 @@ int forced_variant(int k, int group) {
   if (k == 1) {
     if (v == 21 || v == 22 || v == 41 || v == 42 || v == 81 || v == 82) return v;
     const int gv = v - 100 * group;
-    if (group && (gv == 2 || gv == 4 || gv == 8 || gv == 12 || gv == 14 || gv == 32 || gv == 34)) return v;
+    if (group && (gv == 2 || gv == 4 || gv == 8 || gv == 12 || gv == 14 || gv == 32 || gv == 34 || gv == 44 ||
+                  gv == 54))
+      return v;
   } else {
     if (v == 1 || v == 2) return v;
     if (group && (v == 100 * group || v == 100 * group + 50)) return v;
@@ -600,7 +604,8 @@ int forced_variant(int k, int group) {
 // single RHS: variant = lanes per row G (1..8) * 10 + unroll U, or
 // 100 R + 10 (U - 1) + G for the product over groups of R rows with G lanes
 // per group and unroll U, 100 R + 30 + G for the group product with 4 column
-// steps batched; several RHS: unroll 1 or 2, 100 R for the group product, or
+// steps batched, 100 R + 44 / 100 R + 54 for that product with 4 / 3 column
+// steps and a register budget of 4 resident blocks per SM; several RHS: unroll 1 or 2, 100 R for the group product, or
 // 100 R + 50 for the group product with two RHS per thread
 void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col,
                      const float4* At, int64_t n, const float4* pv, float4* q, double2* part, CgState* st,
@@ -615,6 +620,10 @@ void launch_df_spmv1(int variant, int grid, cudaStream_t s, const int64_t* rowpt
     case 212: k_df_spmv_grp<2, 2, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 232: k_df_spmv_grpb<2, 2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 234: k_df_spmv_grpb<2, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 244: k_df_spmv_grpb<2, 4, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 254: k_df_spmv_grpb<2, 4, 3, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 344: k_df_spmv_grpb<3, 4, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 354: k_df_spmv_grpb<3, 4, 3, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 332: k_df_spmv_grpb<3, 2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 334: k_df_spmv_grpb<3, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
     case 214: k_df_spmv_grp<2, 4, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
@@ -916,7 +925,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
           if (k == 1) {
             std::vector<int> cands = {41, 42, 22, 82, 21};
             if (group)
-              for (int gv : {2, 4, 8, 12, 14, 32, 34}) cands.push_back(100 * group + gv);
+              for (int gv : {2, 4, 8, 12, 14, 32, 34, 44, 54}) cands.push_back(100 * group + gv);
             variant = pick_fastest(cands, [&](int v) { launch_single(v, s); }, s);
           } else {
             std::vector<int> cands = {1, 2};

@@ -1,0 +1,707 @@
+// COCG with complex64 inner solves and FP64 iterative refinement
+// (pg_cocg precision 3, "ir32").
+//
+// Outer loop, FP64: r = b - A x with the complex128 matrix, the convergence
+// test ||r_j|| <= rtol ||b_j|| per column, and the update x += c_j S^T y_j.
+// Inner solve, complex64 throughout: the scaled matrix At = S A S^T (Jacobi or
+// entity block-Jacobi, rounded once to complex64), the vectors p, q, r, y and
+// the products and vector updates all run in FP32 on the FP32 pipes; only the
+// block partial sums of the dot products are carried in double.  Each inner
+// solve starts from the current true residual, scaled to unit norm per column
+// (c_j = ||r_j||), with p = r (a restart: the FP32 Krylov space is rebuilt on
+// an exact residual every refinement step, which is what keeps an FP32
+// recurrence convergent at condition numbers where it stagnates alone), and
+// runs per column until its recurrence estimate of the residual has dropped
+// by inner_rtol (or to the final target, whichever is larger).
+//
+// Per inner iteration: product q = At p fused with mu = p^T q (alpha in the
+// last block), the vector update fused with rho = r^T r and the residual
+// estimate (beta in the last block), and the direction update; the launches
+// carry no per-iteration arguments, so runs of them are captured once in a
+// CUDA graph and replayed.  The product shape is chosen per matrix by the
+// same on-line autotuner as the double-float solver.
+#include "pg_cocg.cuh"
+
+namespace {
+
+// ---- FP32 block reductions to a double partial (lanes with equal lane % K combine)
+template <int K>
+__device__ void block_reduce_c32(float2 v, float2* smf, double2* out) {
+#pragma unroll
+  for (int off = 16; off >= K; off >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K) smf[warp * K + lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double sx = 0.0, sy = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) {
+      sx += (double)smf[w * K + threadIdx.x].x;
+      sy += (double)smf[w * K + threadIdx.x].y;
+    }
+    out[threadIdx.x] = make_double2(sx, sy);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ float2 c32_bilin_add(float2 acc, float2 a, float2 b) {   // acc + a*b
+  return cfma(a, b, acc);
+}
+
+// ---- products: q = At p (complex64), partial mu = p^T q; last block: alpha
+// one RHS, G lanes per row
+template <int G>
+__global__ void __launch_bounds__(kThreads) k_ir_spmv1(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                       const float2* __restrict__ val, int64_t n,
+                                                       const float2* __restrict__ pv, float2* __restrict__ q,
+                                                       double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;   // the previous p update has run
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float2 smf[(kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  float2 mu = make_float2(0.f, 0.f);
+  for (int64_t rw = warp_base; rw < n; rw += groups) {
+    const int64_t r = rw + (gid - warp_base);
+    const bool valid = r < n;
+    float2 acc = make_float2(0.f, 0.f);
+    if (valid) {
+      const int64_t e = rowptr[r + 1];
+      for (int64_t k = rowptr[r] + lane; k < e; k += G) acc = cfma(val[k], pv[col[k]], acc);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) acc = cadd(acc, shfl_xor(acc, off));
+    if (valid && lane == 0) {
+      q[r] = acc;
+      mu = c32_bilin_add(mu, pv[r], acc);
+    }
+  }
+  block_reduce_c32<1>(mu, smf, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
+}
+
+// one RHS over groups of R rows that share one column list (the rows of one
+// mesh entity), G lanes per group; each lane issues the loads of B column
+// steps before using them
+template <int R, int G, int B>
+__global__ void __launch_bounds__(kThreads) k_ir_spmv_grp(const int64_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col,
+                                                          const float2* __restrict__ val, int64_t n,
+                                                          const float2* __restrict__ pv, float2* __restrict__ q,
+                                                          double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float2 smf[(kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t ngroups = n / R;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  float2 mu = make_float2(0.f, 0.f);
+  for (int64_t gw = warp_base; gw < ngroups; gw += groups) {
+    const int64_t gi = gw + (gid - warp_base);
+    const bool valid = gi < ngroups;
+    float2 acc[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] = make_float2(0.f, 0.f);
+    if (valid) {
+      const int64_t r0 = gi * R;
+      int64_t off[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+      const int len = (int)(rowptr[r0 + 1] - off[0]);
+      for (int k0 = lane; k0 < len; k0 += G * B) {
+        int c[B];
+        float2 v[B][R], x[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+          const int k = k0 + j * G;
+          c[j] = k < len ? col[off[0] + k] : 0;
+#pragma unroll
+          for (int i = 0; i < R; ++i) v[j][i] = k < len ? val[off[i] + k] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) x[j] = k0 + j * G < len ? pv[c[j]] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < B; ++j)
+#pragma unroll
+          for (int i = 0; i < R; ++i) acc[i] = cfma(v[j][i], x[j], acc[i]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) acc[i] = cadd(acc[i], shfl_xor(acc[i], o));
+    if (valid && lane == 0) {
+      const int64_t r0 = gi * R;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        q[r0 + i] = acc[i];
+        mu = c32_bilin_add(mu, pv[r0 + i], acc[i]);
+      }
+    }
+  }
+  block_reduce_c32<1>(mu, smf, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
+}
+
+// K RHS (RHS fastest): one thread per (group of R rows, rhs); the K threads of
+// a group read the column index and the R matrix values once per step
+// (broadcast) and K consecutive p entries (one coalesced segment)
+template <int K, int R>
+__global__ void __launch_bounds__(kThreads) k_ir_spmm(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                                      const float2* __restrict__ val, int64_t n,
+                                                      const float2* __restrict__ pv, float2* __restrict__ q,
+                                                      double2* partial, CgState* st, CgCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->pending = 0;
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float2 smf[(kThreads / 32) * kMaxK];
+  const int rhs = threadIdx.x % K;
+  const int64_t ngroups = n / R;
+  const int64_t per_pass = ((int64_t)gridDim.x * blockDim.x) / K;
+  float2 mu = make_float2(0.f, 0.f);
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / K; g < ngroups; g += per_pass) {
+    const int64_t r0 = g * R;
+    int64_t off[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
+    const int len = (int)(rowptr[r0 + 1] - off[0]);
+    float2 acc[R], acc1[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] = acc1[i] = make_float2(0.f, 0.f);
+    int k = 0;
+    for (; k + 1 < len; k += 2) {
+      const int32_t c0 = col[off[0] + k], c1 = col[off[0] + k + 1];
+      const float2 x0 = pv[(int64_t)c0 * K + rhs], x1 = pv[(int64_t)c1 * K + rhs];
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        acc[i] = cfma(val[off[i] + k], x0, acc[i]);
+        acc1[i] = cfma(val[off[i] + k + 1], x1, acc1[i]);
+      }
+    }
+    if (k < len) {
+      const float2 x0 = pv[(int64_t)col[off[0] + k] * K + rhs];
+#pragma unroll
+      for (int i = 0; i < R; ++i) acc[i] = cfma(val[off[i] + k], x0, acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float2 a = cadd(acc[i], acc1[i]);
+      q[(r0 + i) * K + rhs] = a;
+      mu = c32_bilin_add(mu, pv[(r0 + i) * K + rhs], a);
+    }
+  }
+  block_reduce_c32<K>(mu, smf, partial + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
+}
+
+// ---- y += alpha p ; r -= alpha q ; partials rho = r^T r, w = sum |r|^2 |D|; last block: beta
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_ir_update(float2* __restrict__ y, float2* __restrict__ r,
+                                                        const float2* __restrict__ pv, const float2* __restrict__ q,
+                                                        const float* __restrict__ wd, int64_t n, CgState* st,
+                                                        double2* prho, double2* pw, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float2 al[kMaxK];
+  __shared__ float2 smf[(kThreads / 32) * kMaxK];
+  if (threadIdx.x < K) {
+    const double2 a = st[threadIdx.x].alpha;
+    al[threadIdx.x] = make_float2((float)a.x, (float)a.y);
+  }
+  __syncthreads();
+  const int rhs = threadIdx.x % K;
+  const float2 a = al[rhs];
+  const float2 na = make_float2(-a.x, -a.y);
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  float2 rho = make_float2(0.f, 0.f);
+  float ww = 0.f;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const float2 ye = cfma(a, pv[e], y[e]);
+    const float2 re = cfma(na, q[e], r[e]);
+    y[e] = ye;
+    r[e] = re;
+    rho = cfma(re, re, rho);
+    ww += (re.x * re.x + re.y * re.y) * wd[e / K];
+  }
+  block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  block_reduce_c32<K>(make_float2(ww, 0.f), smf, pw + (int64_t)blockIdx.x * K);
+  if (arrive_last(&ctl->counter)) cg_beta_final<K>(prho, pw, gridDim.x, st, ctl, 0, 0.0, smem);
+}
+
+// p = r + beta p, once per fresh beta (gated like the double-float solver)
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_ir_pupdate(float2* __restrict__ pv, const float2* __restrict__ r, int64_t n,
+                                                         const CgState* st, const CgCtl* ctl) {
+  __shared__ float2 bt[kMaxK];
+  __shared__ int use[kMaxK];
+  if (!ctl->pending) return;
+  if (threadIdx.x < K) {
+    const double2 b = st[threadIdx.x].beta;
+    bt[threadIdx.x] = make_float2((float)b.x, (float)b.y);
+    use[threadIdx.x] = st[threadIdx.x].beta_iter == 1;
+  }
+  __syncthreads();
+  int anyuse = 0;
+  for (int i = 0; i < K; ++i) anyuse |= use[i];
+  if (!anyuse) return;
+  const int64_t total = n * K;
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < total; e += (int64_t)gridDim.x * kThreads)
+    if (use[e % K]) pv[e] = cfma(bt[e % K], pv[e], r[e]);
+}
+
+// inner start: r = (S r64) / c (r64 already S-applied for block-Jacobi, sr
+// null), y = 0, p = r; partials rho = r^T r and w = sum |r|^2 |D| (double),
+// the same residual estimate the vector update forms
+template <int K>
+__global__ void k_ir_start(const double2* __restrict__ r64, const double2* __restrict__ sr, const double* cinv,
+                           const float* __restrict__ wd, int64_t n, float2* r, float2* y, float2* pv, double2* prho,
+                           double2* pw) {
+  __shared__ double2 smem[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double2 rho = make_double2(0.0, 0.0);
+  double w = 0.0;
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    double2 v = sr ? cmul(sr[e / K], r64[e]) : r64[e];
+    v = dscale(cinv[e % K], v);
+    const float2 vf = make_float2((float)v.x, (float)v.y);
+    r[e] = vf;
+    y[e] = make_float2(0.f, 0.f);
+    pv[e] = vf;
+    const double2 vd = make_double2((double)vf.x, (double)vf.y);
+    rho = dadd(rho, cmul(vd, vd));
+    w += (vd.x * vd.x + vd.y * vd.y) * (double)wd[e / K];
+  }
+  block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
+  block_reduce_rhs<K>(make_double2(w, 0.0), smem, pw + (int64_t)blockIdx.x * K);
+}
+
+// new inner solve for every column: fresh scalars, the starting residual
+// estimate res0, the target as a fraction of it; breakdown flags are cleared
+// (a restart on the exact residual is the remedy for a near-breakdown)
+template <int K>
+__global__ void k_ir_cycle_init(const double2* prho, const double2* pw, int nblocks, CgState* st,
+                                const double* target, const int* want, CgCtl* ctl, int first) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, rhs = threadIdx.x >> 5;
+  if (rhs < K) {
+    double2 rho = make_double2(0.0, 0.0);
+    double w = 0.0;
+    for (int b = lane; b < nblocks; b += 32) {
+      rho = dadd(rho, prho[(int64_t)b * K + rhs]);
+      w += pw[(int64_t)b * K + rhs].x;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      rho = dadd(rho, shfl_xor(rho, off));
+      w += __shfl_xor_sync(0xffffffffu, w, off);
+    }
+    if (lane == 0) {
+      CgState& S = st[rhs];
+      if (first) S.its = 0;
+      S.breakdown = 0;
+      S.beta_iter = 0;
+      S.rho = rho;
+      S.res0 = sqrt(w);
+      S.res = S.res0;
+      S.target = target[rhs] * S.res0;
+      S.active = want[rhs] != 0 && S.res0 > 0.0;
+      S.alpha = S.beta = make_double2(0.0, 0.0);
+      if (S.active) atomicOr(&any, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any;
+    ctl->nonfinite = 0;
+    ctl->counter = 0;
+    ctl->pending = 0;
+  }
+}
+
+// d = c y (double), per column
+template <int K>
+__global__ void k_ir_scaled_y(const float2* __restrict__ y, const double* c, int64_t n, double2* d) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    d[e] = dscale(c[e % K], make_double2((double)y[e].x, (double)y[e].y));
+}
+
+// x += S d (diagonal Jacobi: S^T = S)
+template <int K>
+__global__ void k_ir_xupdate(const double2* __restrict__ d, const double2* __restrict__ S, int64_t n, double2* x) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    x[e] = dadd(x[e], cmul(S[e / K], d[e]));
+}
+
+// At = S A S (diagonal Jacobi), rounded to complex64
+__global__ void k_ir_scale_matrix(const int64_t* rowptr, const int32_t* col, const double2* val, int64_t n,
+                                  const double2* S, float2* out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 sr = S[r];
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const double2 v = cmul(sr, cmul(val[k], S[col[k]]));
+      out[k] = make_float2((float)v.x, (float)v.y);
+    }
+  }
+}
+
+__global__ void k_ir_wd_to_f32(const double* wd, int64_t n, float* wdf) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    wdf[r] = (float)wd[r];
+}
+
+// single RHS: 10 G for the row product with G lanes per row; 100 R + G for
+// the group product (R rows per entity, G lanes, 4 column steps in flight);
+// several RHS: 0 row product, 100 R group product
+void launch_ir_spmv1(int v, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col, const float2* At,
+                     int64_t n, const float2* pv, float2* q, double2* part, CgState* st, CgCtl* ctl) {
+  switch (v) {
+    case 202: k_ir_spmv_grp<2, 2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 204: k_ir_spmv_grp<2, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 208: k_ir_spmv_grp<2, 8, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 302: k_ir_spmv_grp<3, 2, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 304: k_ir_spmv_grp<3, 4, 4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 308: k_ir_spmv_grp<3, 8, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 40: k_ir_spmv1<4><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    case 160: k_ir_spmv1<16><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+    default: k_ir_spmv1<8><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl); break;
+  }
+}
+
+template <int K>
+void launch_ir_spmm(int v, int grid, cudaStream_t s, const int64_t* rowptr, const int32_t* col, const float2* At,
+                    int64_t n, const float2* pv, float2* q, double2* part, CgState* st, CgCtl* ctl) {
+  if (v == 200)
+    k_ir_spmm<K, 2><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else if (v == 300)
+    k_ir_spmm<K, 3><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+  else
+    k_ir_spmm<K, 1><<<grid, kThreads, 0, s>>>(rowptr, col, At, n, pv, q, part, st, ctl);
+}
+
+struct IrTune {
+  int64_t n, nnz;
+  int k, group, variant;
+};
+std::vector<IrTune> g_ir_tune;
+std::mutex g_ir_tune_mu;
+
+}  // namespace
+
+namespace pgk {
+
+size_t ir_layout(const Plan& P, size_t* off /* 16 */) {
+  size_t o = 0;
+  auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
+  put(0, P.nnz * sizeof(float2));               // At (complex64)
+  put(1, sizeof(double2) * P.n);                // S (diagonal Jacobi)
+  put(2, sizeof(double) * P.n);                 // |D|
+  put(3, sizeof(float) * P.n);                  // |D| f32
+  put(4, sizeof(float2) * P.n * P.k);           // p
+  put(5, sizeof(float2) * P.n * P.k);           // q
+  put(6, sizeof(float2) * P.n * P.k);           // r
+  put(7, sizeof(float2) * P.n * P.k);           // y
+  put(8, sizeof(double2) * P.n * P.k);          // r64 (true residual)
+  put(9, sizeof(double2) * (size_t)P.nb * P.k * 3);
+  put(10, sizeof(CgState) * P.k);
+  put(11, sizeof(CgCtl));
+  put(12, sizeof(double) * P.k * 4);            // rnorm, target, c, 1/c
+  put(13, sizeof(int) * (P.k + 1));             // want, status
+  put(14, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);   // block-Jacobi factors
+  put(15, sizeof(double2) * P.n * P.k);         // S r64 (block-Jacobi) / c y
+  return o;
+}
+
+int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b,
+                double2* x, const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws,
+                cudaStream_t s) {
+  size_t off[16];
+  ir_layout(P, off);
+  const bool bj = P.bj.p > 0;
+  float2* At = reinterpret_cast<float2*>(ws + off[0]);
+  double2* S = reinterpret_cast<double2*>(ws + off[1]);
+  double* wd = reinterpret_cast<double*>(ws + off[2]);
+  float* wdf = reinterpret_cast<float*>(ws + off[3]);
+  float2* pv = reinterpret_cast<float2*>(ws + off[4]);
+  float2* q = reinterpret_cast<float2*>(ws + off[5]);
+  float2* r = reinterpret_cast<float2*>(ws + off[6]);
+  float2* y = reinterpret_cast<float2*>(ws + off[7]);
+  double2* r64 = reinterpret_cast<double2*>(ws + off[8]);
+  double2* part = reinterpret_cast<double2*>(ws + off[9]);
+  double2* part2 = part + (size_t)P.nb * P.k;
+  CgState* st = reinterpret_cast<CgState*>(ws + off[10]);
+  CgCtl* ctl = reinterpret_cast<CgCtl*>(ws + off[11]);
+  double* rnorm = reinterpret_cast<double*>(ws + off[12]);
+  double* target = rnorm + P.k;
+  double* cscale = rnorm + 2 * P.k;
+  double* cinv = rnorm + 3 * P.k;
+  int* want = reinterpret_cast<int*>(ws + off[13]);
+  int* dstatus = want + P.k;
+  double2* Sblk = reinterpret_cast<double2*>(ws + off[14]);
+  double2* aux = reinterpret_cast<double2*>(ws + off[15]);
+  const int k = P.k, nb = P.nb;
+  const int nbu = (int)std::min<int64_t>(nb, std::max<int64_t>(152 * 2, (P.n * P.k + 4 * kThreads - 1) / (4 * kThreads)));
+  const int64_t npr = P.nnz / (P.n > 0 ? P.n : 1);
+  const int spmv_grid = 152 * 16;
+  if (spmv_grid > nb) return PG_ERR_ARG;
+  const double tau = o->inner_rtol > 0.0 && o->inner_rtol < 1.0 ? o->inner_rtol : 1e-2;
+
+  PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  PG_CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(CgCtl), s));
+  int group = 0;
+  if (bj) {
+    const int st0 = bj_setup(P, rowptr, col, A, S, wd, Sblk, At, ToCM32(), dstatus, s);
+    if (st0) return st0;
+    if ((P.bj.p == 2 || P.bj.p == 3) && P.n % P.bj.p == 0) {
+      int* gflag = reinterpret_cast<int*>(part);
+      int hg = 1;
+      PG_CUDA_TRY(cudaMemsetAsync(gflag, 0, sizeof(int), s));
+      k_group_check<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, P.n, P.bj.p, gflag);
+      PG_LAUNCH_CHECK();
+      PG_CUDA_TRY(cudaMemcpyAsync(&hg, gflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaStreamSynchronize(s));
+      group = hg == 0 ? P.bj.p : 0;
+    }
+  } else {
+    k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
+    k_ir_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
+  }
+  k_ir_wd_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(wd, P.n, wdf);
+  PG_LAUNCH_CHECK();
+  std::vector<double> bnorm(k), rn(k), tgt(k), sc(4 * (size_t)k);
+  std::vector<int> wnt(k);
+  PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(b, P.n, part), k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+  PG_LAUNCH_CHECK();
+  PG_CUDA_TRY(cudaMemcpyAsync(bnorm.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  int hstatus = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&hstatus, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hstatus) {
+    pg_set_error("pg_cocg: zero diagonal entry (Jacobi scaling undefined)");
+    return PG_ERR_BREAKDOWN;
+  }
+  const char* mon_env = getenv("PG_KSP_MONITOR");
+  const bool monitor = mon_env && mon_env[0] && mon_env[0] != '0';
+  int64_t its = 0, outer = 0;
+  int status = PG_OK;
+  const int64_t max_it = o->max_it > 0 ? o->max_it : 100000;
+  int chunk = o->check_every > 0 ? o->check_every : 64;
+  bool first = true;
+  int variant = 80;
+  int stalls = 0;
+  std::vector<double> best(k, 1e300);
+  auto one_iteration = [&](cudaStream_t ss) {
+    if (k == 1)
+      launch_ir_spmv1(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl);
+    else
+      PG_KSWITCH(k, (launch_ir_spmm<K>(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+    PG_KSWITCH(k, (k_ir_update<K><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl),
+                   k_ir_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, r, P.n, st, ctl)));
+  };
+  const char* genv = getenv("PG_GRAPHS");
+  const bool use_graphs = !(genv && genv[0] == '0');
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_failed = false;
+  auto build_graph = [&]() {
+    if (graph_failed) return;
+    cudaGraph_t graph = nullptr;
+    bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      for (int g = 0; g < kGraphIters; ++g) one_iteration(cs);
+      ok = cudaStreamEndCapture(cs, &graph) == cudaSuccess && graph != nullptr;
+    }
+    if (ok) ok = cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+      cudaGetLastError();   // capture unavailable: keep launching directly
+      gexec = nullptr;
+      graph_failed = true;
+    }
+  };
+  struct GraphCleanup {
+    cudaStream_t& cs;
+    cudaEvent_t& a;
+    cudaEvent_t& b;
+    cudaGraphExec_t& g;
+    ~GraphCleanup() {
+      if (g) cudaGraphExecDestroy(g);
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      if (cs) cudaStreamDestroy(cs);
+    }
+  } graph_cleanup{cs, ev_in, ev_out, gexec};
+  auto true_residual = [&]() {
+    launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
+    PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
+                   k_norm_final<K><<<1, 32 * K, 0, s>>>(part, nb, rnorm)));
+  };
+  for (;;) {
+    true_residual();
+    PG_LAUNCH_CHECK();
+    PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    PG_CUDA_TRY(cudaStreamSynchronize(s));
+    bool all = true, progress = false;
+    for (int i = 0; i < k; ++i) {
+      if (monitor)
+        fprintf(stderr, "pg_cocg(ir32): refinement %lld inner its %lld rhs %d true ||r||/||b|| = %.6e\n",
+                (long long)outer, (long long)its, i, bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0);
+      if (!isfinite(rn[i])) {
+        pg_set_error("pg_cocg: non-finite residual");
+        status = PG_ERR_NONFINITE;
+      }
+      const double tb = o->rtol * bnorm[i];
+      const bool ok = rn[i] <= tb || bnorm[i] == 0.0;
+      wnt[i] = ok ? 0 : 1;
+      const double c = rn[i] > 0.0 && isfinite(rn[i]) ? rn[i] : 1.0;
+      sc[i] = c;
+      sc[k + i] = 1.0 / c;
+      // stop the inner solve at tau, or earlier when less is needed for rtol
+      const double need = 0.5 * tb / c;
+      tgt[i] = need > tau ? need : tau;
+      if (!ok) {
+        all = false;
+        if (rn[i] < 0.5 * best[i]) progress = true;
+      }
+      if (rn[i] < best[i]) best[i] = rn[i];
+    }
+    if (status || all) break;
+    if (its >= max_it) {
+      status = PG_ERR_NOT_CONVERGED;
+      break;
+    }
+    // three refinement steps in a row without halving any column's residual:
+    // the FP32 inner solves no longer make progress
+    stalls = (first || progress) ? 0 : stalls + 1;
+    if (stalls >= 3) {
+      pg_set_error("pg_cocg(ir32): refinement stagnated (complex64 inner solves make no progress)");
+      status = PG_ERR_BREAKDOWN;
+      break;
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    PG_CUDA_TRY(cudaMemcpyAsync(cscale, sc.data(), sizeof(double) * 2 * k, cudaMemcpyHostToDevice, s));
+    if (bj) {
+      PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, aux),
+                     k_ir_start<K><<<nb, kThreads, 0, s>>>(aux, nullptr, cinv, wdf, P.n, r, y, pv, part, part2)));
+    } else {
+      PG_KSWITCH(k, (k_ir_start<K><<<nb, kThreads, 0, s>>>(r64, S, cinv, wdf, P.n, r, y, pv, part, part2)));
+    }
+    PG_KSWITCH(k, (k_ir_cycle_init<K><<<1, 32 * K, 0, s>>>(part, part2, nb, st, target, want, ctl, first ? 1 : 0)));
+    PG_LAUNCH_CHECK();
+    if (first) {
+      const int gk = group * 1000 + k;
+      {
+        std::lock_guard<std::mutex> lock(g_ir_tune_mu);
+        variant = -1;
+        for (const IrTune& t : g_ir_tune)
+          if (t.n == P.n && t.nnz == P.nnz && t.k == k && t.group == gk) variant = t.variant;
+      }
+      if (variant < 0) {
+        std::vector<int> cands;
+        if (k == 1) {
+          cands = {80, 40, 160};
+          if (group)
+            for (int gv : {2, 4, 8}) cands.push_back(100 * group + gv);
+        } else {
+          cands = {0};
+          if (group) cands.push_back(100 * group);
+        }
+        variant = cands[0];
+        if (autotune_enabled() && cands.size() > 1) {
+          variant = pick_fastest(cands, [&](int v) {
+            if (k == 1)
+              launch_ir_spmv1(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl);
+            else
+              PG_KSWITCH(k, (launch_ir_spmm<K>(v, spmv_grid, s, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+          }, s);
+          PG_LAUNCH_CHECK();
+        }
+        std::lock_guard<std::mutex> lock(g_ir_tune_mu);
+        g_ir_tune.push_back(IrTune{P.n, P.nnz, k, gk, variant});
+      }
+      if (monitor)
+        fprintf(stderr, "pg_cocg(ir32): product variant %d for n=%lld nnz=%lld k=%d\n", variant, (long long)P.n,
+                (long long)P.nnz, k);
+    }
+    first = false;
+    // inner solve: replay chunks of iterations until every column reached its
+    // target (the kernels of a finished solve return at once)
+    for (;;) {
+      const int64_t left = max_it - its;
+      const int steps = (int)(left < chunk ? left : chunk);
+      int done = 0;
+      if (use_graphs && steps >= kGraphIters) {
+        if (!gexec) build_graph();
+        if (gexec) {
+          cudaEventRecord(ev_in, s);
+          cudaStreamWaitEvent(cs, ev_in, 0);
+          for (; done + kGraphIters <= steps; done += kGraphIters) cudaGraphLaunch(gexec, cs);
+          cudaEventRecord(ev_out, cs);
+          cudaStreamWaitEvent(s, ev_out, 0);
+        }
+      }
+      for (; done < steps; ++done) one_iteration(s);
+      PG_LAUNCH_CHECK();
+      CgCtl hctl;
+      std::vector<int> hits(k);
+      for (int i = 0; i < k; ++i)
+        PG_CUDA_TRY(cudaMemcpyAsync(&hits[i], &st[i].its, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaMemcpyAsync(&hctl, ctl, sizeof(CgCtl), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaStreamSynchronize(s));
+      int used = 0;
+      for (int i = 0; i < k; ++i) used = hits[i] > used ? hits[i] : used;
+      its = used;
+      if (hctl.nonfinite) {
+        pg_set_error("pg_cocg: non-finite residual");
+        status = PG_ERR_NONFINITE;
+        break;
+      }
+      if (!hctl.any_active || its >= max_it) break;
+      chunk = chunk < 512 ? chunk * 2 : chunk;
+    }
+    if (status) break;
+    ++outer;
+    // x += c S^T y
+    PG_KSWITCH(k, (k_ir_scaled_y<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(y, cscale, P.n, aux)));
+    if (bj) {
+      PG_KSWITCH(k, (k_bj_apply_t_add<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, aux, x, IdD2())));
+    } else {
+      PG_KSWITCH(k, (k_ir_xupdate<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(aux, S, P.n, x)));
+    }
+    PG_LAUNCH_CHECK();
+  }
+  double worst = 0.0;
+  for (int i = 0; i < k; ++i) {
+    const double rr = bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0;
+    if (relres_out) relres_out[i] = rr;
+    worst = rr > worst ? rr : worst;
+  }
+  if (res) {
+    res->iterations = its;
+    res->restarts = outer;
+    res->relres = worst;
+    res->status = status;
+  }
+  if (status == PG_ERR_NOT_CONVERGED) pg_set_error("pg_cocg: max_it reached before rtol");
+  return status;
+}
+
+}  // namespace pgk

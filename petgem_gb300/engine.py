@@ -348,14 +348,14 @@ class DeviceMesh:
         return vals, b
 
     def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True, ksp="gmres", check_every=50, precond="block"):
+              raise_on_fail=True, ksp="gmres", check_every=50, precond="block", inner_rtol=1e-2):
         """Solve A x = b for this mesh's CSR pattern (see solve_csr).
         precond="block": entity block-Jacobi (each edge / face / volume's
         diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal."""
         blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" else None
         return solve_csr(self.rowptr, self.col, vals, b, x0=x0, rtol=rtol, restart=restart, max_it=max_it,
                          precision=precision, reorth=reorth, raise_on_fail=raise_on_fail, ksp=ksp,
-                         check_every=check_every, blocks=blocks)
+                         check_every=check_every, blocks=blocks, inner_rtol=inner_rtol)
 
     def solve_frequencies(self, vals0, frequency0, b, frequencies, **kw):
         """Columns of b (complex128 [N, k]) at their own frequencies in one
@@ -545,7 +545,7 @@ def _new_x(name, b, x0):
 
 
 def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True, ksp="gmres", check_every=50, blocks=None):
+              raise_on_fail=True, ksp="gmres", check_every=50, blocks=None, inner_rtol=1e-2):
     """Solve A x = b for a CSR matrix on the GPU (rowptr int64 [N+1], col
     int32 [nnz], vals complex128 [nnz]); b complex128 [N] or [N, k]
     (k in 1,2,4,8,16,32).  The KSPSolve of petgem/solver.py:584-594.
@@ -554,7 +554,10 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
                  -pc_type jacobi, or bjacobi with blocks);
     ksp="cocg":  Jacobi-scaled COCG for complex-symmetric A.
     precision="fp64" (complex128), "mixed" (complex64 matrix/SpMV, FP64 recurrence and
-    refinement) or "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy).
+    refinement), "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy)
+    or "ir32" (COCG only: FP64 iterative refinement of the true residual around complex64 inner
+    solves, each restarted from the FP64 residual and run until its residual has dropped by
+    inner_rtol; max_it counts inner iterations, info.restarts the refinement steps).
     Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
     blocks=(p, n_edges, n_faces, n_elements): entity block-Jacobi on a pattern
     built by DeviceMesh (rows of one entity share their columns): COCG runs on
@@ -567,9 +570,9 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     nnz = int(col.numel())
     nrhs = 1 if b.ndim == 1 else int(b.shape[1])
     x = _new_x(f"solve_csr({ksp})", b, x0)
-    prec = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
-    if prec == 2 and ksp != "cocg":
-        raise ValueError("precision='df64' is implemented for ksp='cocg'")
+    prec = {"fp64": 0, "mixed": 1, "df64": 2, "ir32": 3}[precision]
+    if prec >= 2 and ksp != "cocg":
+        raise ValueError(f"precision={precision!r} is implemented for ksp='cocg'")
     res = _lib.GmresResult()
     rr = (ctypes.c_double * nrhs)()
     lib = _lib.load()
@@ -585,6 +588,7 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
         o = _lib.CocgOpts()
         lib.pg_cocg_default_opts(ctypes.byref(o))
         o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), prec, int(check_every)
+        o.inner_rtol = float(inner_rtol)
         if blocks is not None:
             o.block_p, o.block_edges, o.block_faces, o.block_volumes = (int(v) for v in blocks)
         nbytes = _lib.query("pg_cocg_workspace_bytes", N, nnz, nrhs, ctypes.byref(o))

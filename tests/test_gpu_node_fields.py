@@ -37,3 +37,19 @@ def test_node_fields_vs_oracle(p, tmp_path):
     p2, t2, fields = vtk.read(path)
     assert np.array_equal(p2, pts2) and np.array_equal(t2, tets2)
     assert np.array_equal(fields["Ex_real"], F[:, 0].real)
+
+
+def test_node_fields_vs_reference_loop_golden():
+    """pg_node_fields against petgem's own VTK nodal loop
+    (postprocessing.py:172-261; tests/golden/make_node_fields_golden.py)."""
+    from petgem_gb300.engine import DeviceMesh
+    from tests.helpers import load
+    g = load("node_fields.npz")
+    cases = [(g["n3_points"], g["n3_tets"], 2, g["n3_x"], g["n3_frequency"], g["n3_fields"])]
+    for p in (1, 3):
+        cases.append((g["tm_points"], g["tm_tets"], p, g[f"tm_p{p}_x"], g["tm_frequency"], g[f"tm_p{p}_fields"]))
+    for pts, tets, p, x, f, ref in cases:
+        m = DeviceMesh(pts, tets, p)
+        F = m.node_fields(torch.as_tensor(x, device=m.device), float(f)).cpu().numpy()
+        assert rel_norm(F[:, :3], ref[:, :3]) < 1e-12, p
+        assert rel_norm(F[:, 3:], ref[:, 3:]) < 1e-12, p

@@ -171,7 +171,7 @@ def test_assembly_df64_test_mesh_vs_oracle(p):
 
 
 @pytest.mark.parametrize("ksp,precision", [("gmres", "fp64"), ("gmres", "mixed"), ("cocg", "fp64"),
-                                           ("cocg", "mixed"), ("cocg", "df64")])
+                                           ("cocg", "mixed"), ("cocg", "df64"), ("cocg", "ir32")])
 def test_solve_and_receivers_vs_reference(precision, ksp):
     g = load("pipeline_n3.npz")
     pts, tets, sigma = g["points"], g["tets"], g["sigma"]
@@ -206,7 +206,8 @@ def test_multi_rhs_matches_single():
         bs.append(b)
     B = torch.stack(bs, 1).contiguous()
     ref = [m.solve(vals, bs[k], rtol=1e-11)[0].cpu().numpy() for k in range(4)]
-    for ksp, prec in (("gmres", "fp64"), ("gmres", "mixed"), ("cocg", "fp64"), ("cocg", "mixed"), ("cocg", "df64")):
+    for ksp, prec in (("gmres", "fp64"), ("gmres", "mixed"), ("cocg", "fp64"), ("cocg", "mixed"), ("cocg", "df64"),
+                      ("cocg", "ir32")):
         if True:
             X, info = m.solve(vals, B, rtol=1e-9, precision=prec, ksp=ksp)
             assert max(info.relres_per_rhs) <= 1e-9
@@ -255,3 +256,30 @@ def test_assembly_high_order_vs_oracle(p):
         assert np.array_equal(A.indptr, Ao.indptr) and np.array_equal(A.indices, Ao.indices)
         assert rel_norm(A.data, Ao.data) < ELEM_TOL
         assert torch.equal(v, m.assemble(sigma, 1.5, arithmetic=ar, records=False))
+
+
+@pytest.mark.parametrize("precond", ["block", "jacobi"])
+@pytest.mark.parametrize("nrhs", [1, 4])
+def test_ir32_refinement_matches_fp64(precond, nrhs):
+    """complex64 inner solves + FP64 refinement (precision "ir32") reach the
+    FP64 true-residual target and the FP64 COCG solution, p = 2, several
+    refinement steps (inner_rtol 1e-2 against rtol 1e-10)."""
+    from petgem_gb300 import synthetic
+    mdl = synthetic.config1(6)
+    m = _mesh(mdl.nodes, mdl.tets, 2)
+    vals = m.assemble(mdl.sigma, 1.0, pec=True)
+    bs = []
+    for x0 in (0.0, -400.0, 300.0, 650.0)[:nrhs]:
+        b, _ = m.source_vector(dict(mdl.source, position=[x0, 20.0, 50.0]))
+        m.pec_rhs(b)
+        bs.append(b)
+    B = bs[0] if nrhs == 1 else torch.stack(bs, 1).contiguous()
+    ref, _ = m.solve(vals, B, rtol=1e-11, ksp="cocg", precision="fp64", precond=precond, max_it=100000)
+    X, info = m.solve(vals, B, rtol=1e-10, ksp="cocg", precision="ir32", precond=precond, max_it=100000)
+    assert info.status == 0 and max(info.relres_per_rhs) <= 1e-10
+    assert info.restarts >= 3                      # several refinement steps were needed
+    A = _csr(m, vals)
+    Xn, Bn = X.cpu().numpy(), B.cpu().numpy()
+    R = A @ Xn - Bn
+    assert np.linalg.norm(R) <= 1e-10 * np.linalg.norm(Bn) * 1.01 * np.sqrt(nrhs)
+    assert rel_norm(Xn, ref.cpu().numpy()) < 1e-8

@@ -120,3 +120,27 @@ def test_pipeline_fields_match_reference():
     F, el = fem.interpolate_fields(g["x"], pts, tets, t["eo"], t["fo"], dofs, p, g["receivers"], src["frequency"])
     assert F.shape == g["fields"].shape          # the receiver outside the mesh is dropped
     assert rel_norm(F, g["fields"]) < 1e-12
+
+
+def _maps(tets, p):
+    eE, eN = topology.compute_edges(tets)
+    eF, fN = topology.compute_faces(tets)
+    fE = topology.compute_faces_edges(eF, eE, fN.shape[0])
+    eo, fo = topology.element_orientation(tets, eE, eN, eF, fE)
+    dofs, _, _, _, _ = topology.compute_connectivity_dofs(eE, eF, p)
+    return eo, fo, dofs
+
+
+def test_node_fields_match_reference_loop():
+    """oracle.fem.node_fields against petgem's own VTK nodal loop
+    (postprocessing.py:172-261, run by tests/golden/make_node_fields_golden.py)."""
+    g = load("node_fields.npz")
+    cases = [("n3", g["n3_points"], g["n3_tets"], 2, g["n3_x"], g["n3_frequency"], g["n3_fields"])]
+    for p in (1, 3):
+        cases.append((f"tm_p{p}", g["tm_points"], g["tm_tets"], p, g[f"tm_p{p}_x"], g["tm_frequency"],
+                      g[f"tm_p{p}_fields"]))
+    for name, pts, tets, p, x, f, ref in cases:
+        eo, fo, dofs = _maps(tets, p)
+        F = fem.node_fields(x, pts, tets, eo, fo, dofs, p, float(f))
+        assert rel_norm(F[:, :3], ref[:, :3]) < 1e-12, name
+        assert rel_norm(F[:, 3:], ref[:, 3:]) < 1e-12, name
