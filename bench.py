@@ -576,9 +576,17 @@ def run_solves(args, torch, mesh, model, vals, b):
     _, r64j = timed("cocg", "fp64", b, args.max_it, precond="jacobi")
     xdf, rdf = timed("cocg", "df64", b, args.max_it)
     Xdb, rdb = timed("cocg", "df64", B.contiguous(), args.max_it)
-    # complex64 inner solves + FP64 iterative refinement (one RHS, then the 16-RHS batch)
-    xir, rir = timed("cocg", "ir32", b, 4 * args.max_it)
-    Xib, rib = timed("cocg", "ir32", B.contiguous(), 4 * args.max_it)
+    # complex64 inner solves + FP64 iterative refinement (one RHS, then the
+    # 16-RHS batch); a stall would be recorded, not raised
+    from petgem_gb300 import _lib
+    def timed_ir(rhs):
+        try:
+            return timed("cocg", "ir32", rhs, 4 * args.max_it)
+        except _lib.PetgemError as exc:
+            return None, {"ksp": "cocg", "precision": "ir32", "converged": False, "status": exc.status,
+                          "error": str(exc)}
+    xir, rir = timed_ir(b)
+    Xib, rib = timed_ir(B.contiguous())
     # several frequencies in one solve: 4 frequencies x 8 sources (32 columns)
     freqs = [0.25, 0.5, 1.0, 2.0]
     f0 = model.source["frequency"]
@@ -614,7 +622,9 @@ def run_solves(args, torch, mesh, model, vals, b):
     Ft, _ = mesh.receiver_fields(xt, model.receivers, model.source["frequency"])
     j1 = fcol.index(f0)      # the workspace source at the workload frequency
     for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf),
-                 (xir, rir), (Xib[:, 0].contiguous(), rib)):
+                 (xir, rir), (None if Xib is None else Xib[:, 0].contiguous(), rib)):
+        if x is None:
+            continue
         F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
         r["receiver_rel_err_vs_fp64_1e-10"] = float(torch.linalg.norm(F - Ft) / torch.linalg.norm(Ft))
     out["fp64"] = r64
@@ -625,13 +635,14 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["df64_multifrequency"] = rmf
     out["ir32"] = rir
     out["ir32_batched"] = rib
+    if rib.get("converged"):
+        out["speedup_ir32_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rib["ms_per_rhs"], 1e-9), 2)
     out["gmres30_mixed_300its"] = rg
     out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; ir32 = complex64 "
                    "inner COCG solves (matrix, vectors, products in FP32), each restarted from the FP64 true residual, "
-                   "inside FP64 iterative refinement; mixed = complex64 matrix/SpMV + FP64 recurrence with reliable "
-                   "updates, which stalls at this conditioning (capped)")
+                   "inside FP64 iterative refinement (each inner solve to a 100x residual drop); mixed = complex64 "
+                   "matrix/SpMV + FP64 recurrence with reliable updates, which stalls at this conditioning (capped)")
     out["speedup_df64_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rdb["ms_per_rhs"], 1e-9), 2)
-    out["speedup_ir32_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rib["ms_per_rhs"], 1e-9), 2)
 
     return out
 
@@ -642,7 +653,7 @@ def profile_solves(args, torch, mesh, vals, b):
     B = torch.stack([b] * args.nrhs, 1).contiguous()
     for name, ksp, prec, rhs in (("cocg_fp64", "cocg", "fp64", b), ("cocg_df64", "cocg", "df64", b),
                                  ("cocg_df64_batched", "cocg", "df64", B), ("cocg_mixed", "cocg", "mixed", b),
-                                 ("cocg_ir32", "cocg", "ir32", b), ("cocg_ir32_batched", "cocg", "ir32", B),
+                                 ("cocg_ir32", "cocg", "ir32", b),
                                  ("cocg_mixed_batched", "cocg", "mixed", B), ("gmres_mixed", "gmres", "mixed", b),
                                  ("gmres_fp64", "gmres", "fp64", b)):
         torch.cuda.synchronize()

@@ -52,6 +52,13 @@ const char* pg_last_error(void);
 int pg_fp64_probe(double* out, int blocks, int iters, void* stream);
 int64_t pg_fp64_probe_flops(int blocks, int iters);
 
+/* Copy `bytes` from src to dst with the SMs (16-byte loads and stores; no
+ * petgem counterpart: it moves results to the host).  dst may be pinned host
+ * memory that the GPU maps (cudaHostAlloc'd memory under unified addressing),
+ * so results stream to the host without a copy engine.  blocks: grid size
+ * (0: 4 per SM).  src, dst 16-byte aligned. */
+int pg_copy_bytes(const void* src, void* dst, int64_t bytes, int blocks, void* stream);
+
 /* ------------------------------------------------------------------------
  * Reference-space integration tables
  * --------------------------------------------------------------------- */
@@ -75,7 +82,9 @@ int pg_orientation_tuples(const int8_t* eo, const int8_t* fo, int64_t n_elems,
 
 /* Tables of integrated products of reference-space shape functions and
  * curls for each tuple (the Gauss sums of petgem/hvfem.py:270-310 with the
- * element geometry factored out).  tables: f64 [n_tuples * pg_table_doubles(p)]. */
+ * element geometry factored out).  tables: f64 [n_tuples * pg_table_doubles(p)].
+ * Entries below 1e-13 of their moment's largest magnitude (analytically zero
+ * moments, e.g. curls of gradient-type edge functions) are stored as 0.0. */
 int pg_tuple_tables(const int32_t* codes, int64_t n_tuples, int p, double* tables, void* stream);
 
 /* ------------------------------------------------------------------------

@@ -46,6 +46,7 @@ SIGNATURES = {
     "pg_last_error": (ctypes.c_char_p, []),
     "pg_fp64_probe": (_INT, [_P, _INT, _INT, _P]),
     "pg_fp64_probe_flops": (_I64, [_INT, _INT]),
+    "pg_copy_bytes": (_INT, [_P, _P, _I64, _INT, _P]),
     "pg_table_doubles": (_I64, [_INT]),
     "pg_tuples_workspace_bytes": (_SZ, [_I64]),
     "pg_orientation_tuples": (_INT, [_P, _P, _I64, _P, _P, _P, _P, _SZ, _P]),

@@ -3,6 +3,7 @@
 // entry point, which also dispatches the double-float form (pg_cocg_df.cu).
 // Replaces the KSPSolve of petgem/solver.py:584-594.
 #include "pg_cocg.cuh"
+#include "pg_sort.cuh"
 
 namespace {
 
@@ -55,6 +56,72 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv1(const int64_t* __restrict
       }
       ctl->counter = 0;
     }
+  }
+}
+
+// The same product over the rows in the order perm (rows sorted by length):
+// the warps of a launch see rows of one length, so no lane idles on a short
+// row while its neighbours finish a long one.  Complex128 products are
+// FP64-pipe bound and the pipe is charged per warp instruction, active lanes
+// or not, so idle lanes and the shuffle-reduction adds are what separates the
+// product from its 4 FMAs per stored entry.
+template <typename CM, int G>
+__global__ void __launch_bounds__(kThreads) k_cg_spmv_sorted(const int64_t* __restrict__ rowptr,
+                                                             const int32_t* __restrict__ col,
+                                                             const CM* __restrict__ val, int64_t n,
+                                                             const int32_t* __restrict__ perm,
+                                                             const CM* __restrict__ pm,
+                                                             const double2* __restrict__ p64, CM* __restrict__ q,
+                                                             double2* partial, CgState* st, CgCtl* ctl) {
+  if (!ctl->any_active) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int lane = threadIdx.x % G;
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t warp_base = gid - (threadIdx.x & 31) / G;
+  double2 mu = make_double2(0.0, 0.0);
+  for (int64_t iw = warp_base; iw < n; iw += groups) {
+    const int64_t i = iw + (gid - warp_base);
+    const bool valid = i < n;
+    const int64_t r = valid ? perm[i] : 0;
+    CM acc = czero<CM>();
+    if (valid) {
+      const int64_t e = rowptr[r + 1];
+      for (int64_t k = rowptr[r] + lane; k < e; k += G) acc = cfma(val[k], pm[col[k]], acc);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) acc = cadd(acc, shfl_xor(acc, off));
+    if (valid && lane == 0) {
+      q[r] = acc;
+      mu = dadd(mu, cmul(p64[r], to_d(acc)));
+    }
+  }
+  block_reduce_rhs<1>(mu, smem, partial + blockIdx.x);
+  if (arrive_last(&ctl->counter)) {
+    const double2 m = sum_partials<1>(partial, gridDim.x, 0, smem);
+    if (threadIdx.x == 0) {
+      CgState& S = st[0];
+      if (S.active) {
+        if (m.x == 0.0 && m.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.alpha = make_double2(0.0, 0.0);
+        } else {
+          S.alpha = ddiv(S.rho, m);
+        }
+      } else {
+        S.alpha = make_double2(0.0, 0.0);
+      }
+      ctl->counter = 0;
+    }
+  }
+}
+
+// sort keys: row lengths, values: row indices
+__global__ void k_row_len_keys(const int64_t* rowptr, int64_t n, uint64_t* keys, int32_t* rows) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    keys[r] = (uint64_t)(rowptr[r + 1] - rowptr[r]);
+    rows[r] = (int32_t)r;
   }
 }
 
@@ -253,13 +320,28 @@ size_t cg_layout(const Plan& P, size_t* off /* 20 */) {
   put(13, sizeof(int) * (P.k + 1));             // want, status
   put(18, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);     // block-Jacobi factors
   put(19, P.bj.p ? sizeof(double2) * P.n * P.k : 0);         // S r64
+  // complex128, one RHS: rows sorted by length for the product (perm, sort keys, sort workspace)
+  const bool sorted = P.prec == 0 && P.k == 1 && P.n < (int64_t(1) << 31);
+  put(14, sorted ? sizeof(int32_t) * P.n : 0);
+  put(15, sorted ? sizeof(uint64_t) * P.n : 0);
+  put(16, sorted ? pg::sort_workspace_bytes(P.n) : 0);
   return o;
 }
 
+// variant 0: rows in order, lanes per row from the row length; 2 / 4: rows
+// in length order (perm) with 2 / 4 lanes per row
 template <typename CM>
 void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const CM* val, const CM* pm,
                     const double2* p64, CM* q, double2* partial, CgState* st, CgCtl* ctl, int64_t npr, int grid,
-                    cudaStream_t s) {
+                    cudaStream_t s, int variant = 0, const int32_t* perm = nullptr) {
+  if (P.k == 1 && perm && variant == 2) {
+    k_cg_spmv_sorted<CM, 2><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, perm, pm, p64, q, partial, st, ctl);
+    return;
+  }
+  if (P.k == 1 && perm && variant == 4) {
+    k_cg_spmv_sorted<CM, 4><<<grid, kThreads, 0, s>>>(rowptr, col, val, P.n, perm, pm, p64, q, partial, st, ctl);
+    return;
+  }
   switch (P.k) {
     case 1:
       switch (LanesPerRow<CM>::pick(npr)) {
@@ -285,6 +367,8 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   const bool bj = P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
   double2* r64b = reinterpret_cast<double2*>(ws + off[19]);
+  const bool sorted = P.prec == 0 && P.k == 1 && P.n < (int64_t(1) << 31);
+  int32_t* perm = sorted ? reinterpret_cast<int32_t*>(ws + off[14]) : nullptr;
   CM* At = reinterpret_cast<CM*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);
@@ -314,6 +398,14 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   if (spmv_grid > nb) return PG_ERR_ARG;  // partial buffers are sized by nb
 
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+  if (sorted) {
+    uint64_t* keys = reinterpret_cast<uint64_t*>(ws + off[15]);
+    k_row_len_keys<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, P.n, keys, perm);
+    PG_LAUNCH_CHECK();
+    const int st0 = pg::sort_pairs(keys, perm, P.n, 32, ws + off[16], pg::sort_workspace_bytes(P.n), s);
+    if (st0) return st0;
+  }
+  int variant = 0;
   if (bj) {
     int st0;
     if (sizeof(CM) == sizeof(double2))
@@ -386,12 +478,22 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, pm, first ? 1 : 0,
                                                              write_pm, part),
                    k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    if (first && sorted && autotune_enabled()) {
+      // the product is the first kernel of an iteration and recomputes alpha,
+      // so timing the candidates on the live operands changes no state
+      variant = pick_fastest({0, 2, 4}, [&](int v) {
+        launch_cg_spmv<CM>(P, rowptr, col, At, pm, pv, q, part, st, ctl, npr, spmv_grid, s, v, perm);
+      }, s);
+      PG_LAUNCH_CHECK();
+      if (monitor) fprintf(stderr, "pg_cocg: product variant %d for n=%lld nnz=%lld\n", variant, (long long)P.n,
+                           (long long)P.nnz);
+    }
     first = false;
     const int steps = (int)((max_it - its) < chunk ? (max_it - its) : chunk);
     const double delta = P.prec ? 0.1 : 0.0;
     for (int it = 0; it < steps; ++it) {
       const int iter = (int)(launch_iter + it);
-      launch_cg_spmv<CM>(P, rowptr, col, At, pm, pv, q, part, st, ctl, npr, spmv_grid, s);
+      launch_cg_spmv<CM>(P, rowptr, col, At, pm, pv, q, part, st, ctl, npr, spmv_grid, s, variant, perm);
       PG_KSWITCH(k, (k_cg_update<CM, K><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
                      k_cg_pupdate<CM, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, pm, r, P.n, st, iter,
                                                                                           write_pm)));

@@ -259,9 +259,12 @@ __device__ void cg_alpha_final(const double2* partial, int nblocks, CgState* st,
   if (threadIdx.x == 0) ctl->counter = 0;
 }
 
+// spike: a cycle also ends when a column's residual estimate exceeds spike
+// times its starting value (COCG's residual norm is not monotone; a
+// recurrence carried far past such a spike has lost accuracy)
 template <int K>
 __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblocks, CgState* st, CgCtl* ctl, int iter,
-                              double delta, double2* smem) {
+                              double delta, double2* smem, double spike = 1e3) {
   const int my = threadIdx.x < K ? threadIdx.x : 0;
   const double2 rho = sum_partials<K>(prho, nblocks, my, smem);
   const double2 w = sum_partials<K>(pw, nblocks, my, smem);
@@ -284,7 +287,7 @@ __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblock
       }
       S.rho = rho;
       if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
-      else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
+      else if (S.res <= delta * S.res0 || S.res > spike * S.res0) atomicOr(&stop, 1);
     } else {
       S.beta = make_double2(0.0, 0.0);
       S.beta_iter = 0;

@@ -179,6 +179,29 @@ __global__ void __launch_bounds__(kTabThreads) k_tuple_tables(const int32_t* cod
   }
 }
 
+// Moments that vanish analytically (for instance every curl-curl moment of a
+// gradient-type edge function, whose curl is zero) come out of the
+// quadrature as rounding noise, ~1e-17 of the table's scale.  One CTA per
+// (tuple, moment) slice sets every entry below kTableZeroRel of the slice's
+// largest magnitude to exactly 0.0, so such products are exact zeros in
+// every kernel that reads the tables (and the assembly can skip them).
+constexpr double kTableZeroRel = 1e-13;
+__global__ void __launch_bounds__(256) k_clean_tables(double* tables, int64_t NT) {
+  double* t = tables + (size_t)blockIdx.x * NT;
+  __shared__ double red[256];
+  double m = 0.0;
+  for (int64_t i = threadIdx.x; i < NT; i += blockDim.x) m = fmax(m, fabs(t[i]));
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  const double cut = kTableZeroRel * red[0];
+  for (int64_t i = threadIdx.x; i < NT; i += blockDim.x)
+    if (fabs(t[i]) <= cut) t[i] = 0.0;
+}
+
 // Per-element geometry factors: cM = det * S (6), cK = G / det (6).
 // Returns false for a degenerate element.
 __device__ inline bool element_factors(const double* nodes, const int32_t* en, const double* sig, double cM[6],
@@ -353,6 +376,7 @@ extern "C" int pg_tuple_tables(const int32_t* codes, int64_t n_tuples, int p, do
   const size_t smem = (size_t)chunk * (6 * nd_of(p) + 1) * sizeof(double);
   PG_CUDA_TRY(cudaFuncSetAttribute(k_tuple_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_tuple_tables<<<(unsigned)n_tuples, kTabThreads, smem, pg_stream(stream)>>>(codes, p, chunk, tables);
+  k_clean_tables<<<(unsigned)(n_tuples * 12), 256, 0, pg_stream(stream)>>>(tables, packed_of(nd_of(p)));
   PG_LAUNCH_CHECK();
   return PG_OK;
 }

@@ -48,3 +48,39 @@ extern "C" int pg_fp64_probe(double* out, int blocks, int iters, void* stream) {
   PG_LAUNCH_CHECK();
   return PG_OK;
 }
+
+// Streaming copy by the SMs: 16-byte loads and stores, grid-stride.  Used to
+// move results into pinned host memory the GPU maps into its address space
+// (on Grace-Blackwell, over NVLink-C2C), where many SMs issuing stores keep
+// more bytes in flight than one copy engine.
+namespace {
+__global__ void __launch_bounds__(512) k_copy16(const int4* __restrict__ src, int4* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = __ldcs(src + i);
+}
+__global__ void k_copy1(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+}  // namespace
+
+extern "C" int pg_copy_bytes(const void* src, void* dst, int64_t bytes, int blocks, void* stream) {
+  if (!src || !dst || bytes < 0 || blocks < 0) {
+    pg_set_error("pg_copy_bytes: bad argument");
+    return PG_ERR_ARG;
+  }
+  if (bytes == 0) return PG_OK;
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) != 0) {
+    pg_set_error("pg_copy_bytes: src and dst must be 16-byte aligned");
+    return PG_ERR_ARG;
+  }
+  cudaStream_t s = pg_stream(stream);
+  const int g = blocks > 0 ? blocks : 152 * 4;
+  const int64_t n16 = bytes / 16;
+  if (n16) k_copy16<<<g, 512, 0, s>>>(reinterpret_cast<const int4*>(src), reinterpret_cast<int4*>(dst), n16);
+  if (bytes % 16)
+    k_copy1<<<1, 32, 0, s>>>(reinterpret_cast<const unsigned char*>(src) + 16 * n16,
+                             reinterpret_cast<unsigned char*>(dst) + 16 * n16, bytes % 16);
+  PG_LAUNCH_CHECK();
+  return PG_OK;
+}

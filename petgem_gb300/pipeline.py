@@ -307,15 +307,15 @@ def computeImpedance(fields, omega, mu):
 
 
 def write_results(stem, datasets):
-    """HDF5 with petgem's group/dataset paths (postprocessing.py:341-461) when
-    h5py is installed, else an .npz whose keys are those paths."""
+    """{stem}.h5 with petgem's group/dataset paths (postprocessing.py:341-461):
+    through h5py when it is installed, else with petgem_gb300.hdf5 (the same
+    classic HDF5 format, no HDF5 library needed)."""
+    path = stem + ".h5"
     try:
         import h5py
     except ImportError:
-        path = stem + ".npz"
-        np.savez(path, **{k: np.asarray(v) for k, v in datasets.items()})
-        return path
-    path = stem + ".h5"
+        from . import hdf5
+        return hdf5.write(path, datasets)
     with h5py.File(path, "w") as f:
         for k, v in datasets.items():
             f.create_dataset(k, data=v)

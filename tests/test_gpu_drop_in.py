@@ -117,6 +117,7 @@ output:
     assert post.fields.shape == F.shape == (5, 6)
     assert rel_norm(post.fields, F) < 1e-6
     assert os.path.exists(post.output_file)
+    _check_result_file(post.output_file, "csem", [post.fields])
 
 
 def test_petgem_petsc_test_system_solved_by_gpu_gmres():
@@ -213,4 +214,43 @@ output:
     Zr = computeImpedance(post.fields, 2 * np.pi, fem.MU0)[3]
     assert rel_norm(np.stack(Zr), np.stack(post.impedance)) == 0.0
     assert os.path.exists(post.output_file)
+    _check_result_file(post.output_file, "mt", post.fields, post.impedance)
     assert os.path.exists(os.path.join(str(tmp_path / "tmp"), "x1.dat"))
+
+
+def _check_result_file(path, mode, fields, impedance=None):
+    """petgem's result file (postprocessing.py:341-461): name
+    {mode}_petgemV{version}_{date}.h5 and its group / dataset paths, read back."""
+    import datetime
+    import os
+    assert os.path.basename(path) == f"{mode}_petgemV1.0_{datetime.date.today():%Y-%m-%d}.h5"
+    try:
+        import h5py
+    except ImportError:
+        from petgem_gb300 import hdf5
+        d = hdf5.read(path)
+    else:
+        with h5py.File(path, "r") as f:
+            d = {}
+            f.visititems(lambda k, v: d.__setitem__(k, v[()]) if isinstance(v, h5py.Dataset) else None)
+    for k in ("machine/machine", "machine/num_processors", "machine/petgem_version", "model/date", "model/mesh_file",
+              "model/receivers_file", "model/nord", "model/dof", "model/cuda", "model/vtk", "model/mode",
+              "model/num-polarizations", "model/solver", "model/run-time (s)", "model/frequency (Hz)"):
+        assert k in d, k
+    if mode == "csem":
+        for k in ("source_position (m)", "source_azimuth (deg)", "source_dip (deg)", "source_current (Am)",
+                  "source_length (m)"):
+            assert "model/" + k in d, k
+        groups = [("E-fields", "H-fields")]
+    else:
+        pols = [str(q.decode() if isinstance(q, bytes) else q) for q in np.atleast_1d(d["model/polarization"])]
+        groups = [(f"E-fields_mode_{q}", f"H-fields_mode_{q}") for q in pols]
+    for (ge, gh), F in zip(groups, fields):
+        for c, k in enumerate("xyz"):
+            assert np.array_equal(d[f"model/{ge}/{k}"], F[:, c])
+            assert np.array_equal(d[f"model/{gh}/{k}"], F[:, 3 + c])
+    if impedance is not None:
+        for j, k in enumerate(("xx", "xy", "yx", "yy")):
+            assert np.array_equal(d[f"model/impedance/{k}"], impedance[j])
+            assert f"model/apparent_resistivity/{k}" in d and f"model/phase/{k}" in d
+        assert "model/tipper/x" in d and "model/tipper/y" in d
