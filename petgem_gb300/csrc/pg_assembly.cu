@@ -219,28 +219,38 @@ __global__ void k_coefficients(const double* nodes, const int32_t* elemsN, const
       for (int t = 0; t < 12; ++t) put_coef(cf, t, 0.0);
       continue;
     }
-    const double id = 1.0 / det;
-    double inv[3][3];
-    inv[0][0] = c00 * id;
-    inv[1][0] = c01 * id;
-    inv[2][0] = c02 * id;
-    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    // With adj = det inv(J) (the adjugate): cK = J J^T / det and
+    // cM = -omega mu det inv^T D inv = -omega mu adj^T D adj / det, which
+    // spares the nine inverse entries and the rescaling by det (GB300's FP64
+    // pipe makes every operation here count); 1 / det correctly rounded.
+    const double id = __drcp_rn(det);
+    double adj[3][3];   // adj[c][a] = inv[c][a] * det
+    adj[0][0] = c00;
+    adj[1][0] = c01;
+    adj[2][0] = c02;
+    adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
     const double D[3] = {sigma[2 * e], sigma[2 * e], sigma[2 * e + 1]};
+    double w[3][3];     // D adj
+    for (int c = 0; c < 3; ++c)
+      for (int b = 0; b < 3; ++b) w[c][b] = D[c] * adj[c][b];
+    const double mscale = -omu * id;
     const int pa[6] = {0, 1, 2, 0, 0, 1};
     const int pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
     for (int t = 0; t < 6; ++t) {
       double s = 0.0, g = 0.0;
+#pragma unroll
       for (int c = 0; c < 3; ++c) {
-        s += inv[c][pa[t]] * D[c] * inv[c][pb[t]];
-        g += J[pa[t]][c] * J[pb[t]][c];
+        s = fma(adj[c][pa[t]], w[c][pb[t]], s);
+        g = fma(J[pa[t]][c], J[pb[t]][c], g);
       }
       put_coef(cf, t, g * id);
-      put_coef(cf, 6 + t, -omu * (det * s));
+      put_coef(cf, 6 + t, mscale * s);
     }
   }
 }

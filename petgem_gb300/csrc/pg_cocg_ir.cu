@@ -12,7 +12,8 @@
 // an exact residual every refinement step, which is what keeps an FP32
 // recurrence convergent at condition numbers where it stagnates alone), and
 // runs per column until its recurrence estimate of the residual has dropped
-// by inner_rtol (or to the final target, whichever is larger).
+// by inner_rtol (or to the final target, whichever is larger), for at most
+// 4x the inner iterations of the first refinement step.
 //
 // Per inner iteration: product q = At p fused with mu = p^T q (alpha in the
 // last block), the vector update fused with rho = r^T r and the residual
@@ -504,6 +505,10 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   bool first = true;
   int variant = 80;
   int stalls = 0;
+  // inner iterations of one refinement step are capped at 4x those of the
+  // first step (at least 500): an inner solve that has stopped contracting
+  // is cut, and the next refinement restarts it on the exact residual
+  int64_t inner_cap = 0;
   std::vector<double> best(k, 1e300);
   auto one_iteration = [&](cudaStream_t ss) {
     if (k == 1)
@@ -646,8 +651,10 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     first = false;
     // inner solve: replay chunks of iterations until every column reached its
     // target (the kernels of a finished solve return at once)
+    const int64_t its0 = its;
     for (;;) {
-      const int64_t left = max_it - its;
+      int64_t left = max_it - its;
+      if (inner_cap > 0 && its0 + inner_cap - its < left) left = its0 + inner_cap - its;
       const int steps = (int)(left < chunk ? left : chunk);
       int done = 0;
       if (use_graphs && steps >= kGraphIters) {
@@ -676,10 +683,11 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
         status = PG_ERR_NONFINITE;
         break;
       }
-      if (!hctl.any_active || its >= max_it) break;
+      if (!hctl.any_active || its >= max_it || (inner_cap > 0 && its - its0 >= inner_cap)) break;
       chunk = chunk < 512 ? chunk * 2 : chunk;
     }
     if (status) break;
+    if (inner_cap == 0) inner_cap = std::max<int64_t>(500, 4 * (its - its0));
     ++outer;
     // x += c S^T y
     PG_KSWITCH(k, (k_ir_scaled_y<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(y, cscale, P.n, aux)));
