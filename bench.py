@@ -651,8 +651,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; ir32 = complex64 "
                    "inner COCG solves (matrix, vectors, products in FP32), each restarted from the FP64 true residual, "
                    "inside FP64 iterative refinement (each inner solve to a 100x residual drop, capped); at this "
-                   "conditioning (eps32 * kappa ~ 1) it converges on the workload's own source but some sources of "
-                   "the 16-source batch stall; mixed = complex64 "
+                   "conditioning (eps32 * kappa ~ 1) its inner solves contract slowly and unevenly; mixed = complex64 "
                    "matrix/SpMV + FP64 recurrence with reliable updates, which stalls at this conditioning (capped)")
     out["speedup_df64_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rdb["ms_per_rhs"], 1e-9), 2)
 

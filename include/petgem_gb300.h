@@ -500,8 +500,8 @@ typedef struct pg_cocg_opts {
   int block_p;
   int64_t block_edges, block_faces, block_volumes;
   /* precision 3: relative residual reduction each complex64 inner solve aims
-   * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 4x the
-   * inner iterations of the first refinement step (at least 500) */
+   * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 8x the
+   * inner iterations of the first refinement step (at least 1,000) */
   double inner_rtol;
 } pg_cocg_opts;
 

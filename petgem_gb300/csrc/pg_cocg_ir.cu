@@ -13,7 +13,7 @@
 // recurrence convergent at condition numbers where it stagnates alone), and
 // runs per column until its recurrence estimate of the residual has dropped
 // by inner_rtol (or to the final target, whichever is larger), for at most
-// 4x the inner iterations of the first refinement step.
+// 8x the inner iterations of the first refinement step.
 //
 // Per inner iteration: product q = At p fused with mu = p^T q (alpha in the
 // last block), the vector update fused with rho = r^T r and the residual
@@ -152,6 +152,22 @@ __global__ void __launch_bounds__(kThreads) k_ir_spmv_grp(const int64_t* __restr
   if (arrive_last(&ctl->counter)) cg_alpha_final<1>(partial, gridDim.x, st, ctl, smem);
 }
 
+// compensated (Kahan) accumulation of complex64 products: a thread sums a
+// whole row, so a plain FP32 sum would carry ~n ulps of error into an
+// operator that is already at the edge of FP32 (eps32 * kappa ~ 1)
+struct KahanC {
+  float2 s = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
+  __device__ __forceinline__ void add(float2 a, float2 x) {
+    const float2 p = cmul(a, x);
+    const float yr = __fsub_rn(p.x, c.x), yi = __fsub_rn(p.y, c.y);
+    const float tr = __fadd_rn(s.x, yr), ti = __fadd_rn(s.y, yi);
+    c.x = __fsub_rn(__fsub_rn(tr, s.x), yr);
+    c.y = __fsub_rn(__fsub_rn(ti, s.y), yi);
+    s.x = tr;
+    s.y = ti;
+  }
+};
+
 // K RHS (RHS fastest): one thread per (group of R rows, rhs); the K threads of
 // a group read the column index and the R matrix values once per step
 // (broadcast) and K consecutive p entries (one coalesced segment)
@@ -174,27 +190,25 @@ __global__ void __launch_bounds__(kThreads) k_ir_spmm(const int64_t* __restrict_
 #pragma unroll
     for (int i = 0; i < R; ++i) off[i] = rowptr[r0 + i];
     const int len = (int)(rowptr[r0 + 1] - off[0]);
-    float2 acc[R], acc1[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i) acc[i] = acc1[i] = make_float2(0.f, 0.f);
+    KahanC acc[R];
     int k = 0;
     for (; k + 1 < len; k += 2) {
       const int32_t c0 = col[off[0] + k], c1 = col[off[0] + k + 1];
       const float2 x0 = pv[(int64_t)c0 * K + rhs], x1 = pv[(int64_t)c1 * K + rhs];
 #pragma unroll
       for (int i = 0; i < R; ++i) {
-        acc[i] = cfma(val[off[i] + k], x0, acc[i]);
-        acc1[i] = cfma(val[off[i] + k + 1], x1, acc1[i]);
+        acc[i].add(val[off[i] + k], x0);
+        acc[i].add(val[off[i] + k + 1], x1);
       }
     }
     if (k < len) {
       const float2 x0 = pv[(int64_t)col[off[0] + k] * K + rhs];
 #pragma unroll
-      for (int i = 0; i < R; ++i) acc[i] = cfma(val[off[i] + k], x0, acc[i]);
+      for (int i = 0; i < R; ++i) acc[i].add(val[off[i] + k], x0);
     }
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const float2 a = cadd(acc[i], acc1[i]);
+      const float2 a = acc[i].s;
       q[(r0 + i) * K + rhs] = a;
       mu = c32_bilin_add(mu, pv[(r0 + i) * K + rhs], a);
     }
@@ -505,8 +519,8 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   bool first = true;
   int variant = 80;
   int stalls = 0;
-  // inner iterations of one refinement step are capped at 4x those of the
-  // first step (at least 500): an inner solve that has stopped contracting
+  // inner iterations of one refinement step are capped at 8x those of the
+  // first step (at least 1,000): an inner solve that has stopped contracting
   // is cut, and the next refinement restarts it on the exact residual
   int64_t inner_cap = 0;
   std::vector<double> best(k, 1e300);
@@ -687,7 +701,7 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       chunk = chunk < 512 ? chunk * 2 : chunk;
     }
     if (status) break;
-    if (inner_cap == 0) inner_cap = std::max<int64_t>(500, 4 * (its - its0));
+    if (inner_cap == 0) inner_cap = std::max<int64_t>(1000, 8 * (its - its0));
     ++outer;
     // x += c S^T y
     PG_KSWITCH(k, (k_ir_scaled_y<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(y, cscale, P.n, aux)));
