@@ -465,6 +465,63 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   if (monitor)
     for (int i = 0; i < k; ++i) fprintf(stderr, "pg_gmres: rhs %d ||b|| = %.6e\n", i, bnorm[i]);
   const int64_t max_it = o->max_it > 0 ? o->max_it : 10000;
+  // One restart cycle's Arnoldi steps: the launches and their arguments are
+  // the same every full cycle (j is fixed per step, converged RHS are
+  // skipped through ctl on the device), so a full cycle is captured once in
+  // a CUDA graph and replayed; small systems are bound by launch latency.
+  auto arnoldi = [&](cudaStream_t ss, int steps) {
+    for (int j = 0; j < steps; ++j) {
+      C* vj = V + (int64_t)j * stride;
+      C* w = V + (int64_t)(j + 1) * stride;
+      launch_spmv<C>(P, rowptr, col, Ahat, vj, w, nullptr, ctl, npr, ss);
+      const int passes = o->reorth ? 2 : 1;
+      for (int pass = 0; pass < passes; ++pass) {
+        PG_KSWITCH(k, (k_dots<C, K><<<nb, kThreads, 0, ss>>>(V, stride, w, P.n, j, dpart, ctl),
+                       k_dots_final<C, K><<<1, 1024, 0, ss>>>(dpart, nb, j, m, st, coef, pass, ctl),
+                       k_update<C, K><<<nb, kThreads, 0, ss>>>(V, stride, w, P.n, j, coef, st, pass, npart, ctl)));
+      }
+      PG_KSWITCH(k, (k_givens<K><<<1, 32 * K, 0, ss>>>(npart, nb, j, m, st, ctl, j == steps - 1)));
+    }
+  };
+  const char* genv = getenv("PG_GRAPHS");
+  const bool use_graphs = !(genv && genv[0] == '0');
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_failed = false;
+  struct GraphCleanup {
+    cudaStream_t& cs;
+    cudaEvent_t& a;
+    cudaEvent_t& b;
+    cudaGraphExec_t& g;
+    ~GraphCleanup() {
+      if (g) cudaGraphExecDestroy(g);
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      if (cs) cudaStreamDestroy(cs);
+    }
+  } graph_cleanup{cs, ev_in, ev_out, gexec};
+  auto build_graph = [&]() {
+    cudaGraph_t graph = nullptr;
+    bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      arnoldi(cs, m);
+      ok = cudaStreamEndCapture(cs, &graph) == cudaSuccess && graph != nullptr;
+    }
+    if (ok) ok = cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+      const cudaError_t e = cudaGetLastError();   // capture unavailable: keep launching directly
+      if (monitor) fprintf(stderr, "pg_gmres: cycle graph not captured (%s); launching directly\n", cudaGetErrorString(e));
+      gexec = nullptr;
+      graph_failed = true;
+    } else if (monitor) {
+      fprintf(stderr, "pg_gmres: restart cycle of %d steps captured as a CUDA graph\n", m);
+    }
+  };
   for (;;) {
     // r = b - A x (FP64), ||r||
     launch_spmv<double2>(P, rowptr, col, A, x, r, b, nullptr, npr, s);
@@ -500,18 +557,19 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
     PG_KSWITCH(k, (k_start<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(r, P.n, rnorm, V),
                    k_cycle_init<K><<<1, 32, 0, s>>>(st, rnorm, target, want, ctl)));
     int steps = (int)((max_it - its) < m ? (max_it - its) : m);
-    for (int j = 0; j < steps; ++j) {
-      C* vj = V + (int64_t)j * stride;
-      C* w = V + (int64_t)(j + 1) * stride;
-      launch_spmv<C>(P, rowptr, col, Ahat, vj, w, nullptr, ctl, npr, s);
-      const int passes = o->reorth ? 2 : 1;
-      for (int pass = 0; pass < passes; ++pass) {
-        PG_KSWITCH(k, (k_dots<C, K><<<nb, kThreads, 0, s>>>(V, stride, w, P.n, j, dpart, ctl),
-                       k_dots_final<C, K><<<1, 1024, 0, s>>>(dpart, nb, j, m, st, coef, pass, ctl),
-                       k_update<C, K><<<nb, kThreads, 0, s>>>(V, stride, w, P.n, j, coef, st, pass, npart, ctl)));
+    bool replayed = false;
+    if (use_graphs && steps == m && !graph_failed) {
+      if (!gexec) build_graph();
+      if (gexec) {
+        cudaEventRecord(ev_in, s);
+        cudaStreamWaitEvent(cs, ev_in, 0);
+        cudaGraphLaunch(gexec, cs);
+        cudaEventRecord(ev_out, cs);
+        cudaStreamWaitEvent(s, ev_out, 0);
+        replayed = true;
       }
-      PG_KSWITCH(k, (k_givens<K><<<1, 32 * K, 0, s>>>(npart, nb, j, m, st, ctl, j == steps - 1)));
     }
+    if (!replayed) arnoldi(s, steps);
     PG_LAUNCH_CHECK();
     if (bj) {
       // x += M^-1 (V y): the combination into r (free until the next true residual), then the blocks
