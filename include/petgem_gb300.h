@@ -452,6 +452,16 @@ typedef struct pg_gmres_opts {
    * DOFs stay diagonal). */
   int block_p;
   int64_t block_edges, block_faces, block_volumes;
+  /* gradient correction (precision 0 with diagonal Jacobi, block_p 0;
+   * grad_rowptr NULL = off), as in pg_cocg_opts: GMRES runs on A B with
+   * B = D^-1 + G diag(G^T A G)^-1 G^T (right preconditioning). */
+  int64_t grad_cols;
+  const int64_t* grad_rowptr;
+  const int32_t* grad_col;
+  const double* grad_val;
+  const int64_t* gradt_rowptr;
+  const int32_t* gradt_row;
+  const double* gradt_val;
 } pg_gmres_opts;
 
 typedef struct pg_gmres_result {
@@ -503,7 +513,48 @@ typedef struct pg_cocg_opts {
    * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 8x the
    * inner iterations of the first refinement step (at least 1,000) */
   double inner_rtol;
+  /* gradient correction (pg_cocg and pg_gmres; precision 0 with diagonal
+   * Jacobi, block_p 0; grad_rowptr NULL = off): G, n rows by grad_cols columns, and
+   * its transpose from pg_gradient_map.  The preconditioner becomes
+   *   B = D^-1 + G diag(G^T A G)^-1 G^T
+   * (D = diag A; diag(G^T A G) is formed from A when the solve starts), which
+   * adds a Jacobi step on the gradient fields that the edge Jacobi step
+   * cannot reduce; no petgem counterpart (petgem/solver.py:584-594 leaves
+   * the preconditioner to PETSc). */
+  int64_t grad_cols;
+  const int64_t* grad_rowptr;
+  const int32_t* grad_col;
+  const double* grad_val;
+  const int64_t* gradt_rowptr;
+  const int32_t* gradt_row;
+  const double* gradt_val;
 } pg_cocg_opts;
+
+/* Discrete gradient for the COCG gradient correction (no petgem counterpart):
+ * G[r, phi] = coefficient of grad(phi) on H(curl) DOF r, phi running over
+ * the order-p H1 functions (p 1..3): the mesh's vertices, then (p >= 2) one
+ * quadratic bubble per edge, then (p = 3) a cubic bubble per edge and one
+ * per face.  Built from the mesh maps of pg_topology / pg_connectivity_dofs /
+ * pg_orientation_tuples (dofs int32 [n_elems * nd], tuple_of_elem and codes
+ * as pg_tuple_tables takes them) by exact L2 projection on the reference
+ * element; rows follow the DOF numbering (edges, faces, volumes), entries of
+ * a row are written by one owner element.  Columns with an entry in a row
+ * flagged in pec_flags (uint8 [n], may be NULL) are dropped, zeros are not
+ * stored.  G: g_rowptr int64 [n + 1], g_col int32, g_val f64; its transpose:
+ * gt_rowptr int64 [n_cols + 1], gt_row int32 (ascending in each row), gt_val
+ * f64; the entry arrays hold at most max_entries (pg_gradient_map_sizes) and
+ * g_rowptr[n] = gt_rowptr[n_cols] entries are stored.  Deterministic;
+ * synchronises (PG_ERR_UNSUPPORTED if a coefficient falls outside its row's
+ * entity structure, i.e. the basis and the map disagree). */
+int pg_gradient_map_sizes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems, int p,
+                          int64_t* n_cols /* host */, int64_t* max_entries /* host */);
+size_t pg_gradient_map_workspace_bytes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems,
+                                       int64_t n_tuples, int p);
+int pg_gradient_map(const int32_t* elemsN, const int32_t* elemsE, const int32_t* elemsF, const int32_t* dofs,
+                    const int32_t* tuple_of_elem, const int32_t* codes, int64_t n_tuples, int64_t n_elems,
+                    int64_t n_nodes, int64_t n_edges, int64_t n_faces, int p, const uint8_t* pec_flags,
+                    int64_t* g_rowptr, int32_t* g_col, double* g_val, int64_t* gt_rowptr, int32_t* gt_row,
+                    double* gt_val, void* workspace, size_t workspace_bytes, void* stream);
 
 void pg_cocg_default_opts(pg_cocg_opts* opts);
 size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts);

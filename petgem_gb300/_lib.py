@@ -20,7 +20,10 @@ class GmresOpts(ctypes.Structure):
     """pg_gmres_opts (include/petgem_gb300.h)."""
     _fields_ = [("restart", ctypes.c_int), ("max_it", ctypes.c_int), ("rtol", ctypes.c_double),
                 ("precision", ctypes.c_int), ("reorth", ctypes.c_int), ("block_p", ctypes.c_int),
-                ("block_edges", ctypes.c_int64), ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64)]
+                ("block_edges", ctypes.c_int64), ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64),
+                ("grad_cols", ctypes.c_int64), ("grad_rowptr", ctypes.c_void_p), ("grad_col", ctypes.c_void_p),
+                ("grad_val", ctypes.c_void_p), ("gradt_rowptr", ctypes.c_void_p), ("gradt_row", ctypes.c_void_p),
+                ("gradt_val", ctypes.c_void_p)]
 
 
 class GmresResult(ctypes.Structure):
@@ -33,7 +36,10 @@ class CocgOpts(ctypes.Structure):
     """pg_cocg_opts (include/petgem_gb300.h)."""
     _fields_ = [("max_it", ctypes.c_int), ("rtol", ctypes.c_double), ("precision", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("block_p", ctypes.c_int), ("block_edges", ctypes.c_int64),
-                ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64), ("inner_rtol", ctypes.c_double)]
+                ("block_faces", ctypes.c_int64), ("block_volumes", ctypes.c_int64), ("inner_rtol", ctypes.c_double),
+                ("grad_cols", ctypes.c_int64), ("grad_rowptr", ctypes.c_void_p), ("grad_col", ctypes.c_void_p),
+                ("grad_val", ctypes.c_void_p), ("gradt_rowptr", ctypes.c_void_p), ("gradt_row", ctypes.c_void_p),
+                ("gradt_val", ctypes.c_void_p)]
 
 
 _PO = ctypes.POINTER(GmresOpts)
@@ -108,6 +114,10 @@ SIGNATURES = {
     "pg_gmres_default_opts": (None, [_PO]),
     "pg_gmres_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PO]),
     "pg_gmres": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PO, _PR, _P, _P, _SZ, _P]),
+    "pg_gradient_map_sizes": (_INT, [_I64, _I64, _I64, _I64, _INT, _P, _P]),
+    "pg_gradient_map_workspace_bytes": (_SZ, [_I64, _I64, _I64, _I64, _I64, _INT]),
+    "pg_gradient_map": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _P, _P,
+                               _P, _P, _SZ, _P]),
     "pg_cocg_default_opts": (None, [_PC]),
     "pg_cocg_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PC]),
     "pg_cocg": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PC, _PR, _P, _P, _SZ, _P]),

@@ -190,6 +190,39 @@ __device__ void pg_shape3d(double x, double y, double z, const int eo[6], const 
   }
 }
 
+// Gauss-Legendre nodes/weights on [0,1] by Newton iteration on P_n.
+__device__ inline void gauss_legendre01(int n, double* x, double* w) {
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    double z = cos(pi * (i + 0.75) / (n + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = pk;
+      }
+      // p1 = P_n(z), p0 = P_{n-1}(z)
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = pk;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+    }
+    x[n - 1 - i] = 0.5 * (z + 1.0);
+    w[n - 1 - i] = 1.0 / ((1.0 - z * z) * dp * dp);  // 2/((1-z^2)P'^2) mapped to [0,1]
+  }
+}
+
 // Runtime-order dispatch.
 __device__ inline void pg_shape3d_dispatch(int p, double x, double y, double z, const int eo[6],
                                            const int fo[4], double* N, double* C, int ld) {

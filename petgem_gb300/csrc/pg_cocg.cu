@@ -168,13 +168,16 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmm(const int64_t* __restrict_
 // y += alpha p ; r -= alpha q (FP64) ; partials rho = r^T r, w = sum |r|^2 |D|.
 // Last block: beta, residual estimate, activity; the cycle stops for every
 // RHS when one needs a reliable update (estimate dropped below delta * res0
-// or grew above 1e3 * res0), or when all have converged.
-template <typename CM, int K>
+// or grew above 1e3 * res0), or when all have converged.  GRAD (gradient
+// correction): also u = S^-1 r; rho = r^T z and beta are left to
+// k_grad_prolong.
+template <typename CM, int K, bool GRAD = false>
 __global__ void __launch_bounds__(kThreads) k_cg_update(double2* __restrict__ y, double2* __restrict__ r,
                                                         const double2* __restrict__ pv, const CM* __restrict__ q,
                                                         const double* __restrict__ wd, int64_t n, CgState* st,
                                                         double2* prho, double2* pw, CgCtl* ctl, int iter,
-                                                        double delta) {
+                                                        double delta, double2* __restrict__ u = nullptr,
+                                                        const double2* __restrict__ Sinv = nullptr) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ double2 al[kMaxK];
@@ -194,15 +197,20 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(double2* __restrict__ y,
     re.y -= a.x * qe.y + a.y * qe.x;
     y[e] = ye;
     r[e] = re;
-    rr += re.x * re.x - re.y * re.y;
-    ri += 2 * re.x * re.y;
+    if constexpr (GRAD) {
+      u[e] = cmul(Sinv[e / K], re);
+    } else {
+      rr += re.x * re.x - re.y * re.y;
+      ri += 2 * re.x * re.y;
+    }
     ww += (re.x * re.x + re.y * re.y) * wd[e / K];
   }
-  block_reduce_rhs<K>(make_double2(rr, ri), smem, prho + (int64_t)blockIdx.x * K);
+  if constexpr (!GRAD) block_reduce_rhs<K>(make_double2(rr, ri), smem, prho + (int64_t)blockIdx.x * K);
   block_reduce_rhs<K>(make_double2(ww, 0.0), smem, pw + (int64_t)blockIdx.x * K);
   if (arrive_last(&ctl->counter)) {
     const int my = threadIdx.x < K ? threadIdx.x : 0;
-    const double2 rho = sum_partials<K>(prho, gridDim.x, my, smem);
+    double2 rho = make_double2(0.0, 0.0);
+    if constexpr (!GRAD) rho = sum_partials<K>(prho, gridDim.x, my, smem);
     const double2 w = sum_partials<K>(pw, gridDim.x, my, smem);
     __shared__ int any, stop;
     if (threadIdx.x == 0) { any = 0; stop = 0; }
@@ -214,17 +222,19 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(double2* __restrict__ y,
         S.its += 1;
         S.res = sqrt(w.x);
         if (!isfinite(S.res)) ctl->nonfinite = 1;
-        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
-          S.breakdown = 1;
-          S.active = 0;
-          S.beta = make_double2(0.0, 0.0);
-        } else {
-          S.beta = ddiv(rho, S.rho);
+        if constexpr (!GRAD) {
+          if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+            S.breakdown = 1;
+            S.active = 0;
+            S.beta = make_double2(0.0, 0.0);
+          } else {
+            S.beta = ddiv(rho, S.rho);
+          }
+          S.rho = rho;
         }
-        S.rho = rho;
         if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
         else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
-      } else {
+      } else if constexpr (!GRAD) {
         S.beta = make_double2(0.0, 0.0);
       }
       if (S.active) atomicOr(&any, 1);
@@ -301,7 +311,7 @@ __global__ void k_cg_xupdate(const double2* __restrict__ y, const double2* __res
     x[e] = dadd(x[e], cmul(S[e / K], y[e]));
 }
 
-size_t cg_layout(const Plan& P, size_t* off /* 20 */) {
+size_t cg_layout(const Plan& P, size_t* off /* 24 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   put(0, P.nnz * P.csize);                      // At (matrix precision)
@@ -325,6 +335,12 @@ size_t cg_layout(const Plan& P, size_t* off /* 20 */) {
   put(14, sorted ? sizeof(int32_t) * P.n : 0);
   put(15, sorted ? sizeof(uint64_t) * P.n : 0);
   put(16, sorted ? pg::sort_workspace_bytes(P.n) : 0);
+  // gradient correction: S^-1, diag(G^T A G)^-1, u = S^-1 r, t = invD G^T u, z
+  put(17, P.gn ? sizeof(double2) * P.n : 0);
+  put(20, P.gn ? sizeof(double2) * P.gn : 0);
+  put(21, P.gn ? sizeof(double2) * P.n * P.k : 0);
+  put(22, P.gn ? sizeof(double2) * P.gn * P.k : 0);
+  put(23, P.gn ? sizeof(double2) * P.n * P.k : 0);
   return o;
 }
 
@@ -362,7 +378,7 @@ void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, co
 template <typename CM>
 int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
              const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  size_t off[20];
+  size_t off[24];
   cg_layout(P, off);
   const bool bj = P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
@@ -387,6 +403,14 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   double* target = rnorm + P.k;
   int* want = reinterpret_cast<int*>(ws + off[13]);
   int* dstatus = want + P.k;
+  // gradient correction (diagonal Jacobi, complex128 only; checked by pg_cocg)
+  const bool grad = P.gn > 0;
+  double2* Sinv = reinterpret_cast<double2*>(ws + off[17]);
+  double2* invD = reinterpret_cast<double2*>(ws + off[20]);
+  double2* gu = reinterpret_cast<double2*>(ws + off[21]);
+  double2* gt = reinterpret_cast<double2*>(ws + off[22]);
+  double2* gz = reinterpret_cast<double2*>(ws + off[23]);
+  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   const int write_pm = same ? 0 : 1;
   const int k = P.k, nb = P.nb;
   // vector-update grid: at least ~4 elements per thread, so the per-block
@@ -416,6 +440,11 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   } else {
     k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
     k_cg_scale_matrix<CM><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
+    if (grad) {
+      k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n, Sinv);
+      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                       P.gn, invD);
+    }
   }
   PG_LAUNCH_CHECK();
   std::vector<double> bnorm(k), rn(k), tgt(k);
@@ -475,9 +504,19 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
     if (bj) PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, r64b)));
-    PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, pm, first ? 1 : 0,
-                                                             write_pm, part),
-                   k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    if (grad) {
+      // r = S r64, then z = r + S^-1 G invD G^T r64 (S^-1 r = r64), rho = r^T z
+      PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, pm, 0, write_pm, part),
+                     k_grad_restrict<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                     invD, r64, P.gn, gt, st, -1),
+                     k_grad_prolong<K><<<nb, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv, gt, r,
+                                                               P.n, gz, pv, first ? 1 : 0, part, st, ctl, -1),
+                     k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    } else {
+      PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, pm, first ? 1 : 0,
+                                                               write_pm, part),
+                     k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    }
     if (first && sorted && autotune_enabled()) {
       // the product is the first kernel of an iteration and recomputes alpha,
       // so timing the candidates on the live operands changes no state
@@ -494,9 +533,21 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     for (int it = 0; it < steps; ++it) {
       const int iter = (int)(launch_iter + it);
       launch_cg_spmv<CM>(P, rowptr, col, At, pm, pv, q, part, st, ctl, npr, spmv_grid, s, variant, perm);
-      PG_KSWITCH(k, (k_cg_update<CM, K><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter, delta),
-                     k_cg_pupdate<CM, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, pm, r, P.n, st, iter,
-                                                                                          write_pm)));
+      if (grad) {
+        PG_KSWITCH(k, (k_cg_update<CM, K, true><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl,
+                                                                        iter, delta, gu, Sinv),
+                       k_grad_restrict<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                       invD, gu, P.gn, gt, st, iter),
+                       k_grad_prolong<K><<<nbu, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv, gt,
+                                                                  r, P.n, gz, pv, 0, part, st, ctl, iter),
+                       k_cg_pupdate<CM, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, pm, gz, P.n, st,
+                                                                                            iter, write_pm)));
+      } else {
+        PG_KSWITCH(k, (k_cg_update<CM, K><<<nbu, kThreads, 0, s>>>(y, r, pv, q, wd, P.n, st, part, part2, ctl, iter,
+                                                                  delta),
+                       k_cg_pupdate<CM, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(pv, pm, r, P.n, st, iter,
+                                                                                            write_pm)));
+      }
     }
     PG_LAUNCH_CHECK();
     launch_iter += steps;
@@ -574,7 +625,7 @@ extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = cg_plan(n, nnz, nrhs, opts);
-  size_t off[20];
+  size_t off[24];
   if (opts->precision == 3) return ir_layout(P, off) + 256;
   return (opts->precision == 2 ? df_layout(P, off) : cg_layout(P, off)) + 256;
 }
@@ -586,6 +637,14 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
       opts->precision < 0 || opts->precision > 3) {
     pg_set_error("pg_cocg: bad argument (nrhs 1..32 power of two, rtol > 0, precision 0/1/2/3)");
     return PG_ERR_ARG;
+  }
+  if (opts->grad_rowptr) {
+    if (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row || !opts->gradt_val ||
+        opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0 || opts->precision != 0) {
+      pg_set_error("pg_cocg: gradient correction needs all six G arrays, grad_cols >= 1, precision 0 and diagonal "
+                   "Jacobi (block_p 0)");
+      return PG_ERR_ARG;
+    }
   }
   if (opts->block_p > 0) {
     const int64_t pp = opts->block_p;

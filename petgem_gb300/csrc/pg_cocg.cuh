@@ -130,6 +130,110 @@ __global__ void k_cg_cycle_init(const double2* prho, int nblocks, CgState* st, c
   }
 }
 
+// ----------------------------------------------------------------------------
+// Gradient correction (Hiptmair's hybrid smoother) on the Jacobi-scaled system
+// At = S A S:  z = r + S^-1 G diag(G^T A G)^-1 G^T S^-1 r, which is
+// B = D^-1 + G diag(G^T A G)^-1 G^T in the unscaled variables.  G is real;
+// its rows (CSR) drive the prolongation, its transpose (rows ascending) the
+// restriction, so both sums run in a fixed order.
+// ----------------------------------------------------------------------------
+
+__global__ void k_grad_sinv(const double2* S, int64_t n, double2* Sinv) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    Sinv[r] = ddiv(make_double2(1.0, 0.0), S[r]);
+}
+
+// true when some RHS ran this iteration's update (iter < 0: always)
+template <int K>
+__device__ __forceinline__ bool grad_due(const CgState* st, int iter) {
+  if (iter < 0) return true;
+  bool any = false;
+  for (int i = 0; i < K; ++i) any |= st[i].beta_iter == iter;
+  return any;
+}
+
+// t = invD .* (G^T u), u = S^-1 r (K RHS interleaved)
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_grad_restrict(const int64_t* __restrict__ gtp,
+                                                            const int32_t* __restrict__ gtr,
+                                                            const double* __restrict__ gtv,
+                                                            const double2* __restrict__ invD,
+                                                            const double2* __restrict__ u, int64_t gn,
+                                                            double2* __restrict__ t, const CgState* st, int iter) {
+  if (!grad_due<K>(st, iter)) return;
+  const int64_t total = gn * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / K;
+    const int rhs = (int)(e % K);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
+      const double g = gtv[j];
+      const double2 v = u[(int64_t)gtr[j] * K + rhs];
+      acc.x = fma(g, v.x, acc.x);
+      acc.y = fma(g, v.y, acc.y);
+    }
+    t[e] = cmul(invD[c], acc);
+  }
+}
+
+// z = r + S^-1 (G t); partial rho = r^T z.  iter >= 0 (inside an iteration):
+// the last block sets beta = rho / rho_old and rho for every RHS that ran
+// this iteration's update.  iter < 0 (cycle start): partials only, and p = z
+// when set_p.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_grad_prolong(const int64_t* __restrict__ gp,
+                                                           const int32_t* __restrict__ gc,
+                                                           const double* __restrict__ gv,
+                                                           const double2* __restrict__ Sinv,
+                                                           const double2* __restrict__ t,
+                                                           const double2* __restrict__ r, int64_t n,
+                                                           double2* __restrict__ z, double2* __restrict__ pv,
+                                                           int set_p, double2* prho, CgState* st, CgCtl* ctl,
+                                                           int iter) {
+  if (!grad_due<K>(st, iter)) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  double2 rho = make_double2(0.0, 0.0);
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const int64_t row = e / K;
+    const int rhs = (int)(e % K);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
+      const double g = gv[j];
+      const double2 v = t[(int64_t)gc[j] * K + rhs];
+      acc.x = fma(g, v.x, acc.x);
+      acc.y = fma(g, v.y, acc.y);
+    }
+    const double2 re = r[e];
+    const double2 ze = dadd(re, cmul(Sinv[row], acc));
+    z[e] = ze;
+    if (set_p) pv[e] = ze;
+    rho = dadd(rho, cmul(re, ze));
+  }
+  block_reduce_rhs<K>(rho, smem, prho + (int64_t)blockIdx.x * K);
+  if (iter >= 0 && arrive_last(&ctl->counter)) {
+    const double2 rr = sum_partials<K>(prho, gridDim.x, threadIdx.x < K ? threadIdx.x : 0, smem);
+    if (threadIdx.x < K) {
+      CgState& S = st[threadIdx.x];
+      if (S.beta_iter == iter) {
+        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.beta = make_double2(0.0, 0.0);
+        } else {
+          S.beta = ddiv(rr, S.rho);
+        }
+        S.rho = rr;
+      } else {
+        S.beta = make_double2(0.0, 0.0);
+      }
+    }
+    if (threadIdx.x == 0) ctl->counter = 0;
+  }
+}
+
 struct ToCM64 {
   __device__ double2 operator()(double2 v) const { return v; }
 };
@@ -338,6 +442,7 @@ inline Plan cg_plan(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* o) {
   Plan P{n, nnz, nrhs, 1, o->precision, nb, o->precision == 1 ? sizeof(float2) : sizeof(double2), BjInfo{}};
   P.bj = BjInfo{o->block_edges, o->block_faces, o->block_volumes, o->block_p, n};
   if (o->block_p < 1 || o->block_p > 6) P.bj.p = 0;
+  P.gn = o->grad_rowptr && o->grad_cols > 0 ? o->grad_cols : 0;
   return P;
 }
 
@@ -404,7 +509,7 @@ int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
 namespace pgk {
 
 // workspace layout of the double-float COCG (mf: several frequencies)
-size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf = false);
+size_t df_layout(const Plan& P, size_t* off /* 24 */, bool mf = false);
 // double-float COCG; col_scale (host [k]) selects the several-frequencies form
 int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,

@@ -660,7 +660,7 @@ void launch_df_spmm(int variant, int grid, cudaStream_t s, const int64_t* rowptr
 
 namespace pgk {
 
-size_t df_layout(const Plan& P, size_t* off /* 20 */, bool mf) {
+size_t df_layout(const Plan& P, size_t* off /* 24 */, bool mf) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   const size_t ns = mf ? (size_t)P.n * P.k : (size_t)P.n;   // scaling entries: per column with several frequencies
@@ -691,7 +691,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
                 const double* col_scale) {
   const bool mf = col_scale != nullptr;
-  size_t off[20];
+  size_t off[24];
   df_layout(P, off, mf);
   float4* ps = reinterpret_cast<float4*>(ws + off[14]);
   float4* Sdf = reinterpret_cast<float4*>(ws + off[15]);
@@ -1022,7 +1022,7 @@ extern "C" size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int 
   pg_cocg_default_opts(&o);
   o.precision = 2;
   Plan P = cg_plan(n, nnz, nrhs, &o);
-  size_t off[20];
+  size_t off[24];
   return df_layout(P, off, true) + 256;
 }
 

@@ -69,39 +69,6 @@ __global__ void k_tuple_of_elem(const int8_t* eo, const int8_t* fo, int64_t T, c
   }
 }
 
-// Gauss-Legendre nodes/weights on [0,1] by Newton iteration on P_n.
-__device__ void gauss_legendre01(int n, double* x, double* w) {
-  const double pi = 3.14159265358979323846;
-  for (int i = 0; i < n; ++i) {
-    double z = cos(pi * (i + 0.75) / (n + 0.5));
-    double dp = 1.0;
-    for (int it = 0; it < 100; ++it) {
-      double p0 = 1.0, p1 = z;
-      for (int k = 2; k <= n; ++k) {
-        double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-        p0 = p1;
-        p1 = pk;
-      }
-      // p1 = P_n(z), p0 = P_{n-1}(z)
-      dp = n * (z * p1 - p0) / (z * z - 1.0);
-      double dz = p1 / dp;
-      z -= dz;
-      if (fabs(dz) < 1e-16) break;
-    }
-    {
-      double p0 = 1.0, p1 = z;
-      for (int k = 2; k <= n; ++k) {
-        double pk = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-        p0 = p1;
-        p1 = pk;
-      }
-      dp = n * (z * p1 - p0) / (z * z - 1.0);
-    }
-    x[n - 1 - i] = 0.5 * (z + 1.0);
-    w[n - 1 - i] = 1.0 / ((1.0 - z * z) * dp * dp);  // 2/((1-z^2)P'^2) mapped to [0,1]
-  }
-}
-
 // One CTA per tuple.  Quadrature: collapsed Gauss-Legendre product rule with
 // n = p+2 points per direction, exact for the degree-2p integrands.
 // Points are evaluated chunk by chunk into shared memory; each thread owns a

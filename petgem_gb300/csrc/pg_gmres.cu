@@ -303,7 +303,72 @@ __global__ void k_scale_cols(const int32_t* col, const double2* val, int64_t nnz
     out[q] = cfrom<C>(cmul(val[q], dinv[col[q]]));
 }
 
-size_t ws_layout(const Plan& P, size_t* off /* 16 */) {
+// Gradient correction, right preconditioning B = D^-1 T with
+// T v = v + D G invD G^T v (invD = diag(G^T A G)^-1): the Arnoldi product is
+// Ahat (T v), Ahat = A D^-1, and the update x += D^-1 T (V y).
+// t = invD .* (G^T v)
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_gm_restrict(const int64_t* __restrict__ gtp,
+                                                          const int32_t* __restrict__ gtr,
+                                                          const double* __restrict__ gtv,
+                                                          const double2* __restrict__ invD,
+                                                          const C* __restrict__ v, int64_t gn,
+                                                          double2* __restrict__ t, const Ctl* ctl) {
+  if (ctl && !ctl->any_active) return;
+  const int64_t total = gn * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / K;
+    const int rhs = (int)(e % K);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
+      const double g = gtv[j];
+      const double2 x = to_d(v[(int64_t)gtr[j] * K + rhs]);
+      acc.x = fma(g, x.x, acc.x);
+      acc.y = fma(g, x.y, acc.y);
+    }
+    t[e] = cmul(invD[c], acc);
+  }
+}
+
+// u = v + d .* (G t)
+template <typename C, int K>
+__global__ void __launch_bounds__(kThreads) k_gm_prolong(const int64_t* __restrict__ gp,
+                                                         const int32_t* __restrict__ gc,
+                                                         const double* __restrict__ gv,
+                                                         const double2* __restrict__ d,
+                                                         const double2* __restrict__ t, const C* __restrict__ v,
+                                                         int64_t n, C* __restrict__ u, const Ctl* ctl) {
+  if (ctl && !ctl->any_active) return;
+  const int64_t total = n * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / K;
+    const int rhs = (int)(e % K);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
+      const double g = gv[j];
+      const double2 x = t[(int64_t)gc[j] * K + rhs];
+      acc.x = fma(g, x.x, acc.x);
+      acc.y = fma(g, x.y, acc.y);
+    }
+    u[e] = cfrom<C>(dadd(to_d(v[e]), cmul(d[row], acc)));
+  }
+}
+
+// x += dinv .* u
+template <int K>
+__global__ void k_gm_xadd(const double2* __restrict__ dinv, const double2* __restrict__ u, int64_t n,
+                          double2* __restrict__ x) {
+  const int64_t total = n * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    x[e] = dadd(x[e], cmul(dinv[e / K], u[e]));
+}
+
+__global__ void k_recip(const double2* a, int64_t n, double2* out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+    out[r] = ddiv(make_double2(1.0, 0.0), a[r]);
+}
+
+size_t ws_layout(const Plan& P, size_t* off /* 24 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   put(0, P.nnz * P.csize);                                   // Ahat
@@ -322,6 +387,12 @@ size_t ws_layout(const Plan& P, size_t* off /* 16 */) {
   put(13, sizeof(int));                                      // status
   put(14, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);    // block-Jacobi factors S
   put(15, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);    // block inverses M^-1
+  // gradient correction: invD, t, u = T v (Arnoldi precision), d = diag A, ones
+  put(16, P.gn ? sizeof(double2) * P.gn : 0);
+  put(17, P.gn ? sizeof(double2) * P.gn * P.k : 0);
+  put(18, P.gn ? P.csize * P.n * P.k : 0);
+  put(19, P.gn ? sizeof(double2) * P.n : 0);
+  put(20, P.gn ? sizeof(double2) * P.n : 0);
   return o;
 }
 
@@ -392,7 +463,7 @@ __global__ void k_bj_minv_apply_add(const double2* Minv, BjInfo B, const double2
 template <typename C>
 int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
               const pg_gmres_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  size_t off[16];
+  size_t off[24];
   ws_layout(P, off);
   C* Ahat = reinterpret_cast<C*>(ws + off[0]);
   double2* dinv = reinterpret_cast<double2*>(ws + off[1]);
@@ -415,6 +486,13 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   const bool bj = P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[14]);
   double2* Minv = reinterpret_cast<double2*>(ws + off[15]);
+  const bool grad = P.gn > 0;   // diagonal Jacobi and complex128 only (checked by pg_gmres)
+  double2* invD = reinterpret_cast<double2*>(ws + off[16]);
+  double2* gt = reinterpret_cast<double2*>(ws + off[17]);
+  C* gu = reinterpret_cast<C*>(ws + off[18]);
+  double2* dA = reinterpret_cast<double2*>(ws + off[19]);
+  double2* ones = reinterpret_cast<double2*>(ws + off[20]);
+  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
   if (bj) {
     // right preconditioning with the entity blocks' inverses: Ahat = A M^-1
@@ -435,6 +513,12 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   } else {
     k_diag_inv<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, dinv, dstatus);
     k_scale_cols<C><<<pg_blocks(P.nnz, 256), 256, 0, s>>>(col, A, P.nnz, dinv, Ahat);
+    if (grad) {
+      k_recip<<<pg_blocks(P.n, 256), 256, 0, s>>>(dinv, P.n, dA);
+      k_fill_one<<<pg_blocks(P.n, 256), 256, 0, s>>>(ones, P.n);
+      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                       P.gn, invD);
+    }
   }
   PG_LAUNCH_CHECK();
 
@@ -473,7 +557,15 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
     for (int j = 0; j < steps; ++j) {
       C* vj = V + (int64_t)j * stride;
       C* w = V + (int64_t)(j + 1) * stride;
-      launch_spmv<C>(P, rowptr, col, Ahat, vj, w, nullptr, ctl, npr, ss);
+      if (grad) {
+        PG_KSWITCH(k, (k_gm_restrict<C, K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                         invD, vj, P.gn, gt, ctl),
+                       k_gm_prolong<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(
+                           o->grad_rowptr, o->grad_col, o->grad_val, dA, gt, vj, P.n, gu, ctl)));
+        launch_spmv<C>(P, rowptr, col, Ahat, gu, w, nullptr, ctl, npr, ss);
+      } else {
+        launch_spmv<C>(P, rowptr, col, Ahat, vj, w, nullptr, ctl, npr, ss);
+      }
       const int passes = o->reorth ? 2 : 1;
       for (int pass = 0; pass < passes; ++pass) {
         PG_KSWITCH(k, (k_dots<C, K><<<nb, kThreads, 0, ss>>>(V, stride, w, P.n, j, dpart, ctl),
@@ -578,6 +670,19 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
                      k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n,
                                                                                         ycoef, dinv, r),
                      k_bj_minv_apply_add<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Minv, P.bj, r, x)));
+    } else if (grad) {
+      // x += D^-1 T (V y): V y into r (free until the next true residual), T into gu, then scale and add
+      PG_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(double2) * P.n * k, s));
+      PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
+                     k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n,
+                                                                                        ycoef, ones, r),
+                     k_gm_restrict<double2, K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row,
+                                                                             o->gradt_val, invD, r, P.gn, gt, nullptr),
+                     k_gm_prolong<double2, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(
+                         o->grad_rowptr, o->grad_col, o->grad_val, dA, gt, r, P.n, reinterpret_cast<double2*>(gu),
+                         nullptr),
+                     k_gm_xadd<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(
+                         dinv, reinterpret_cast<double2*>(gu), P.n, x)));
     } else {
       PG_KSWITCH(k, (k_backsolve<K><<<1, 32, 0, s>>>(st, m, ycoef),
                      k_update_x<C, K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, s>>>(V, stride, steps, P.n,
@@ -633,13 +738,14 @@ static Plan gmres_plan(int64_t n, int64_t nnz, int nrhs, const pg_gmres_opts* o)
   Plan P{n, nnz, nrhs, o->restart, o->precision, pick_blocks(n, nrhs),
          o->precision ? sizeof(float2) : sizeof(double2)};
   if (o->block_p >= 1 && o->block_p <= 6) P.bj = BjInfo{o->block_edges, o->block_faces, o->block_volumes, o->block_p, n};
+  P.gn = o->grad_rowptr && o->grad_cols > 0 ? o->grad_cols : 0;
   return P;
 }
 
 extern "C" size_t pg_gmres_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_gmres_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = gmres_plan(n, nnz, nrhs, opts);
-  size_t off[16];
+  size_t off[24];
   return ws_layout(P, off) + 256;
 }
 
@@ -654,6 +760,14 @@ extern "C" int pg_gmres(const int64_t* rowptr, const int32_t* col, const double*
       (opts->precision != 0 && opts->precision != 1)) {
     pg_set_error("pg_gmres: restart must be 1..64, rtol > 0, precision 0 or 1");
     return PG_ERR_ARG;
+  }
+  if (opts->grad_rowptr) {
+    if (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row || !opts->gradt_val ||
+        opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0 || opts->precision != 0) {
+      pg_set_error("pg_gmres: gradient correction needs all six G arrays, grad_cols >= 1, precision 0 and diagonal "
+                   "Jacobi (block_p 0)");
+      return PG_ERR_ARG;
+    }
   }
   if (opts->block_p > 0) {
     const int64_t pp = opts->block_p;

@@ -29,6 +29,7 @@ struct Plan {
   int nb;             // reduction blocks
   size_t csize;       // sizeof Arnoldi complex
   BjInfo bj;          // COCG entity block-Jacobi (bj.p == 0: diagonal Jacobi)
+  int64_t gn = 0;     // gradient correction (COCG, GMRES): columns of G (0: off)
 };
 
 }  // namespace pgk
@@ -254,6 +255,40 @@ void launch_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, const
   }
 
 bool valid_k(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32; }
+
+// Gradient correction shared by COCG and GMRES: G (real, DOF rows x H1
+// columns, from pg_gradient_map) and its transpose (rows ascending).
+// invD[phi] = 1 / (G^T A G)_{phi phi} (0 for an empty or vanishing column).
+// (A G_phi)_r = sum_k A_rk G_{k phi}; G_{k phi} is looked up by binary search
+// in the transpose row of phi.
+__global__ void k_grad_diag(const int64_t* rowptr, const int32_t* col, const double2* A, const int64_t* gtp,
+                            const int32_t* gtr, const double* gtv, int64_t gn, double2* invD) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < gn; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lo = gtp[c], hi = gtp[c + 1];
+    double2 d = make_double2(0.0, 0.0);
+    for (int64_t j = lo; j < hi; ++j) {
+      const int64_t r = gtr[j];
+      double2 acc = make_double2(0.0, 0.0);
+      for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+        const int32_t s = col[k];
+        int64_t a = lo, b = hi;
+        while (a < b) {
+          const int64_t m = (a + b) >> 1;
+          if (gtr[m] < s) a = m + 1;
+          else b = m;
+        }
+        if (a < hi && gtr[a] == s) {
+          acc.x = fma(A[k].x, gtv[a], acc.x);
+          acc.y = fma(A[k].y, gtv[a], acc.y);
+        }
+      }
+      d.x = fma(gtv[j], acc.x, d.x);
+      d.y = fma(gtv[j], acc.y, d.y);
+    }
+    invD[c] = (d.x == 0.0 && d.y == 0.0) ? make_double2(0.0, 0.0) : ddiv(make_double2(1.0, 0.0), d);
+  }
+}
+
 
 
 }  // namespace

@@ -16,7 +16,7 @@ void pg_set_cuda_error(cudaError_t e) {
   snprintf(g_last_error, sizeof(g_last_error), "CUDA error %d: %s", (int)e, cudaGetErrorString(e));
 }
 
-extern "C" int pg_abi_version(void) { return 3; }
+extern "C" int pg_abi_version(void) { return 4; }
 
 extern "C" const char* pg_last_error(void) { return g_last_error; }
 

@@ -239,6 +239,31 @@ class DeviceMesh:
             self._pec_mask = f
         return self._pec_mask
 
+    def gradient_map(self):
+        """The mesh's discrete gradient G and its transpose (pg_gradient_map;
+        built once, p <= 3), with the columns of H1 functions that touch a PEC
+        DOF dropped: the gradient correction of ``solve(precond="grad")``."""
+        if getattr(self, "_grad", None) is None:
+            dev = self.device
+            nc, me = ctypes.c_int64(), ctypes.c_int64()
+            _lib.call("pg_gradient_map_sizes", self.n_nodes, self.nE, self.nF, self.T, self.p, ctypes.byref(nc),
+                      ctypes.byref(me))
+            nc, me = int(nc.value), int(me.value)
+            g = GradientMap(nc, torch.empty(self.N + 1, dtype=torch.int64, device=dev),
+                            torch.empty(me, dtype=torch.int32, device=dev),
+                            torch.empty(me, dtype=torch.float64, device=dev),
+                            torch.empty(nc + 1, dtype=torch.int64, device=dev),
+                            torch.empty(me, dtype=torch.int32, device=dev),
+                            torch.empty(me, dtype=torch.float64, device=dev))
+            ws = _ws(_lib.query("pg_gradient_map_workspace_bytes", self.n_nodes, self.nE, self.nF, self.T,
+                                self.n_tuples, self.p), dev)
+            _lib.call("pg_gradient_map", _p(self.elemsN), _p(self.elemsE), _p(self.elemsF), _p(self.dofs),
+                      _p(self.tuple_of_elem), _p(self.codes), self.n_tuples, self.T, self.n_nodes, self.nE, self.nF,
+                      self.p, _p(self.pec_mask()), _p(g.rowptr), _p(g.col), _p(g.val), _p(g.t_rowptr), _p(g.t_row),
+                      _p(g.t_val), _p(ws), ws.numel(), _s())
+            self._grad = g
+        return self._grad
+
     def records(self):
         """Assembly records (once per mesh): output / transpose position,
         first member and PEC flags of every item of the work list."""
@@ -351,11 +376,15 @@ class DeviceMesh:
               raise_on_fail=True, ksp="gmres", check_every=50, precond="block", inner_rtol=1e-2):
         """Solve A x = b for this mesh's CSR pattern (see solve_csr).
         precond="block": entity block-Jacobi (each edge / face / volume's
-        diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal."""
+        diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal;
+        "grad": diagonal Jacobi plus the gradient correction
+        D^-1 + G diag(G^T A G)^-1 G^T (COCG and GMRES in fp64, p <= 3;
+        gradient_map)."""
         blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" else None
+        gradient = self.gradient_map() if precond == "grad" else None
         return solve_csr(self.rowptr, self.col, vals, b, x0=x0, rtol=rtol, restart=restart, max_it=max_it,
                          precision=precision, reorth=reorth, raise_on_fail=raise_on_fail, ksp=ksp,
-                         check_every=check_every, blocks=blocks, inner_rtol=inner_rtol)
+                         check_every=check_every, blocks=blocks, inner_rtol=inner_rtol, gradient=gradient)
 
     def solve_frequencies(self, vals0, frequency0, b, frequencies, **kw):
         """Columns of b (complex128 [N, k]) at their own frequencies in one
@@ -511,6 +540,31 @@ class DeviceMesh:
         return y
 
 
+class GradientMap:
+    """Discrete gradient G (CSR, real, rows = H(curl) DOFs, n_cols H1
+    columns) and its transpose, as pg_gradient_map writes them."""
+
+    def __init__(self, n_cols, rowptr, col, val, t_rowptr, t_row, t_val):
+        self.n_cols = n_cols
+        self.rowptr, self.col, self.val = rowptr, col, val
+        self.t_rowptr, self.t_row, self.t_val = t_rowptr, t_row, t_val
+
+    @property
+    def nnz(self):
+        return int(self.rowptr[-1].item())
+
+
+def _n_rows(rowptr):
+    return int(rowptr.numel()) - 1
+
+
+def _set_gradient(o, g):
+    """Point solver options (pg_cocg_opts / pg_gmres_opts) at a GradientMap."""
+    o.grad_cols = g.n_cols
+    o.grad_rowptr, o.grad_col, o.grad_val = _p(g.rowptr), _p(g.col), _p(g.val)
+    o.gradt_rowptr, o.gradt_row, o.gradt_val = _p(g.t_rowptr), _p(g.t_row), _p(g.t_val)
+
+
 def _check_csr(name, rowptr, col, vals, b):
     """CSR system on the GPU: rowptr int64 [N+1], col int32 [nnz], vals
     complex128 [nnz], b complex128 [N] or [N, k]; raises ValueError before
@@ -545,7 +599,7 @@ def _new_x(name, b, x0):
 
 
 def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True, ksp="gmres", check_every=50, blocks=None, inner_rtol=1e-2):
+              raise_on_fail=True, ksp="gmres", check_every=50, blocks=None, inner_rtol=1e-2, gradient=None):
     """Solve A x = b for a CSR matrix on the GPU (rowptr int64 [N+1], col
     int32 [nnz], vals complex128 [nnz]); b complex128 [N] or [N, k]
     (k in 1,2,4,8,16,32).  The KSPSolve of petgem/solver.py:584-594.
@@ -564,8 +618,16 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     S A S^T (S = D^-1/2 L^-1 per block), GMRES on A M^-1 (M^-1 = A_aa^-1 per
     block, right preconditioning: PETSc -pc_type bjacobi with one block per
     edge / face / element).
+    gradient: a GradientMap (DeviceMesh.gradient_map) for the gradient
+    correction: the preconditioner D^-1 + G diag(G^T A G)^-1 G^T (fp64,
+    diagonal Jacobi; GMRES applies it on the right).
     """
     _check_csr(f"solve_csr({ksp})", rowptr, col, vals, b)
+    if gradient is not None:
+        if blocks is not None:
+            raise ValueError("the gradient correction is implemented with diagonal Jacobi (blocks=None)")
+        if int(gradient.rowptr.numel()) != _n_rows(rowptr) + 1:
+            raise ValueError("solve_csr: the gradient map's rows do not match the matrix")
     N = int(rowptr.numel()) - 1
     nnz = int(col.numel())
     nrhs = 1 if b.ndim == 1 else int(b.shape[1])
@@ -582,6 +644,8 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
         o.restart, o.max_it, o.rtol, o.precision, o.reorth = int(restart), int(max_it), float(rtol), prec, int(reorth)
         if blocks is not None:
             o.block_p, o.block_edges, o.block_faces, o.block_volumes = (int(v) for v in blocks)
+        if gradient is not None:
+            _set_gradient(o, gradient)
         nbytes = _lib.query("pg_gmres_workspace_bytes", N, nnz, nrhs, ctypes.byref(o))
         fn = lib.pg_gmres
     elif ksp == "cocg":
@@ -591,6 +655,8 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
         o.inner_rtol = float(inner_rtol)
         if blocks is not None:
             o.block_p, o.block_edges, o.block_faces, o.block_volumes = (int(v) for v in blocks)
+        if gradient is not None:
+            _set_gradient(o, gradient)
         nbytes = _lib.query("pg_cocg_workspace_bytes", N, nnz, nrhs, ctypes.byref(o))
         fn = lib.pg_cocg
     else:

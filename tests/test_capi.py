@@ -32,7 +32,7 @@ def test_ctypes_signatures_cover_header():
 
 def test_host_queries():
     lib = _lib.load()
-    assert lib.pg_abi_version() == 3
+    assert lib.pg_abi_version() == 4
     assert _lib.query("pg_table_doubles", 2) == 12 * 20 * 21 // 2
     assert _lib.query("pg_table_doubles", 7) == 0
     assert _lib.query("pg_pattern_local_entities", 1) == 6

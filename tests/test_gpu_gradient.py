@@ -1,0 +1,170 @@
+"""GPU discrete gradient and the gradient-corrected COCG.
+
+* pg_gradient_map equals the oracle's map (oracle/gradient.py) entry for
+  entry (values within 1e-12; the coefficients are O(1)), for p = 1..3 on a
+  jittered box and on petgem's unstructured test mesh; its transpose is G^T
+  bit for bit with rows ascending; two builds are bitwise equal.
+* At larger sizes the map is checked through a size-independent property:
+  K G = 0, seen as A(f1) G f2 - A(f2) G f1 = (f2 - f1) K G on two assembled
+  systems.
+* COCG with the correction B = D^-1 + G diag(G^T A G)^-1 G^T reaches the
+  true 1e-10 residual in far fewer iterations than Jacobi alone, with the
+  same solution (1 and 4 RHS), and is deterministic.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from oracle import gradient
+from petgem_gb300 import synthetic
+from tests.helpers import load_test_mesh, rel_norm
+
+pytestmark = pytest.mark.gpu
+
+MAP_TOL = 1e-12
+
+
+def _mesh(nodes, tets, p, pattern=True):
+    from petgem_gb300.engine import DeviceMesh
+    return DeviceMesh(nodes, tets, p, pattern=pattern)
+
+
+def _box(n):
+    nodes, tets = synthetic.kuhn_box(n)
+    lo, hi = (-1000.0,) * 3, (1000.0,) * 3
+    return synthetic.jitter_interior(nodes, n, 0.15, 0, lo, hi), tets
+
+
+def _g_csr(g, n_rows):
+    rp = g.rowptr.cpu().numpy()
+    nnz = int(rp[-1])
+    return sp.csr_matrix((g.val[:nnz].cpu().numpy(), g.col[:nnz].cpu().numpy().astype(np.int64), rp),
+                         shape=(n_rows, g.n_cols))
+
+
+def _gt_csr(g, n_rows):
+    rp = g.t_rowptr.cpu().numpy()
+    nnz = int(rp[-1])
+    return sp.csr_matrix((g.t_val[:nnz].cpu().numpy(), g.t_row[:nnz].cpu().numpy().astype(np.int64), rp),
+                         shape=(g.n_cols, n_rows))
+
+
+def _a_csr(m, vals):
+    return sp.csr_matrix((vals.cpu().numpy(), m.col.cpu().numpy().astype(np.int64), m.rowptr.cpu().numpy()),
+                         shape=(m.N, m.N))
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+@pytest.mark.parametrize("case", ["box3", "test_mesh"])
+def test_gradient_map_matches_oracle(case, p):
+    nodes, tets = _box(3) if case == "box3" else load_test_mesh()[:2]
+    m = _mesh(nodes, tets, p, pattern=False)
+    g = m.gradient_map()
+    G = _g_csr(g, m.N)
+    Go, res = gradient.gradient_map(tets, m.elemsE.cpu().numpy(), m.elemsF.cpu().numpy(), m.eo.cpu().numpy(),
+                                    m.fo.cpu().numpy(), m.dofs.cpu().numpy(), m.N, len(nodes), p,
+                                    pec=m.bnd.cpu().numpy())
+    assert res < 1e-12
+    assert g.n_cols == Go.shape[1]
+    Gs = G.copy()
+    Gs.sort_indices()
+    assert Gs.nnz == Go.nnz
+    assert np.array_equal(Gs.indptr, Go.indptr) and np.array_equal(Gs.indices, Go.indices)
+    assert np.abs(Gs.data - Go.data).max() <= MAP_TOL
+    # the transpose: G^T exactly, each row ascending
+    Gt = _gt_csr(g, m.N)
+    assert np.array_equal(Gt.indptr, G.T.tocsr().indptr)
+    for c in range(0, g.n_cols, max(1, g.n_cols // 200)):
+        rows = Gt.indices[Gt.indptr[c]:Gt.indptr[c + 1]]
+        assert (np.diff(rows) > 0).all()
+    assert (Gt - G.T).count_nonzero() == 0
+    # deterministic: a second build on a fresh mesh object is bitwise equal
+    m2 = _mesh(nodes, tets, p, pattern=False)
+    g2 = m2.gradient_map()
+    n = g.nnz
+    assert torch.equal(g.rowptr, g2.rowptr) and torch.equal(g.t_rowptr, g2.t_rowptr)
+    for a, b in ((g.col, g2.col), (g.val, g2.val), (g.t_row, g2.t_row), (g.t_val, g2.t_val)):
+        assert torch.equal(a[:n], b[:n])
+
+
+@pytest.mark.parametrize("p,n", [(2, 10), (3, 6)])
+def test_gradient_map_is_curl_free_at_size(p, n):
+    mdl = synthetic.csem_two_layer(n, p)
+    m = _mesh(mdl.nodes, mdl.tets, p)
+    G = _g_csr(m.gradient_map(), m.N)
+    A1 = _a_csr(m, m.assemble(mdl.sigma, 1.0, pec=True))
+    A4 = _a_csr(m, m.assemble(mdl.sigma, 4.0, pec=True))
+    R = (A1 @ G) * 4.0 - (A4 @ G)          # = 3 K G
+    assert abs(R).max() <= 3e-12 * abs(A1).max()
+    assert abs(A1 @ G).max() >= 1e-6 * abs(A1).max()   # the mass part is there
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_cocg_gradient_correction_matches_jacobi(p, monkeypatch):
+    mdl = synthetic.csem_two_layer(6, p)
+    m = _mesh(mdl.nodes, mdl.tets, p)
+    vals = m.assemble(mdl.sigma, 1.0, pec=True)
+    bs = []
+    for x0 in (-500.0, 0.0, 250.0, 600.0):
+        b, _ = m.source_vector(dict(mdl.source, position=[x0, 20.0, 50.0]))
+        m.pec_rhs(b)
+        bs.append(b)
+    for rhs in (bs[1], torch.stack(bs, 1).contiguous()):
+        xj, ij = m.solve(vals, rhs, ksp="cocg", precond="jacobi", rtol=1e-10, max_it=100000)
+        xg, ig = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000)
+        assert ig.status == 0 and max(ig.relres_per_rhs) <= 1e-10
+        assert ig.iterations * 3 < ij.iterations, (ig.iterations, ij.iterations)
+        assert rel_norm(xg.cpu().numpy(), xj.cpu().numpy()) <= 1e-7
+        # bitwise repeatable with the product variant fixed (with one RHS the
+        # autotuner picks the lanes per row by timing, and each variant sums
+        # in its own order)
+        monkeypatch.setenv("PG_AUTOTUNE", "0")
+        xa, ia = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000)
+        xb, ib = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000)
+        monkeypatch.delenv("PG_AUTOTUNE")
+        assert ia.iterations == ib.iterations and torch.equal(xa, xb)
+
+
+@pytest.mark.parametrize("restart", [30])
+def test_gmres_gradient_correction(restart, monkeypatch):
+    """petgem's KSP, GMRES(30), right-preconditioned with the correction:
+    the true 1e-9 residual in far fewer steps than with Jacobi alone, the
+    COCG solution, and restart cycles replayed from a CUDA graph equal to
+    direct launches bit for bit (1 and 4 RHS)."""
+    mdl = synthetic.csem_two_layer(6, 2)
+    m = _mesh(mdl.nodes, mdl.tets, 2)
+    vals = m.assemble(mdl.sigma, 1.0, pec=True)
+    bs = []
+    for x0 in (-500.0, 0.0, 250.0, 600.0):
+        b, _ = m.source_vector(dict(mdl.source, position=[x0, 20.0, 50.0]))
+        m.pec_rhs(b)
+        bs.append(b)
+    for rhs in (bs[1], torch.stack(bs, 1).contiguous()):
+        xc, _ = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-11, max_it=100000)
+        monkeypatch.setenv("PG_GRAPHS", "1")
+        xg, ig = m.solve(vals, rhs, ksp="gmres", restart=restart, precond="grad", rtol=1e-9, max_it=20000)
+        assert ig.status == 0 and max(ig.relres_per_rhs) <= 1e-9
+        assert rel_norm(xg.cpu().numpy(), xc.cpu().numpy()) <= 1e-6
+        xj, ij = m.solve(vals, rhs, ksp="gmres", restart=restart, precond="jacobi", rtol=1e-9, max_it=20000,
+                         raise_on_fail=False)
+        assert ig.iterations * 3 < ij.iterations, (ig.iterations, ij.iterations)
+        monkeypatch.setenv("PG_GRAPHS", "0")
+        xd, idd = m.solve(vals, rhs, ksp="gmres", restart=restart, precond="grad", rtol=1e-9, max_it=20000)
+        assert idd.iterations == ig.iterations and torch.equal(xg, xd)
+
+
+def test_gradient_correction_rejects_other_forms():
+    from petgem_gb300 import _lib
+    from petgem_gb300.engine import solve_csr
+    mdl = synthetic.csem_two_layer(3, 2)
+    m = _mesh(mdl.nodes, mdl.tets, 2)
+    vals = m.assemble(mdl.sigma, 1.0, pec=True)
+    b, _ = m.source_vector(mdl.source)
+    g = m.gradient_map()
+    with pytest.raises(ValueError):
+        solve_csr(m.rowptr, m.col, vals, b, ksp="cocg", blocks=(2, m.nE, m.nF, m.T), gradient=g)
+    for ksp in ("cocg", "gmres"):
+        with pytest.raises(_lib.PetgemError) as e:
+            solve_csr(m.rowptr, m.col, vals, b, ksp=ksp, precision="mixed", gradient=g)
+        assert e.value.status == -1

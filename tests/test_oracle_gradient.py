@@ -1,0 +1,58 @@
+"""The gradient map's oracle, pinned by its defining properties (petgem has no
+counterpart to check against): every column of G is exactly representable in
+petgem's H(curl) basis, petgem's curl-curl matrix annihilates it (K G = 0,
+petgem/hvfem.py:223-316), and the mass matrix does not; rows are unique per
+DOF and PEC columns are dropped."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import gradient, system
+from petgem_gb300 import synthetic
+
+
+def _box(n=3):
+    nodes, tets = synthetic.kuhn_box(n)
+    lo, hi = (-1000.0,) * 3, (1000.0,) * 3
+    return synthetic.jitter_interior(nodes, n, 0.15, 0, lo, hi), tets
+
+
+def _global(mats, dofs, N):
+    T, nd = dofs.shape
+    rows = np.repeat(dofs, nd, axis=1).reshape(-1)
+    cols = np.tile(dofs, (1, nd)).reshape(-1)
+    return sp.coo_matrix((mats.reshape(-1), (rows, cols)), shape=(N, N)).tocsr()
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_gradient_columns_are_curl_free_gradients(p):
+    nodes, tets = _box()
+    mm = system.mesh_maps(nodes, tets, p)
+    M, K = system.element_matrices(nodes[tets], mm["eo"], mm["fo"], np.ones((len(tets), 2)), p, processes=1)
+    Kg, Mg = _global(K, mm["dofs"], mm["N"]), _global(M, mm["dofs"], mm["N"])
+    G, res = gradient.gradient_map(tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"],
+                                   len(nodes), p)
+    assert res < 1e-12
+    nE, nF = int(mm["elemsE"].max()) + 1, int(mm["elemsF"].max()) + 1
+    n_cols = {1: 64, 2: 64 + nE, 3: 64 + 2 * nE + nF}[p]   # 3^3 box: 64 nodes
+    assert G.shape == (mm["N"], n_cols)
+    assert abs(Kg @ G).max() <= 1e-12 * abs(Kg).max()
+    # a gradient has mass: M G is not small
+    assert abs(Mg @ G).max() >= 0.1 * abs(Mg).max()
+    # every column is used
+    assert (np.diff(G.tocsc().indptr) > 0).all()
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_gradient_pec_columns_dropped(p):
+    nodes, tets = _box()
+    mm = system.mesh_maps(nodes, tets, p)
+    G, _ = gradient.gradient_map(tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"],
+                                 len(nodes), p, pec=mm["bnd"])
+    assert G[mm["bnd"]].nnz == 0
+    kept = np.diff(G.tocsc().indptr) > 0
+    G0, _ = gradient.gradient_map(tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"],
+                                  len(nodes), p)
+    touched = np.unique(G0[mm["bnd"]].indices)
+    assert kept.sum() == G0.shape[1] - len(touched)
+    assert kept[:64].sum() == 8   # interior vertices of the 3^3 box
