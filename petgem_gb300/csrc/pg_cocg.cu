@@ -467,6 +467,7 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
   int chunk = o->check_every > 0 ? o->check_every : 50;
   bool first = true;
   int64_t launch_iter = 1;
+  std::vector<int> rec_done(k, 0);
   for (;;) {
     launch_spmv<double2>(P, rowptr, col, A, x, r64, b, nullptr, npr, s);
     PG_KSWITCH(k, (k_norm2<K><<<nb, kThreads, 0, s>>>(r64, P.n, part),
@@ -501,10 +502,31 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
       status = PG_ERR_NOT_CONVERGED;
       break;
     }
+    if (grad) {
+      bool stalled = false, live = false;
+      for (int i = 0; i < k; ++i) {
+        if (!wnt[i]) continue;
+        if (rec_done[i]) {
+          stalled = true;
+          wnt[i] = 0;
+        } else {
+          live = true;
+        }
+      }
+      if (stalled && !live) {
+        pg_set_error("pg_cocg: the recurrence reached rtol but the true residual did not (attainable accuracy of "
+                     "the system in FP64)");
+        status = PG_ERR_NOT_CONVERGED;
+        break;
+      }
+    }
     PG_CUDA_TRY(cudaMemcpyAsync(target, tgt.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     PG_CUDA_TRY(cudaMemcpyAsync(want, wnt.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
     if (bj) PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, r64b)));
-    if (grad) {
+    if (grad && !first) {
+      PG_CUDA_TRY(cudaMemsetAsync(y, 0, sizeof(double2) * P.n * k, s));
+      PG_KSWITCH(k, (k_cg_cycle_keep<K><<<1, 32, 0, s>>>(st, target, want, ctl)));
+    } else if (grad) {
       // r = S r64, then z = r + S^-1 G invD G^T r64 (S^-1 r = r64), rho = r^T z
       PG_KSWITCH(k, (k_cg_start<CM, K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, pm, 0, write_pm, part),
                      k_grad_restrict<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
@@ -558,11 +580,18 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     }
     std::vector<int> hits(k);
     std::vector<int> hbrk(k);
+    std::vector<int> hact(k);
     for (int i = 0; i < k; ++i) {
       PG_CUDA_TRY(cudaMemcpyAsync(&hits[i], &st[i].its, sizeof(int), cudaMemcpyDeviceToHost, s));
       PG_CUDA_TRY(cudaMemcpyAsync(&hbrk[i], &st[i].breakdown, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA_TRY(cudaMemcpyAsync(&hact[i], &st[i].active, sizeof(int), cudaMemcpyDeviceToHost, s));
     }
     PG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (grad) {
+      // a recurrence that met its target ends; if its true residual then
+      // misses rtol, the attainable accuracy is reached (checked below)
+      for (int i = 0; i < k; ++i) rec_done[i] = rec_done[i] || (wnt[i] && !hact[i]);
+    }
     int used = 0;
     for (int i = 0; i < k; ++i) used = hits[i] > used ? hits[i] : used;
     const int64_t cycle_its = used - its;
@@ -602,7 +631,7 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     res->relres = worst;
     res->status = status;
   }
-  if (status == PG_ERR_NOT_CONVERGED) pg_set_error("pg_cocg: max_it reached before rtol");
+  if (status == PG_ERR_NOT_CONVERGED && its >= max_it) pg_set_error("pg_cocg: max_it reached before rtol");
   return status;
 }
 

@@ -143,6 +143,33 @@ __global__ void k_grad_sinv(const double2* S, int64_t n, double2* Sinv) {
     Sinv[r] = ddiv(make_double2(1.0, 0.0), S[r]);
 }
 
+// Gradient correction, later cycles: the recurrence continues (r, p, rho,
+// the residual estimate are kept; y restarts at 0 after x += S y) instead
+// of restarting from the true residual.  Replacing r by b - A x would inject
+// the true residual's rounding in the directions the correction amplifies
+// (gradient fields of nearly non-conducting regions, where invD is largest),
+// which can make the iteration diverge; the FP64 recurrence needs no
+// replacement.  RHS whose true residual converged stop (want = 0).
+template <int K>
+__global__ void k_cg_cycle_keep(CgState* st, const double* target, const int* want, CgCtl* ctl) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    CgState& S = st[threadIdx.x];
+    S.target = target[threadIdx.x];
+    S.res0 = S.res;
+    S.active = want[threadIdx.x] && S.active;
+    if (S.active) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->any_active = any;
+    ctl->nonfinite = 0;
+    ctl->counter = 0;
+  }
+}
+
 // true when some RHS ran this iteration's update (iter < 0: always)
 template <int K>
 __device__ __forceinline__ bool grad_due(const CgState* st, int iter) {

@@ -239,11 +239,14 @@ class DeviceMesh:
             self._pec_mask = f
         return self._pec_mask
 
-    def gradient_map(self):
+    def gradient_map(self, pec=True):
         """The mesh's discrete gradient G and its transpose (pg_gradient_map;
-        built once, p <= 3), with the columns of H1 functions that touch a PEC
-        DOF dropped: the gradient correction of ``solve(precond="grad")``."""
-        if getattr(self, "_grad", None) is None:
+        built once per variant, p <= 3): the gradient correction of
+        ``solve(precond="grad")``.  pec=True drops the columns of H1 functions
+        that touch a PEC DOF (CSEM systems, PEC applied); pec=False keeps
+        every column (MT systems, whose boundary DOFs stay unknowns)."""
+        cache = self.__dict__.setdefault("_grad", {})
+        if bool(pec) not in cache:
             dev = self.device
             nc, me = ctypes.c_int64(), ctypes.c_int64()
             _lib.call("pg_gradient_map_sizes", self.n_nodes, self.nE, self.nF, self.T, self.p, ctypes.byref(nc),
@@ -259,10 +262,10 @@ class DeviceMesh:
                                 self.n_tuples, self.p), dev)
             _lib.call("pg_gradient_map", _p(self.elemsN), _p(self.elemsE), _p(self.elemsF), _p(self.dofs),
                       _p(self.tuple_of_elem), _p(self.codes), self.n_tuples, self.T, self.n_nodes, self.nE, self.nF,
-                      self.p, _p(self.pec_mask()), _p(g.rowptr), _p(g.col), _p(g.val), _p(g.t_rowptr), _p(g.t_row),
-                      _p(g.t_val), _p(ws), ws.numel(), _s())
-            self._grad = g
-        return self._grad
+                      self.p, _p(self.pec_mask()) if pec else None, _p(g.rowptr), _p(g.col), _p(g.val),
+                      _p(g.t_rowptr), _p(g.t_row), _p(g.t_val), _p(ws), ws.numel(), _s())
+            cache[bool(pec)] = g
+        return cache[bool(pec)]
 
     def records(self):
         """Assembly records (once per mesh): output / transpose position,
@@ -373,15 +376,17 @@ class DeviceMesh:
         return vals, b
 
     def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True, ksp="gmres", check_every=50, precond="block", inner_rtol=1e-2):
+              raise_on_fail=True, ksp="gmres", check_every=50, precond="block", inner_rtol=1e-2, pec=True):
         """Solve A x = b for this mesh's CSR pattern (see solve_csr).
         precond="block": entity block-Jacobi (each edge / face / volume's
         diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal;
         "grad": diagonal Jacobi plus the gradient correction
         D^-1 + G diag(G^T A G)^-1 G^T (COCG and GMRES in fp64, p <= 3;
-        gradient_map)."""
+        gradient_map; pec=False for systems without PEC rows, e.g. MT)."""
+        if precond not in ("block", "jacobi", "grad"):
+            raise ValueError(f"unknown preconditioner {precond!r} (block, jacobi, grad)")
         blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" else None
-        gradient = self.gradient_map() if precond == "grad" else None
+        gradient = self.gradient_map(pec) if precond == "grad" else None
         return solve_csr(self.rowptr, self.col, vals, b, x0=x0, rtol=rtol, restart=restart, max_it=max_it,
                          precision=precision, reorth=reorth, raise_on_fail=raise_on_fail, ksp=ksp,
                          check_every=check_every, blocks=blocks, inner_rtol=inner_rtol, gradient=gradient)

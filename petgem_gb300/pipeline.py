@@ -146,11 +146,17 @@ class Solver:
         if ksp not in ("gmres", "cocg"):
             raise ValueError(f"-ksp_type {ksp}: supported types are gmres and cocg")
         pc = str(opts.get("pc_type", "jacobi"))
-        if pc not in ("jacobi", "sor", "none", "bjacobi"):
-            raise ValueError(f"-pc_type {pc}: supported preconditioners are jacobi and bjacobi")
+        if pc not in ("jacobi", "sor", "none", "bjacobi", "hypre"):
+            raise ValueError(f"-pc_type {pc}: supported preconditioners are jacobi, bjacobi and hypre (ams)")
+        if pc == "hypre" and str(opts.get("pc_hypre_type", "ams")) != "ams":
+            raise ValueError("-pc_type hypre: supported -pc_hypre_type is ams")
         # bjacobi: one block per edge / face / element; sor (petgem's default,
-        # a sequential sweep) and none run with the entity blocks as well
-        precond = "jacobi" if pc == "jacobi" else "block"
+        # a sequential sweep) and none run with the entity blocks as well;
+        # hypre's AMS (auxiliary-space Maxwell) is served by its one-level
+        # relative, Jacobi plus the discrete-gradient correction
+        precond = {"jacobi": "jacobi", "hypre": "grad"}.get(pc, "block")
+        if precond == "grad" and self.mesh.p > 3:
+            raise ValueError("-pc_type hypre: the gradient correction is built for nord <= 3")
         self.info = []
         self.ksp = ksp
         # all polarisations in one batched solve (one SpMM per iteration)
@@ -159,7 +165,7 @@ class Solver:
                                   restart=int(opts.get("ksp_gmres_restart", 30)),
                                   max_it=int(opts.get("ksp_max_it", 10000)),
                                   precision=str(opts.get("pg_precision", "fp64")), ksp=ksp,
-                                  raise_on_fail=False, precond=precond)
+                                  raise_on_fail=False, precond=precond, pec=getattr(self, "mode", "csem") == "csem")
         for i in range(len(self.b)):
             self.x[i] = X[:, i].contiguous() if X.ndim == 2 else X
             self.info.append(info)

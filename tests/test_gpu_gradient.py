@@ -168,3 +168,37 @@ def test_gradient_correction_rejects_other_forms():
         with pytest.raises(_lib.PetgemError) as e:
             solve_csr(m.rowptr, m.col, vals, b, ksp=ksp, precision="mixed", gradient=g)
         assert e.value.status == -1
+
+
+def test_mt_solve_with_gradient_matches_oracle():
+    """The MT system of a reduced air-layer mesh (the MT model on 6^3 cubes,
+    p = 3, 26,298 DOFs, air at 1e-8 S/m, no PEC).  Its solution carries
+    air-gradient components of ~1e10 (the air's near-null space), so FP64
+    cannot evaluate b - A x below ~eps |A| |x| ~ 1e-7 |b|: the oracle's sparse
+    LU (backward error 1e-16) leaves a true relative residual of 1.3e-7.
+    Batched COCG with Jacobi plus the gradient correction (every column
+    kept) must reach a true residual below the LU's own for both
+    polarisations, and its receiver E and H agree with the LU solution to the
+    accuracy that conditioning allows (4.2e-5 measured on the CPU with the
+    same preconditioner; checked at 2e-4)."""
+    import scipy.sparse.linalg as spla
+    from oracle import fem, system
+    mdl = synthetic.config4(6)
+    f = 1.0
+    m = _mesh(mdl.nodes, mdl.tets, 3)
+    vals = m.assemble(mdl.sigma, f)
+    B = m.mt_rhs(mdl.sigma, f, ("x", "y"))
+    X, info = m.solve(vals, B, ksp="cocg", precond="grad", pec=False, rtol=1e-7, max_it=20000)
+    assert info.status == 0 and max(info.relres_per_rhs) <= 1e-7
+    mm = system.mesh_maps(mdl.nodes, mdl.tets, 3)
+    M, K = system.element_matrices(mdl.nodes[mdl.tets], mm["eo"], mm["fo"], mdl.sigma, 3, processes=1)
+    A = fem.assemble(M, K, mm["dofs"], mm["N"], f).tocsc()
+    lu = spla.splu(A)
+    for k in range(2):
+        bk = B[:, k].cpu().numpy()
+        x = lu.solve(bk)
+        lu_res = np.linalg.norm(bk - A @ x) / np.linalg.norm(bk)
+        assert info.relres_per_rhs[k] <= lu_res
+        Fo, _ = system.receiver_fields(mm, x, mdl.nodes, mdl.tets, 3, mdl.receivers, f)
+        Fd, _ = m.receiver_fields(X[:, k].contiguous(), mdl.receivers, f)
+        assert rel_norm(Fd.cpu().numpy(), Fo) <= 2e-4
