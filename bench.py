@@ -594,6 +594,8 @@ def run_solves(args, torch, mesh, model, vals, b):
     xg, rgr = timed("cocg", "fp64", b, args.max_it, precond="grad")
     Xgb, rgb = timed("cocg", "fp64", B.contiguous(), args.max_it, precond="grad")
     xgm, rgm = timed("gmres", "fp64", b, args.max_it, precond="grad")
+    xgd, rgd = timed("cocg", "df64", b, args.max_it, precond="grad")
+    Xgdb, rgdb = timed("cocg", "df64", B.contiguous(), args.max_it, precond="grad")
     xdf, rdf = timed("cocg", "df64", b, args.max_it)
     Xdb, rdb = timed("cocg", "df64", B.contiguous(), args.max_it)
     # complex64 inner solves + FP64 iterative refinement (one RHS, then the
@@ -643,7 +645,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     j1 = fcol.index(f0)      # the workspace source at the workload frequency
     for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf),
                  (xir, rir), (None if Xib is None else Xib[:, 0].contiguous(), rib), (xg, rgr),
-                 (Xgb[:, 0].contiguous(), rgb), (xgm, rgm)):
+                 (Xgb[:, 0].contiguous(), rgb), (xgm, rgm), (xgd, rgd), (Xgdb[:, 0].contiguous(), rgdb)):
         if x is None:
             continue
         F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
@@ -653,6 +655,9 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["fp64_grad"] = rgr
     out["fp64_grad_batched"] = rgb
     out["gmres30_fp64_grad"] = rgm
+    out["df64_grad"] = rgd
+    out["df64_grad_batched"] = rgdb
+    out["speedup_df64_grad_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rgdb["ms_per_rhs"], 1e-9), 2)
     out["speedup_fp64_grad_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rgr["ms_per_rhs"], 1e-9), 2)
     out["speedup_fp64_grad_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rgb["ms_per_rhs"], 1e-9), 2)
     out["df64"] = rdf

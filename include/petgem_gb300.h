@@ -513,8 +513,8 @@ typedef struct pg_cocg_opts {
    * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 8x the
    * inner iterations of the first refinement step (at least 1,000) */
   double inner_rtol;
-  /* gradient correction (pg_cocg and pg_gmres; precision 0 with diagonal
-   * Jacobi, block_p 0; grad_rowptr NULL = off): G, n rows by grad_cols columns, and
+  /* gradient correction (pg_cocg: precision 0 or 2; pg_gmres: precision 0;
+   * diagonal Jacobi, block_p 0; grad_rowptr NULL = off): G, n rows by grad_cols columns, and
    * its transpose from pg_gradient_map.  The preconditioner becomes
    *   B = D^-1 + G diag(G^T A G)^-1 G^T
    * (D = diag A; diag(G^T A G) is formed from A when the solve starts), which

@@ -311,7 +311,7 @@ __global__ void k_cg_xupdate(const double2* __restrict__ y, const double2* __res
     x[e] = dadd(x[e], cmul(S[e / K], y[e]));
 }
 
-size_t cg_layout(const Plan& P, size_t* off /* 24 */) {
+size_t cg_layout(const Plan& P, size_t* off /* 28 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   put(0, P.nnz * P.csize);                      // At (matrix precision)
@@ -378,7 +378,7 @@ void launch_cg_spmv(const Plan& P, const int64_t* rowptr, const int32_t* col, co
 template <typename CM>
 int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
              const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s) {
-  size_t off[24];
+  size_t off[28];
   cg_layout(P, off);
   const bool bj = P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
@@ -654,7 +654,7 @@ extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   Plan P = cg_plan(n, nnz, nrhs, opts);
-  size_t off[24];
+  size_t off[28];
   if (opts->precision == 3) return ir_layout(P, off) + 256;
   return (opts->precision == 2 ? df_layout(P, off) : cg_layout(P, off)) + 256;
 }
@@ -669,9 +669,10 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
   }
   if (opts->grad_rowptr) {
     if (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row || !opts->gradt_val ||
-        opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0 || opts->precision != 0) {
-      pg_set_error("pg_cocg: gradient correction needs all six G arrays, grad_cols >= 1, precision 0 and diagonal "
-                   "Jacobi (block_p 0)");
+        opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0 ||
+        (opts->precision != 0 && opts->precision != 2)) {
+      pg_set_error("pg_cocg: gradient correction needs all six G arrays, grad_cols >= 1, precision 0 or 2 and "
+                   "diagonal Jacobi (block_p 0)");
       return PG_ERR_ARG;
     }
   }

@@ -393,11 +393,14 @@ __device__ void cg_alpha_final(const double2* partial, int nblocks, CgState* st,
 // spike: a cycle also ends when a column's residual estimate exceeds spike
 // times its starting value (COCG's residual norm is not monotone; a
 // recurrence carried far past such a spike has lost accuracy)
-template <int K>
+// GRAD (gradient correction): rho and beta are left to the prolongation,
+// which forms z first.
+template <int K, bool GRAD = false>
 __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblocks, CgState* st, CgCtl* ctl, int iter,
                               double delta, double2* smem, double spike = 1e3) {
   const int my = threadIdx.x < K ? threadIdx.x : 0;
-  const double2 rho = sum_partials<K>(prho, nblocks, my, smem);
+  double2 rho = make_double2(0.0, 0.0);
+  if constexpr (!GRAD) rho = sum_partials<K>(prho, nblocks, my, smem);
   const double2 w = sum_partials<K>(pw, nblocks, my, smem);
   __shared__ int any, stop;
   if (threadIdx.x == 0) { any = 0; stop = 0; }
@@ -409,14 +412,16 @@ __device__ void cg_beta_final(const double2* prho, const double2* pw, int nblock
       S.its += 1;
       S.res = sqrt(w.x);
       if (!isfinite(S.res)) ctl->nonfinite = 1;
-      if (S.rho.x == 0.0 && S.rho.y == 0.0) {
-        S.breakdown = 1;
-        S.active = 0;
-        S.beta = make_double2(0.0, 0.0);
-      } else {
-        S.beta = ddiv(rho, S.rho);
+      if constexpr (!GRAD) {
+        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.beta = make_double2(0.0, 0.0);
+        } else {
+          S.beta = ddiv(rho, S.rho);
+        }
+        S.rho = rho;
       }
-      S.rho = rho;
       if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
       else if (S.res <= delta * S.res0 || S.res > spike * S.res0) atomicOr(&stop, 1);
     } else {
@@ -536,7 +541,7 @@ int pick_fastest(const std::vector<int>& cands, F&& launch, cudaStream_t s) {
 namespace pgk {
 
 // workspace layout of the double-float COCG (mf: several frequencies)
-size_t df_layout(const Plan& P, size_t* off /* 24 */, bool mf = false);
+size_t df_layout(const Plan& P, size_t* off /* 28 */, bool mf = false);
 // double-float COCG; col_scale (host [k]) selects the several-frequencies form
 int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b, double2* x,
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,

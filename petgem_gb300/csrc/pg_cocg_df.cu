@@ -91,13 +91,15 @@ __global__ void __launch_bounds__(kThreads) k_df_spmm(const int64_t* __restrict_
   if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
 }
 
-// y += alpha p ; r -= alpha q ; partials rho = r^T r (df), w = sum |r|^2 |D| (FP32 estimate)
-template <int K, bool PC = false>
+// y += alpha p ; r -= alpha q ; partials rho = r^T r (df), w = sum |r|^2 |D| (FP32 estimate).
+// GRAD: no rho (the gradient prolongation forms z and rho = r^T z).
+template <int K, bool PC = false, bool GRAD = false>
 __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, float4* __restrict__ r,
                                                         const float4* __restrict__ pv, const float4* __restrict__ q,
                                                         const float* __restrict__ wd, int64_t n, CgState* st,
                                                         double2* prho, double2* pw, CgCtl* ctl, int iter,
-                                                        double delta) {
+                                                        double delta, float2* __restrict__ u = nullptr,
+                                                        const float2* __restrict__ Sinv = nullptr) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ float4 al[kMaxK];
@@ -122,13 +124,120 @@ __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, 
     re = df_norm(re);
     y[e] = ye;
     r[e] = re;
-    cdf_mac(rho, re, re);
+    if constexpr (GRAD) {
+      u[e] = cmul(Sinv[e / K], make_float2(re.x, re.z));
+    } else {
+      cdf_mac(rho, re, re);
+    }
     ww += (re.x * re.x + re.z * re.z) * wd[PC ? e : e / K];
   }
   __shared__ float4 smf[(kThreads / 32) * kMaxK];
-  block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  if constexpr (!GRAD) block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   block_reduce_f<K>(ww, reinterpret_cast<float*>(smf), pw + (int64_t)blockIdx.x * K);
-  if (arrive_last(&ctl->counter)) cg_beta_final<K>(prho, pw, gridDim.x, st, ctl, iter, delta, smem);
+  if (arrive_last(&ctl->counter)) cg_beta_final<K, GRAD>(prho, pw, gridDim.x, st, ctl, iter, delta, smem);
+}
+
+// Gradient correction on the double-float recurrence (diagonal scaling, PEC
+// systems): z = r + S^-1 G invD G^T S^-1 r.  The residual recurrence and rho
+// stay double-float; the correction only shapes the search direction, so its
+// products run in FP32 (the update writes u = S^-1 r from r's leading
+// float, the restriction t = invD G^T u and the prolongation S^-1 G t are
+// FP32, and z = r + S^-1 G t is a double-float sum).  Inside an iteration
+// both run only when this iteration's update ran (ctl->pending, cleared by
+// the next product); start = 1 at a cycle start.
+template <int K>
+__global__ void k_dfg_u_start(const double2* __restrict__ r64, int64_t n, float2* __restrict__ u) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    u[e] = make_float2((float)r64[e].x, (float)r64[e].y);
+}
+
+__global__ void k_dfg_to_f32(const double2* __restrict__ a, int64_t n, float2* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_dfg_restrict(const int64_t* __restrict__ gtp,
+                                                           const int32_t* __restrict__ gtr,
+                                                           const double* __restrict__ gtv,
+                                                           const float2* __restrict__ invD,
+                                                           const float2* __restrict__ u, int64_t gn,
+                                                           float2* __restrict__ t, const CgCtl* ctl, int start) {
+  if (!start && !ctl->pending) return;
+  const int64_t total = gn * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / K;
+    const int rhs = (int)(e % K);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
+      const float g = __double2float_rn(gtv[j]);
+      const float2 v = u[(int64_t)gtr[j] * K + rhs];
+      acc.x = fmaf(g, v.x, acc.x);
+      acc.y = fmaf(g, v.y, acc.y);
+    }
+    t[e] = cmul(invD[c], acc);
+  }
+}
+
+// z = r + S^-1 (G t), partial rho = r^T z (double-float); in an iteration the
+// last block sets beta = rho / rho_old and rho for the RHS updated in it
+// (beta_iter == 1); at a cycle start p = z when set_p.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restrict__ gp,
+                                                          const int32_t* __restrict__ gc,
+                                                          const double* __restrict__ gv,
+                                                          const float2* __restrict__ Sinv,
+                                                          const float2* __restrict__ t,
+                                                          const float4* __restrict__ r, int64_t n,
+                                                          float4* __restrict__ z, float4* __restrict__ pv, int set_p,
+                                                          double2* prho, CgState* st, CgCtl* ctl, int start) {
+  if (!start && !ctl->pending) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const int64_t row = e / K;
+    const int rhs = (int)(e % K);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
+      const float g = __double2float_rn(gv[j]);
+      const float2 v = t[(int64_t)gc[j] * K + rhs];
+      acc.x = fmaf(g, v.x, acc.x);
+      acc.y = fmaf(g, v.y, acc.y);
+    }
+    const float2 cr = cmul(Sinv[row], acc);
+    const float4 re = r[e];
+    float4 ze = re;
+    df_add(ze.x, ze.y, cr.x, 0.f);
+    df_add(ze.z, ze.w, cr.y, 0.f);
+    ze = df_norm(ze);
+    z[e] = ze;
+    if (set_p) pv[e] = ze;
+    cdf_mac(rho, re, ze);
+  }
+  block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  if (!start && arrive_last(&ctl->counter)) {
+    const double2 rr = sum_partials<K>(prho, gridDim.x, threadIdx.x < K ? threadIdx.x : 0, smem);
+    if (threadIdx.x < K) {
+      CgState& S = st[threadIdx.x];
+      if (S.beta_iter == 1) {
+        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.beta = make_double2(0.0, 0.0);
+        } else {
+          S.beta = ddiv(rr, S.rho);
+        }
+        S.rho = rr;
+      } else {
+        S.beta = make_double2(0.0, 0.0);
+      }
+    }
+    if (threadIdx.x == 0) ctl->counter = 0;
+  }
 }
 
 template <int K, bool PC = false>
@@ -660,7 +769,7 @@ void launch_df_spmm(int variant, int grid, cudaStream_t s, const int64_t* rowptr
 
 namespace pgk {
 
-size_t df_layout(const Plan& P, size_t* off /* 24 */, bool mf) {
+size_t df_layout(const Plan& P, size_t* off /* 28 */, bool mf) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   const size_t ns = mf ? (size_t)P.n * P.k : (size_t)P.n;   // scaling entries: per column with several frequencies
@@ -684,6 +793,13 @@ size_t df_layout(const Plan& P, size_t* off /* 24 */, bool mf) {
   put(17, sizeof(float) * 2 * P.k);               // the same as (hi, lo)
   put(18, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);     // block-Jacobi factors
   put(19, P.bj.p ? sizeof(double2) * P.n * P.k : 0);         // S r64
+  // gradient correction (FP32 products): S^-1, diag(G^T A G)^-1, t = invD G^T u,
+  // z, u = S^-1 r; z also holds diag(G^T A G)^-1 in FP64 while it is formed
+  put(20, P.gn ? sizeof(float2) * P.n : 0);
+  put(21, P.gn ? sizeof(float2) * P.gn : 0);
+  put(22, P.gn ? sizeof(float2) * P.gn * P.k : 0);
+  put(23, P.gn ? std::max(sizeof(float4) * P.n * P.k, sizeof(double2) * (size_t)P.gn) : 0);
+  put(24, P.gn ? sizeof(float2) * P.n * P.k : 0);
   return o;
 }
 
@@ -691,7 +807,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                 const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws, cudaStream_t s,
                 const double* col_scale) {
   const bool mf = col_scale != nullptr;
-  size_t off[24];
+  size_t off[28];
   df_layout(P, off, mf);
   float4* ps = reinterpret_cast<float4*>(ws + off[14]);
   float4* Sdf = reinterpret_cast<float4*>(ws + off[15]);
@@ -700,6 +816,13 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   const bool bj = !mf && P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
   double2* r64b = reinterpret_cast<double2*>(ws + off[19]);
+  const bool grad = !mf && P.gn > 0;   // diagonal scaling only (checked by pg_cocg)
+  float2* Sinv = reinterpret_cast<float2*>(ws + off[20]);
+  float2* invD = reinterpret_cast<float2*>(ws + off[21]);
+  float2* gt = reinterpret_cast<float2*>(ws + off[22]);
+  float4* gz = reinterpret_cast<float4*>(ws + off[23]);
+  float2* gu = reinterpret_cast<float2*>(ws + off[24]);
+  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);
@@ -767,6 +890,14 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   } else {
     k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
     k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At, wdf, wd);
+    if (grad) {
+      double2* tmp = reinterpret_cast<double2*>(gz);   // FP64 scratch until the first z
+      k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n, reinterpret_cast<double2*>(gz));
+      k_dfg_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(reinterpret_cast<double2*>(gz), P.n, Sinv);
+      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                       P.gn, tmp);
+      k_dfg_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, invD);
+    }
   }
   PG_LAUNCH_CHECK();
   std::vector<double> bnorm(k), rn(k), tgt(k), sc(k), sc_prev(k, 1.0), scal(4 * (size_t)k);
@@ -817,6 +948,16 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       launch_single(variant, ss);
     else
       PG_KSWITCH(k, (launch_df_spmm<K>(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+    if (grad) {
+      PG_KSWITCH(k, (k_df_update<K, false, true><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2,
+                                                                           ctl, 0, delta, gu, Sinv),
+                     k_dfg_restrict<K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                     invD, gu, P.gn, gt, ctl, 0),
+                     k_dfg_prolong<K><<<nbu, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv, gt,
+                                                                r, P.n, gz, pv, 0, part, st, ctl, 0),
+                     k_df_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, gz, P.n, st, ctl)));
+      return;
+    }
     PG_KSWITCH(k, (k_df_update<K><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, 0, delta),
                    k_df_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, r, P.n, st, ctl)));
   };
@@ -914,7 +1055,18 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       PG_KSWITCH(k, (k_df_start<K, true><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part, ps)));
     } else {
       if (bj) PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, r64b)));
-      PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, first ? 1 : 0, part)));
+      if (grad) {
+        // r = S r64, then z = r + S^-1 G invD G^T S^-1 r and rho = r^T z (p = z on the first cycle)
+        PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, 0, part),
+                       k_dfg_u_start<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, P.n, gu),
+                       k_dfg_restrict<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                      invD, gu, P.gn, gt, ctl, 1),
+                       k_dfg_prolong<K><<<nb, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv, gt,
+                                                                r, P.n, gz, pv, first ? 1 : 0, part, st, ctl, 1)));
+      } else {
+        PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(bj ? r64b : r64, S, P.n, r, y, pv, first ? 1 : 0,
+                                                             part)));
+      }
     }
     PG_KSWITCH(k, (k_cg_cycle_init<K><<<1, 32 * K, 0, s>>>(part, nb, st, rnorm, target, want, ctl, first ? 1 : 0)));
     if (first && !mf) {
@@ -1022,7 +1174,7 @@ extern "C" size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int 
   pg_cocg_default_opts(&o);
   o.precision = 2;
   Plan P = cg_plan(n, nnz, nrhs, &o);
-  size_t off[24];
+  size_t off[28];
   return df_layout(P, off, true) + 256;
 }
 

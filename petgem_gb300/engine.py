@@ -381,8 +381,9 @@ class DeviceMesh:
         precond="block": entity block-Jacobi (each edge / face / volume's
         diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal;
         "grad": diagonal Jacobi plus the gradient correction
-        D^-1 + G diag(G^T A G)^-1 G^T (COCG and GMRES in fp64, p <= 3;
-        gradient_map; pec=False for systems without PEC rows, e.g. MT)."""
+        D^-1 + G diag(G^T A G)^-1 G^T (COCG in fp64 or df64, GMRES in fp64;
+        p <= 3; gradient_map; pec=False for systems without PEC rows, e.g.
+        MT, which want fp64: their true residual has an FP64 floor)."""
         if precond not in ("block", "jacobi", "grad"):
             raise ValueError(f"unknown preconditioner {precond!r} (block, jacobi, grad)")
         blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" else None
@@ -624,8 +625,8 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     block, right preconditioning: PETSc -pc_type bjacobi with one block per
     edge / face / element).
     gradient: a GradientMap (DeviceMesh.gradient_map) for the gradient
-    correction: the preconditioner D^-1 + G diag(G^T A G)^-1 G^T (fp64,
-    diagonal Jacobi; GMRES applies it on the right).
+    correction: the preconditioner D^-1 + G diag(G^T A G)^-1 G^T (diagonal
+    Jacobi; COCG in fp64 or df64, GMRES in fp64 on the right).
     """
     _check_csr(f"solve_csr({ksp})", rowptr, col, vals, b)
     if gradient is not None:

@@ -100,8 +100,9 @@ def test_gradient_map_is_curl_free_at_size(p, n):
     assert abs(A1 @ G).max() >= 1e-6 * abs(A1).max()   # the mass part is there
 
 
+@pytest.mark.parametrize("prec", ["fp64", "df64"])
 @pytest.mark.parametrize("p", [2, 3])
-def test_cocg_gradient_correction_matches_jacobi(p, monkeypatch):
+def test_cocg_gradient_correction_matches_jacobi(p, prec, monkeypatch):
     mdl = synthetic.csem_two_layer(6, p)
     m = _mesh(mdl.nodes, mdl.tets, p)
     vals = m.assemble(mdl.sigma, 1.0, pec=True)
@@ -112,7 +113,7 @@ def test_cocg_gradient_correction_matches_jacobi(p, monkeypatch):
         bs.append(b)
     for rhs in (bs[1], torch.stack(bs, 1).contiguous()):
         xj, ij = m.solve(vals, rhs, ksp="cocg", precond="jacobi", rtol=1e-10, max_it=100000)
-        xg, ig = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000)
+        xg, ig = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000, precision=prec)
         assert ig.status == 0 and max(ig.relres_per_rhs) <= 1e-10
         assert ig.iterations * 3 < ij.iterations, (ig.iterations, ij.iterations)
         assert rel_norm(xg.cpu().numpy(), xj.cpu().numpy()) <= 1e-7
@@ -120,8 +121,8 @@ def test_cocg_gradient_correction_matches_jacobi(p, monkeypatch):
         # autotuner picks the lanes per row by timing, and each variant sums
         # in its own order)
         monkeypatch.setenv("PG_AUTOTUNE", "0")
-        xa, ia = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000)
-        xb, ib = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000)
+        xa, ia = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000, precision=prec)
+        xb, ib = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000, precision=prec)
         monkeypatch.delenv("PG_AUTOTUNE")
         assert ia.iterations == ib.iterations and torch.equal(xa, xb)
 
@@ -164,9 +165,9 @@ def test_gradient_correction_rejects_other_forms():
     g = m.gradient_map()
     with pytest.raises(ValueError):
         solve_csr(m.rowptr, m.col, vals, b, ksp="cocg", blocks=(2, m.nE, m.nF, m.T), gradient=g)
-    for ksp in ("cocg", "gmres"):
+    for ksp, prec in (("cocg", "mixed"), ("cocg", "ir32"), ("gmres", "mixed")):
         with pytest.raises(_lib.PetgemError) as e:
-            solve_csr(m.rowptr, m.col, vals, b, ksp=ksp, precision="mixed", gradient=g)
+            solve_csr(m.rowptr, m.col, vals, b, ksp=ksp, precision=prec, gradient=g)
         assert e.value.status == -1
 
 
