@@ -73,6 +73,8 @@ def parse():
                     help="assemble from the item list instead of the per-mesh assembly records")
     ap.add_argument("--solve-iters", type=int, default=0,
                     help="profiling mode: run each solver form for exactly this many iterations")
+    ap.add_argument("--profile-only", default="",
+                    help="profiling mode: comma-separated solver forms to run (default: all)")
     return ap.parse_args()
 
 
@@ -601,14 +603,16 @@ def run_solves(args, torch, mesh, model, vals, b):
     # complex64 inner solves + FP64 iterative refinement (one RHS, then the
     # 16-RHS batch); a stall would be recorded, not raised
     from petgem_gb300 import _lib
-    def timed_ir(rhs):
+    def timed_ir(rhs, precond="block"):
         try:
-            return timed("cocg", "ir32", rhs, args.max_it)
+            return timed("cocg", "ir32", rhs, args.max_it, precond=precond)
         except _lib.PetgemError as exc:
             return None, {"ksp": "cocg", "precision": "ir32", "converged": False, "status": exc.status,
                           "error": str(exc)}
     xir, rir = timed_ir(b)
     Xib, rib = timed_ir(B.contiguous())
+    xgi, rgi = timed_ir(b, precond="grad")
+    Xgib, rgib = timed_ir(B.contiguous(), precond="grad")
     # several frequencies in one solve: 4 frequencies x 8 sources (32 columns)
     freqs = [0.25, 0.5, 1.0, 2.0]
     f0 = model.source["frequency"]
@@ -633,6 +637,16 @@ def run_solves(args, torch, mesh, model, vals, b):
            "seconds": round(dtf, 3), "ms_per_rhs": round(dtf * 1e3 / len(fcol), 2), "iterations": inf.iterations,
            "ms_per_iteration": round(dtf * 1e3 / max(inf.iterations, 1), 4), "relres": inf.relres,
            "converged": inf.status == 0}
+    torch.cuda.synchronize()
+    t = time.time()
+    Xfg, infg = mesh.solve_frequencies(vals, f0, Bf, fcol, precond="grad", rtol=1e-8, max_it=args.max_it,
+                                       raise_on_fail=False)
+    torch.cuda.synchronize()
+    dtg = time.time() - t
+    rmfg = {"ksp": "cocg", "precision": "df64", "precond": "grad", "nrhs": len(fcol), "frequencies_hz": freqs,
+            "sources": 8, "seconds": round(dtg, 3), "ms_per_rhs": round(dtg * 1e3 / len(fcol), 2),
+            "iterations": infg.iterations, "ms_per_iteration": round(dtg * 1e3 / max(infg.iterations, 1), 4),
+            "relres": infg.relres, "converged": infg.status == 0}
     # the FP32-operator form stalls above 1e-8 at this conditioning: capped, per-iteration cost reported
     xmx, rmx = timed("cocg", "mixed", b, 3000)
     _, rg = timed("gmres", "mixed", b, 300)
@@ -645,7 +659,9 @@ def run_solves(args, torch, mesh, model, vals, b):
     j1 = fcol.index(f0)      # the workspace source at the workload frequency
     for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf),
                  (xir, rir), (None if Xib is None else Xib[:, 0].contiguous(), rib), (xg, rgr),
-                 (Xgb[:, 0].contiguous(), rgb), (xgm, rgm), (xgd, rgd), (Xgdb[:, 0].contiguous(), rgdb)):
+                 (Xgb[:, 0].contiguous(), rgb), (xgm, rgm), (xgd, rgd), (Xgdb[:, 0].contiguous(), rgdb),
+                 (Xfg[:, j1].contiguous(), rmfg), (xgi, rgi),
+                 (None if Xgib is None else Xgib[:, 0].contiguous(), rgib)):
         if x is None:
             continue
         F, _ = mesh.receiver_fields(x, model.receivers, model.source["frequency"])
@@ -656,6 +672,8 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["fp64_grad_batched"] = rgb
     out["gmres30_fp64_grad"] = rgm
     out["df64_grad"] = rgd
+    out["ir32_grad"] = rgi
+    out["ir32_grad_batched"] = rgib
     out["df64_grad_batched"] = rgdb
     out["speedup_df64_grad_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rgdb["ms_per_rhs"], 1e-9), 2)
     out["speedup_fp64_grad_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rgr["ms_per_rhs"], 1e-9), 2)
@@ -664,6 +682,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["df64_batched"] = rdb
     out["mixed"] = rmx
     out["df64_multifrequency"] = rmf
+    out["df64_multifrequency_grad"] = rmfg
     out["ir32"] = rir
     out["ir32_batched"] = rib
     if rib.get("converged"):
@@ -686,15 +705,19 @@ def profile_solves(args, torch, mesh, vals, b):
     """Fixed iteration counts of every solver form (for kernel launch lists)."""
     out = {}
     B = torch.stack([b] * args.nrhs, 1).contiguous()
-    for name, ksp, prec, rhs in (("cocg_fp64", "cocg", "fp64", b), ("cocg_df64", "cocg", "df64", b),
-                                 ("cocg_df64_batched", "cocg", "df64", B), ("cocg_mixed", "cocg", "mixed", b),
-                                 ("cocg_ir32", "cocg", "ir32", b),
-                                 ("cocg_mixed_batched", "cocg", "mixed", B), ("gmres_mixed", "gmres", "mixed", b),
-                                 ("gmres_fp64", "gmres", "fp64", b)):
+    for name, ksp, prec, rhs, pc in (("cocg_fp64", "cocg", "fp64", b, "block"), ("cocg_df64", "cocg", "df64", b, "block"),
+                                     ("cocg_df64_batched", "cocg", "df64", B, "block"),
+                                     ("cocg_mixed", "cocg", "mixed", b, "block"), ("cocg_ir32", "cocg", "ir32", b, "block"),
+                                     ("cocg_mixed_batched", "cocg", "mixed", B, "block"),
+                                     ("gmres_mixed", "gmres", "mixed", b, "block"), ("gmres_fp64", "gmres", "fp64", b, "block"),
+                                     ("cocg_fp64_grad", "cocg", "fp64", b, "grad"),
+                                     ("cocg_df64_grad_batched", "cocg", "df64", B, "grad")):
+        if args.profile_only and name not in args.profile_only.split(","):
+            continue
         torch.cuda.synchronize()
         t = time.time()
         _, info = mesh.solve(vals, rhs, rtol=1e-30, precision=prec, max_it=args.solve_iters, raise_on_fail=False,
-                             ksp=ksp, check_every=args.solve_iters)
+                             ksp=ksp, check_every=args.solve_iters, precond=pc)
         torch.cuda.synchronize()
         dt = time.time() - t
         out[name] = {"iterations": info.iterations, "ms_per_iteration": round(dt * 1e3 / max(info.iterations, 1), 4)}

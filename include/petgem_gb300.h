@@ -513,7 +513,7 @@ typedef struct pg_cocg_opts {
    * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 8x the
    * inner iterations of the first refinement step (at least 1,000) */
   double inner_rtol;
-  /* gradient correction (pg_cocg: precision 0 or 2; pg_gmres: precision 0;
+  /* gradient correction (pg_cocg: precision 0, 2 or 3; pg_gmres: precision 0;
    * diagonal Jacobi, block_p 0; grad_rowptr NULL = off): G, n rows by grad_cols columns, and
    * its transpose from pg_gradient_map.  The preconditioner becomes
    *   B = D^-1 + G diag(G^T A G)^-1 G^T
@@ -568,8 +568,10 @@ int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* vals, int64
  * M is assembled (PEC applied) at one frequency omega_0 and s_j = omega_j /
  * omega_0 > 0 (col_scale: host array [nrhs]).  The matrix is read once per
  * iteration for all columns; each column has its own Jacobi scaling.  b, x
- * complex128 [n * nrhs] (RHS fastest).  Other arguments as pg_cocg. */
-size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs);
+ * complex128 [n * nrhs] (RHS fastest).  The gradient correction of
+ * pg_cocg_opts applies (diag(G^T A_j G) = s_j diag(G^T A0 G), since
+ * G^T K G = 0); block_p is ignored.  Other arguments as pg_cocg. */
+size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts /* may be NULL */);
 int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
                       const double* b, double* x, int nrhs, const double* col_scale, const pg_cocg_opts* opts,
                       pg_gmres_result* result, double* relres_per_rhs, void* workspace, size_t workspace_bytes,

@@ -121,7 +121,7 @@ SIGNATURES = {
     "pg_cocg_default_opts": (None, [_PC]),
     "pg_cocg_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PC]),
     "pg_cocg": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PC, _PR, _P, _P, _SZ, _P]),
-    "pg_cocg_multifreq_workspace_bytes": (_SZ, [_I64, _I64, _INT]),
+    "pg_cocg_multifreq_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PC]),
     "pg_cocg_multifreq": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _P, _PC, _PR, _P, _P, _SZ, _P]),
     "pg_cocg_segments_workspace_bytes": (_SZ, [_I64, _I64, _INT, _P, _INT, _P, _PC]),
     "pg_cocg_segments": (_INT, [_P, _P, _P, _I64, _I64, _P, _INT, _P, _P, _P, _INT, _PC, _PR, _P, _P, _P, _SZ, _P]),

@@ -670,8 +670,8 @@ extern "C" int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* 
   if (opts->grad_rowptr) {
     if (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row || !opts->gradt_val ||
         opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0 ||
-        (opts->precision != 0 && opts->precision != 2)) {
-      pg_set_error("pg_cocg: gradient correction needs all six G arrays, grad_cols >= 1, precision 0 or 2 and "
+        opts->precision == 1) {
+      pg_set_error("pg_cocg: gradient correction needs all six G arrays, grad_cols >= 1, precision 0, 2 or 3 and "
                    "diagonal Jacobi (block_p 0)");
       return PG_ERR_ARG;
     }

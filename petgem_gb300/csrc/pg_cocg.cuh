@@ -170,6 +170,44 @@ __global__ void k_cg_cycle_keep(CgState* st, const double* target, const int* wa
   }
 }
 
+// FP32 restriction of the gradient correction, shared by the double-float and
+// complex64 solvers: t = invD .* (G^T u), u = S^-1 r in FP32 (the correction
+// only shapes the search direction).  Inside an iteration it runs only when
+// this iteration's update ran (ctl->pending, cleared by the next product);
+// start = 1 at a cycle start.
+__global__ void k_to_f32(const double2* __restrict__ a, int64_t n, float2* __restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+
+// PC (several frequencies): column j's diag(G^T A_j G) is s_j diag(G^T A_0 G)
+// (G^T K G = 0), so t carries the column's 1 / s_j (cinv).
+template <int K, bool PC = false>
+__global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __restrict__ gtp,
+                                                           const int32_t* __restrict__ gtr,
+                                                           const double* __restrict__ gtv,
+                                                           const float2* __restrict__ invD,
+                                                           const float2* __restrict__ u, int64_t gn,
+                                                           float2* __restrict__ t, const CgCtl* ctl, int start,
+                                                           const float* __restrict__ cinv = nullptr) {
+  if (!start && !ctl->pending) return;
+  const int64_t total = gn * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / K;
+    const int rhs = (int)(e % K);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
+      const float g = __double2float_rn(gtv[j]);
+      const float2 v = u[(int64_t)gtr[j] * K + rhs];
+      acc.x = fmaf(g, v.x, acc.x);
+      acc.y = fmaf(g, v.y, acc.y);
+    }
+    float2 w = cmul(invD[c], acc);
+    if (PC) w = make_float2(w.x * cinv[rhs], w.y * cinv[rhs]);
+    t[e] = w;
+  }
+}
+
 // true when some RHS ran this iteration's update (iter < 0: always)
 template <int K>
 __device__ __forceinline__ bool grad_due(const CgState* st, int iter) {

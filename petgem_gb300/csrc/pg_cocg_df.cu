@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kThreads) k_df_update(float4* __restrict__ y, 
     y[e] = ye;
     r[e] = re;
     if constexpr (GRAD) {
-      u[e] = cmul(Sinv[e / K], make_float2(re.x, re.z));
+      u[e] = cmul(Sinv[PC ? e : e / K], make_float2(re.x, re.z));
     } else {
       cdf_mac(rho, re, re);
     }
@@ -151,38 +151,11 @@ __global__ void k_dfg_u_start(const double2* __restrict__ r64, int64_t n, float2
     u[e] = make_float2((float)r64[e].x, (float)r64[e].y);
 }
 
-__global__ void k_dfg_to_f32(const double2* __restrict__ a, int64_t n, float2* __restrict__ out) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    out[e] = make_float2((float)a[e].x, (float)a[e].y);
-}
-
-template <int K>
-__global__ void __launch_bounds__(kThreads) k_dfg_restrict(const int64_t* __restrict__ gtp,
-                                                           const int32_t* __restrict__ gtr,
-                                                           const double* __restrict__ gtv,
-                                                           const float2* __restrict__ invD,
-                                                           const float2* __restrict__ u, int64_t gn,
-                                                           float2* __restrict__ t, const CgCtl* ctl, int start) {
-  if (!start && !ctl->pending) return;
-  const int64_t total = gn * K;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = e / K;
-    const int rhs = (int)(e % K);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
-      const float g = __double2float_rn(gtv[j]);
-      const float2 v = u[(int64_t)gtr[j] * K + rhs];
-      acc.x = fmaf(g, v.x, acc.x);
-      acc.y = fmaf(g, v.y, acc.y);
-    }
-    t[e] = cmul(invD[c], acc);
-  }
-}
-
 // z = r + S^-1 (G t), partial rho = r^T z (double-float); in an iteration the
 // last block sets beta = rho / rho_old and rho for the RHS updated in it
-// (beta_iter == 1); at a cycle start p = z when set_p.
-template <int K>
+// (beta_iter == 1); at a cycle start p = z when set_p.  PC (several
+// frequencies): S^-1 per element, and ps = S o p is set with p.
+template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restrict__ gp,
                                                           const int32_t* __restrict__ gc,
                                                           const double* __restrict__ gv,
@@ -190,7 +163,9 @@ __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restr
                                                           const float2* __restrict__ t,
                                                           const float4* __restrict__ r, int64_t n,
                                                           float4* __restrict__ z, float4* __restrict__ pv, int set_p,
-                                                          double2* prho, CgState* st, CgCtl* ctl, int start) {
+                                                          double2* prho, CgState* st, CgCtl* ctl, int start,
+                                                          float4* __restrict__ ps = nullptr,
+                                                          const float4* __restrict__ Sdf = nullptr) {
   if (!start && !ctl->pending) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ float4 smf[(kThreads / 32) * kMaxK];
@@ -208,14 +183,21 @@ __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restr
       acc.x = fmaf(g, v.x, acc.x);
       acc.y = fmaf(g, v.y, acc.y);
     }
-    const float2 cr = cmul(Sinv[row], acc);
+    const float2 cr = cmul(Sinv[PC ? e : row], acc);
     const float4 re = r[e];
     float4 ze = re;
     df_add(ze.x, ze.y, cr.x, 0.f);
     df_add(ze.z, ze.w, cr.y, 0.f);
     ze = df_norm(ze);
     z[e] = ze;
-    if (set_p) pv[e] = ze;
+    if (set_p) {
+      pv[e] = ze;
+      if (PC) {
+        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+        cdf_mac(w, Sdf[e], ze);
+        ps[e] = df_norm(w);
+      }
+    }
     cdf_mac(rho, re, ze);
   }
   block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
@@ -795,11 +777,12 @@ size_t df_layout(const Plan& P, size_t* off /* 28 */, bool mf) {
   put(19, P.bj.p ? sizeof(double2) * P.n * P.k : 0);         // S r64
   // gradient correction (FP32 products): S^-1, diag(G^T A G)^-1, t = invD G^T u,
   // z, u = S^-1 r; z also holds diag(G^T A G)^-1 in FP64 while it is formed
-  put(20, P.gn ? sizeof(float2) * P.n : 0);
+  put(20, P.gn ? sizeof(float2) * ns : 0);
   put(21, P.gn ? sizeof(float2) * P.gn : 0);
   put(22, P.gn ? sizeof(float2) * P.gn * P.k : 0);
   put(23, P.gn ? std::max(sizeof(float4) * P.n * P.k, sizeof(double2) * (size_t)P.gn) : 0);
   put(24, P.gn ? sizeof(float2) * P.n * P.k : 0);
+  put(25, P.gn && mf ? sizeof(float) * P.k : 0);   // 1 / s_j per column
   return o;
 }
 
@@ -816,12 +799,13 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   const bool bj = !mf && P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[18]);
   double2* r64b = reinterpret_cast<double2*>(ws + off[19]);
-  const bool grad = !mf && P.gn > 0;   // diagonal scaling only (checked by pg_cocg)
+  const bool grad = P.gn > 0;   // diagonal scaling only (checked by pg_cocg / pg_cocg_multifreq)
   float2* Sinv = reinterpret_cast<float2*>(ws + off[20]);
   float2* invD = reinterpret_cast<float2*>(ws + off[21]);
   float2* gt = reinterpret_cast<float2*>(ws + off[22]);
   float4* gz = reinterpret_cast<float4*>(ws + off[23]);
   float2* gu = reinterpret_cast<float2*>(ws + off[24]);
+  float* gcinv = reinterpret_cast<float*>(ws + off[25]);
   const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
@@ -870,6 +854,18 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                                                                           dstatus)));
     k_mf_sdf<<<pg_blocks(P.n * k, 256), 256, 0, s>>>(S, P.n * k, Sdf);
     k_mf_df_matrix<<<pg_blocks(P.nnz, 256), 256, 0, s>>>(A, P.nnz, At);
+    if (grad) {
+      double2* tmp = reinterpret_cast<double2*>(gz);   // FP64 scratch until the first z
+      k_grad_sinv<<<pg_blocks(P.n * k, 256), 256, 0, s>>>(S, P.n * k, tmp);
+      k_to_f32<<<pg_blocks(P.n * k, 256), 256, 0, s>>>(tmp, P.n * k, Sinv);
+      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                       P.gn, tmp);
+      k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, invD);
+      std::vector<float> ci(k);
+      for (int i = 0; i < k; ++i) ci[i] = (float)(1.0 / col_scale[i]);
+      PG_CUDA_TRY(cudaMemcpyAsync(gcinv, ci.data(), sizeof(float) * k, cudaMemcpyHostToDevice, s));
+      PG_CUDA_TRY(cudaStreamSynchronize(s));   // ci must outlive the copy
+    }
     // the host copy of the scales must outlive the asynchronous copy
     PG_CUDA_TRY(cudaStreamSynchronize(s));
   } else if (bj) {
@@ -893,10 +889,10 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     if (grad) {
       double2* tmp = reinterpret_cast<double2*>(gz);   // FP64 scratch until the first z
       k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n, reinterpret_cast<double2*>(gz));
-      k_dfg_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(reinterpret_cast<double2*>(gz), P.n, Sinv);
+      k_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(reinterpret_cast<double2*>(gz), P.n, Sinv);
       k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                        P.gn, tmp);
-      k_dfg_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, invD);
+      k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, invD);
     }
   }
   PG_LAUNCH_CHECK();
@@ -935,6 +931,20 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   // no per-iteration launch arguments, so a run of them can be captured once
   // in a CUDA graph and replayed
   auto one_iteration = [&](cudaStream_t ss) {
+    if (mf && grad) {
+      PG_KSWITCH(k, (k_mf_spmm<K><<<spmv_grid, kThreads, 0, ss>>>(rowptr, col, At, P.n, dscale_hl, Sdf, pv, ps, q,
+                                                                  part, st, ctl),
+                     k_df_update<K, true, true><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl,
+                                                                          0, delta, gu, Sinv),
+                     k_grad_restrict32<K, true><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row,
+                                                                           o->gradt_val, invD, gu, P.gn, gt, ctl, 0,
+                                                                           gcinv),
+                     k_dfg_prolong<K, true><<<nbu, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv,
+                                                                      gt, r, P.n, gz, pv, 0, part, st, ctl, 0),
+                     k_df_pupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, gz, P.n, st, ctl,
+                                                                                              ps, Sdf)));
+      return;
+    }
     if (mf) {
       PG_KSWITCH(k, (k_mf_spmm<K><<<spmv_grid, kThreads, 0, ss>>>(rowptr, col, At, P.n, dscale_hl, Sdf, pv, ps, q,
                                                                   part, st, ctl),
@@ -951,7 +961,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     if (grad) {
       PG_KSWITCH(k, (k_df_update<K, false, true><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2,
                                                                            ctl, 0, delta, gu, Sinv),
-                     k_dfg_restrict<K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                     k_grad_restrict32<K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                                      invD, gu, P.gn, gt, ctl, 0),
                      k_dfg_prolong<K><<<nbu, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv, gt,
                                                                 r, P.n, gz, pv, 0, part, st, ctl, 0),
@@ -1051,7 +1061,16 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       PG_KSWITCH(k, (k_scale_cols_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(pv, P.n, clam)));
       if (mf) PG_KSWITCH(k, (k_scale_cols_df<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(ps, P.n, clam)));
     }
-    if (mf) {
+    if (mf && grad) {
+      PG_KSWITCH(k, (k_df_start<K, true><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, 0, part, ps),
+                     k_dfg_u_start<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, P.n, gu),
+                     k_grad_restrict32<K, true><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row,
+                                                                          o->gradt_val, invD, gu, P.gn, gt, ctl, 1,
+                                                                          gcinv),
+                     k_dfg_prolong<K, true><<<nb, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv,
+                                                                     gt, r, P.n, gz, pv, first ? 1 : 0, part, st, ctl,
+                                                                     1, ps, Sdf)));
+    } else if (mf) {
       PG_KSWITCH(k, (k_df_start<K, true><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, first ? 1 : 0, part, ps)));
     } else {
       if (bj) PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, r64b)));
@@ -1059,7 +1078,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
         // r = S r64, then z = r + S^-1 G invD G^T S^-1 r and rho = r^T z (p = z on the first cycle)
         PG_KSWITCH(k, (k_df_start<K><<<nb, kThreads, 0, s>>>(r64, S, P.n, r, y, pv, 0, part),
                        k_dfg_u_start<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, P.n, gu),
-                       k_dfg_restrict<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                       k_grad_restrict32<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                                       invD, gu, P.gn, gt, ctl, 1),
                        k_dfg_prolong<K><<<nb, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv, gt,
                                                                 r, P.n, gz, pv, first ? 1 : 0, part, st, ctl, 1)));
@@ -1168,11 +1187,13 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
 
 using pgk::df_layout;
 using pgk::run_cocg_df;
-extern "C" size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs) {
+extern "C" size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {
   if (n < 1 || !valid_k(nrhs)) return 0;
   pg_cocg_opts o;
   pg_cocg_default_opts(&o);
+  if (opts) o = *opts;
   o.precision = 2;
+  o.block_p = 0;
   Plan P = cg_plan(n, nnz, nrhs, &o);
   size_t off[28];
   return df_layout(P, off, true) + 256;
@@ -1192,14 +1213,21 @@ extern "C" int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, cons
       pg_set_error("pg_cocg_multifreq: column frequency scales must be positive");
       return PG_ERR_ARG;
     }
-  const size_t need = pg_cocg_multifreq_workspace_bytes(n, nnz, nrhs);
+  if (opts->grad_rowptr && (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row ||
+                            !opts->gradt_val || opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31))) {
+    pg_set_error("pg_cocg_multifreq: gradient correction needs all six G arrays and grad_cols >= 1");
+    return PG_ERR_ARG;
+  }
+  const size_t need = pg_cocg_multifreq_workspace_bytes(n, nnz, nrhs, opts);
   if (!workspace || workspace_bytes < need) {
     pg_set_error("pg_cocg_multifreq: workspace too small");
     return PG_ERR_WORKSPACE;
   }
   char* ws = reinterpret_cast<char*>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
-  Plan P = cg_plan(n, nnz, nrhs, opts);
+  pg_cocg_opts o = *opts;
+  o.block_p = 0;   // diagonal scaling per column
+  Plan P = cg_plan(n, nnz, nrhs, &o);
   return run_cocg_df(P, rowptr, col, reinterpret_cast<const double2*>(vals), reinterpret_cast<const double2*>(b),
-                     reinterpret_cast<double2*>(x), opts, result, relres_per_rhs, ws, pg_stream(stream), col_scale);
+                     reinterpret_cast<double2*>(x), &o, result, relres_per_rhs, ws, pg_stream(stream), col_scale);
 }
 

@@ -217,12 +217,16 @@ __global__ void __launch_bounds__(kThreads) k_ir_spmm(const int64_t* __restrict_
   if (arrive_last(&ctl->counter)) cg_alpha_final<K>(partial, gridDim.x, st, ctl, smem);
 }
 
-// ---- y += alpha p ; r -= alpha q ; partials rho = r^T r, w = sum |r|^2 |D|; last block: beta
-template <int K>
+// ---- y += alpha p ; r -= alpha q ; partials rho = r^T r, w = sum |r|^2 |D|; last block: beta.
+// GRAD (gradient correction): also u = S^-1 r; rho and beta are left to
+// k_irg_prolong.
+template <int K, bool GRAD = false>
 __global__ void __launch_bounds__(kThreads) k_ir_update(float2* __restrict__ y, float2* __restrict__ r,
                                                         const float2* __restrict__ pv, const float2* __restrict__ q,
                                                         const float* __restrict__ wd, int64_t n, CgState* st,
-                                                        double2* prho, double2* pw, CgCtl* ctl) {
+                                                        double2* prho, double2* pw, CgCtl* ctl,
+                                                        float2* __restrict__ u = nullptr,
+                                                        const float2* __restrict__ Sinv = nullptr) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ float2 al[kMaxK];
@@ -245,14 +249,84 @@ __global__ void __launch_bounds__(kThreads) k_ir_update(float2* __restrict__ y, 
     const float2 re = cfma(na, q[e], r[e]);
     y[e] = ye;
     r[e] = re;
-    rho = cfma(re, re, rho);
+    if constexpr (GRAD) {
+      u[e] = cmul(Sinv[e / K], re);
+    } else {
+      rho = cfma(re, re, rho);
+    }
     ww += (re.x * re.x + re.y * re.y) * wd[e / K];
   }
-  block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  if constexpr (!GRAD) block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   block_reduce_c32<K>(make_float2(ww, 0.f), smf, pw + (int64_t)blockIdx.x * K);
   // no early end on residual spikes: an inner solve only needs a 100x drop,
   // far above what a spike costs an FP32 recurrence (eps32 x the spike)
-  if (arrive_last(&ctl->counter)) cg_beta_final<K>(prho, pw, gridDim.x, st, ctl, 0, 0.0, smem, 1e30);
+  if (arrive_last(&ctl->counter)) cg_beta_final<K, GRAD>(prho, pw, gridDim.x, st, ctl, 0, 0.0, smem, 1e30);
+}
+
+// Gradient correction in the complex64 inner solve (diagonal scaling):
+// z = r + S^-1 (G t) in FP32, partial rho = r^T z; inside an iteration the
+// last block sets beta = rho / rho_old and rho for the RHS updated in it
+// (beta_iter == 1).  At an inner start (start = 1) p = z.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_irg_prolong(const int64_t* __restrict__ gp,
+                                                          const int32_t* __restrict__ gc,
+                                                          const double* __restrict__ gv,
+                                                          const float2* __restrict__ Sinv,
+                                                          const float2* __restrict__ t,
+                                                          const float2* __restrict__ r, int64_t n,
+                                                          float2* __restrict__ z, float2* __restrict__ pv,
+                                                          double2* prho, CgState* st, CgCtl* ctl, int start) {
+  if (!start && !ctl->pending) return;
+  __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
+  __shared__ float2 smf[(kThreads / 32) * kMaxK];
+  const int64_t total = n * K;
+  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+  float2 rho = make_float2(0.f, 0.f);
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const int64_t row = e / K;
+    const int rhs = (int)(e % K);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
+      const float g = __double2float_rn(gv[j]);
+      const float2 v = t[(int64_t)gc[j] * K + rhs];
+      acc.x = fmaf(g, v.x, acc.x);
+      acc.y = fmaf(g, v.y, acc.y);
+    }
+    const float2 re = r[e];
+    const float2 ze = cfma(Sinv[row], acc, re);
+    z[e] = ze;
+    if (start) pv[e] = ze;
+    rho = cfma(re, ze, rho);
+  }
+  block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  if (!start && arrive_last(&ctl->counter)) {
+    const double2 rr = sum_partials<K>(prho, gridDim.x, threadIdx.x < K ? threadIdx.x : 0, smem);
+    if (threadIdx.x < K) {
+      CgState& S = st[threadIdx.x];
+      if (S.beta_iter == 1) {
+        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+          S.breakdown = 1;
+          S.active = 0;
+          S.beta = make_double2(0.0, 0.0);
+        } else {
+          S.beta = ddiv(rr, S.rho);
+        }
+        S.rho = rr;
+      } else {
+        S.beta = make_double2(0.0, 0.0);
+      }
+    }
+    if (threadIdx.x == 0) ctl->counter = 0;
+  }
+}
+
+// u = S^-1 r at an inner start
+template <int K>
+__global__ void k_irg_u_start(const float2* __restrict__ r, const float2* __restrict__ Sinv, int64_t n,
+                              float2* __restrict__ u) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    u[e] = cmul(Sinv[e / K], r[e]);
 }
 
 // p = r + beta p, once per fresh beta (gated like the double-float solver)
@@ -439,15 +513,28 @@ size_t ir_layout(const Plan& P, size_t* off /* 16 */) {
   put(13, sizeof(int) * (P.k + 1));             // want, status
   put(14, P.bj.p ? sizeof(double2) * P.bj.s_size() : 0);   // block-Jacobi factors
   put(15, sizeof(double2) * P.n * P.k);         // S r64 (block-Jacobi) / c y
+  // gradient correction (FP32): S^-1, diag(G^T A G)^-1, t, z, u = S^-1 r
+  put(16, P.gn ? sizeof(float2) * P.n : 0);
+  put(17, P.gn ? sizeof(float2) * P.gn : 0);
+  put(18, P.gn ? sizeof(float2) * P.gn * P.k : 0);
+  put(19, P.gn ? sizeof(float2) * P.n * P.k : 0);
+  put(20, P.gn ? sizeof(float2) * P.n * P.k : 0);
   return o;
 }
 
 int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const double2* A, const double2* b,
                 double2* x, const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out, char* ws,
                 cudaStream_t s) {
-  size_t off[16];
+  size_t off[28];
   ir_layout(P, off);
   const bool bj = P.bj.p > 0;
+  const bool grad = P.gn > 0;   // diagonal scaling only (checked by pg_cocg)
+  float2* gSinv = reinterpret_cast<float2*>(ws + off[16]);
+  float2* ginvD = reinterpret_cast<float2*>(ws + off[17]);
+  float2* gt = reinterpret_cast<float2*>(ws + off[18]);
+  float2* gz = reinterpret_cast<float2*>(ws + off[19]);
+  float2* gu = reinterpret_cast<float2*>(ws + off[20]);
+  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   float2* At = reinterpret_cast<float2*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);
@@ -495,6 +582,14 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   } else {
     k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, wd, dstatus);
     k_ir_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
+    if (grad) {
+      double2* tmp = reinterpret_cast<double2*>(ws + off[15]);   // FP64 scratch (n * k >= n, gn entries)
+      k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n, tmp);
+      k_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(tmp, P.n, gSinv);
+      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                       P.gn, tmp);
+      k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, ginvD);
+    }
   }
   k_ir_wd_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(wd, P.n, wdf);
   PG_LAUNCH_CHECK();
@@ -529,6 +624,16 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       launch_ir_spmv1(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl);
     else
       PG_KSWITCH(k, (launch_ir_spmm<K>(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl)));
+    if (grad) {
+      PG_KSWITCH(k, (k_ir_update<K, true><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, gu,
+                                                                    gSinv),
+                     k_grad_restrict32<K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                        ginvD, gu, P.gn, gt, ctl, 0),
+                     k_irg_prolong<K><<<nbu, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, gSinv, gt,
+                                                                r, P.n, gz, pv, part, st, ctl, 0),
+                     k_ir_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, gz, P.n, st, ctl)));
+      return;
+    }
     PG_KSWITCH(k, (k_ir_update<K><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl),
                    k_ir_pupdate<K><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, r, P.n, st, ctl)));
   };
@@ -622,6 +727,14 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     if (bj) {
       PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(Sblk, P.bj, r64, aux),
                      k_ir_start<K><<<nb, kThreads, 0, s>>>(aux, nullptr, cinv, wdf, P.n, r, y, pv, part, part2)));
+    } else if (grad) {
+      // r = S r64 / c, then z = r + S^-1 G invD G^T S^-1 r, p = z, rho = r^T z (w from the start kernel)
+      PG_KSWITCH(k, (k_ir_start<K><<<nb, kThreads, 0, s>>>(r64, S, cinv, wdf, P.n, r, y, pv, part, part2),
+                     k_irg_u_start<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r, gSinv, P.n, gu),
+                     k_grad_restrict32<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                       ginvD, gu, P.gn, gt, ctl, 1),
+                     k_irg_prolong<K><<<nb, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, gSinv, gt, r,
+                                                              P.n, gz, pv, part, st, ctl, 1)));
     } else {
       PG_KSWITCH(k, (k_ir_start<K><<<nb, kThreads, 0, s>>>(r64, S, cinv, wdf, P.n, r, y, pv, part, part2)));
     }

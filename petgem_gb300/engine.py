@@ -392,12 +392,13 @@ class DeviceMesh:
                          precision=precision, reorth=reorth, raise_on_fail=raise_on_fail, ksp=ksp,
                          check_every=check_every, blocks=blocks, inner_rtol=inner_rtol, gradient=gradient)
 
-    def solve_frequencies(self, vals0, frequency0, b, frequencies, **kw):
+    def solve_frequencies(self, vals0, frequency0, b, frequencies, precond="jacobi", **kw):
         """Columns of b (complex128 [N, k]) at their own frequencies in one
         solve: vals0 is A assembled (PEC applied) at frequency0; see
-        solve_csr_frequencies."""
+        solve_csr_frequencies.  precond="grad" adds the gradient correction."""
         scale = [float(f) / float(frequency0) for f in frequencies]
-        return solve_csr_frequencies(self.rowptr, self.col, vals0, b, scale, **kw)
+        gradient = self.gradient_map() if precond == "grad" else None
+        return solve_csr_frequencies(self.rowptr, self.col, vals0, b, scale, gradient=gradient, **kw)
 
     def receiver_fields(self, x, receivers, frequency):
         """(fields complex128 [R', 6], kept mask) like petgem fieldInterpolator
@@ -678,11 +679,12 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
 
 
 def solve_csr_frequencies(rowptr, col, vals0, b, col_scale, x0=None, rtol=1e-8, max_it=100000, raise_on_fail=True,
-                          check_every=50):
+                          check_every=50, gradient=None):
     """Several frequencies in one double-float COCG: column j of b (complex128
     [N, k], k in 1,2,4,8,16,32) is solved with (Re A0 + i s_j Im A0), where
     vals0 = A0 = K - i omega_0 mu M (PEC applied) and s_j = omega_j / omega_0.
-    One matrix read per iteration serves every column."""
+    One matrix read per iteration serves every column.  gradient: a
+    GradientMap for the gradient correction (see solve_csr)."""
     if b.ndim != 2:
         raise ValueError("b must be [N, k]")
     _check_csr("solve_csr_frequencies", rowptr, col, vals0, b)
@@ -697,9 +699,11 @@ def solve_csr_frequencies(rowptr, col, vals0, b, col_scale, x0=None, rtol=1e-8, 
     o = _lib.CocgOpts()
     lib.pg_cocg_default_opts(ctypes.byref(o))
     o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), 2, int(check_every)
+    if gradient is not None:
+        _set_gradient(o, gradient)
     res = _lib.GmresResult()
     rr = (ctypes.c_double * k)()
-    ws = _ws(_lib.query("pg_cocg_multifreq_workspace_bytes", N, nnz, k) + 256, b.device)
+    ws = _ws(_lib.query("pg_cocg_multifreq_workspace_bytes", N, nnz, k, ctypes.byref(o)) + 256, b.device)
     st = lib.pg_cocg_multifreq(_p(rowptr), _p(col), _p(vals0), N, nnz, _p(b.contiguous()), _p(x), k,
                                ctypes.c_void_p(sc.ctypes.data), ctypes.byref(o), ctypes.byref(res),
                                ctypes.cast(rr, ctypes.c_void_p), _p(ws), ws.numel(), _s())

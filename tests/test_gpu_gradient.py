@@ -7,9 +7,12 @@
 * At larger sizes the map is checked through a size-independent property:
   K G = 0, seen as A(f1) G f2 - A(f2) G f1 = (f2 - f1) K G on two assembled
   systems.
-* COCG with the correction B = D^-1 + G diag(G^T A G)^-1 G^T reaches the
-  true 1e-10 residual in far fewer iterations than Jacobi alone, with the
-  same solution (1 and 4 RHS), and is deterministic.
+* COCG with the correction B = D^-1 + G diag(G^T A G)^-1 G^T (FP64,
+  double-float, complex64 inner solves in FP64 refinement) reaches the true
+  1e-10 residual in far fewer iterations than Jacobi alone, with the same
+  solution (1 and 4 RHS), and is deterministic; GMRES(30) and the
+  several-frequency solver take it too; the MT system is checked against
+  the oracle's LU.
 """
 import numpy as np
 import pytest
@@ -100,7 +103,7 @@ def test_gradient_map_is_curl_free_at_size(p, n):
     assert abs(A1 @ G).max() >= 1e-6 * abs(A1).max()   # the mass part is there
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df64"])
+@pytest.mark.parametrize("prec", ["fp64", "df64", "ir32"])
 @pytest.mark.parametrize("p", [2, 3])
 def test_cocg_gradient_correction_matches_jacobi(p, prec, monkeypatch):
     mdl = synthetic.csem_two_layer(6, p)
@@ -115,7 +118,10 @@ def test_cocg_gradient_correction_matches_jacobi(p, prec, monkeypatch):
         xj, ij = m.solve(vals, rhs, ksp="cocg", precond="jacobi", rtol=1e-10, max_it=100000)
         xg, ig = m.solve(vals, rhs, ksp="cocg", precond="grad", rtol=1e-10, max_it=100000, precision=prec)
         assert ig.status == 0 and max(ig.relres_per_rhs) <= 1e-10
-        assert ig.iterations * 3 < ij.iterations, (ig.iterations, ij.iterations)
+        # ir32 counts the inner iterations of all its refinement steps (each
+        # restarts the Krylov space), hence the smaller factor
+        factor = 2 if prec == "ir32" else 3
+        assert ig.iterations * factor < ij.iterations, (ig.iterations, ij.iterations)
         assert rel_norm(xg.cpu().numpy(), xj.cpu().numpy()) <= 1e-7
         # bitwise repeatable with the product variant fixed (with one RHS the
         # autotuner picks the lanes per row by timing, and each variant sums
@@ -165,7 +171,7 @@ def test_gradient_correction_rejects_other_forms():
     g = m.gradient_map()
     with pytest.raises(ValueError):
         solve_csr(m.rowptr, m.col, vals, b, ksp="cocg", blocks=(2, m.nE, m.nF, m.T), gradient=g)
-    for ksp, prec in (("cocg", "mixed"), ("cocg", "ir32"), ("gmres", "mixed")):
+    for ksp, prec in (("cocg", "mixed"), ("gmres", "mixed")):
         with pytest.raises(_lib.PetgemError) as e:
             solve_csr(m.rowptr, m.col, vals, b, ksp=ksp, precision=prec, gradient=g)
         assert e.value.status == -1
@@ -203,3 +209,31 @@ def test_mt_solve_with_gradient_matches_oracle():
         Fo, _ = system.receiver_fields(mm, x, mdl.nodes, mdl.tets, 3, mdl.receivers, f)
         Fd, _ = m.receiver_fields(X[:, k].contiguous(), mdl.receivers, f)
         assert rel_norm(Fd.cpu().numpy(), Fo) <= 2e-4
+
+
+def test_multifrequency_gradient_matches_per_frequency():
+    """Several frequencies in one double-float COCG with the gradient
+    correction (diag(G^T A_j G) = s_j diag(G^T A_0 G)): every column equals
+    a separate FP64 solve at its own frequency, in fewer iterations than the
+    same solve without the correction."""
+    mdl = synthetic.csem_two_layer(6, 2)
+    m = _mesh(mdl.nodes, mdl.tets, 2)
+    f0 = 1.0
+    freqs = [0.25, 0.5, 1.0, 2.0]
+    vals0 = m.assemble(mdl.sigma, f0, pec=True)
+    cols, fcol = [], []
+    for f in freqs:
+        for x0 in (-500.0, 300.0):
+            b, _ = m.source_vector(dict(mdl.source, position=[x0, 20.0, 50.0], frequency=f))
+            m.pec_rhs(b)
+            cols.append(b)
+            fcol.append(f)
+    B = torch.stack(cols, 1).contiguous()
+    Xg, ig = m.solve_frequencies(vals0, f0, B, fcol, precond="grad", rtol=1e-10)
+    Xj, ij = m.solve_frequencies(vals0, f0, B, fcol, rtol=1e-10)
+    assert ig.status == 0 and max(ig.relres_per_rhs) <= 1e-10
+    assert ig.iterations * 3 < ij.iterations, (ig.iterations, ij.iterations)
+    for j, f in enumerate(fcol):
+        vf = m.assemble(mdl.sigma, f, pec=True)
+        xf, _ = m.solve(vf, B[:, j].contiguous(), ksp="cocg", precond="grad", rtol=1e-11, max_it=100000)
+        assert rel_norm(Xg[:, j].cpu().numpy(), xf.cpu().numpy()) <= 1e-7
