@@ -452,9 +452,10 @@ typedef struct pg_gmres_opts {
    * DOFs stay diagonal). */
   int block_p;
   int64_t block_edges, block_faces, block_volumes;
-  /* gradient correction (precision 0 with diagonal Jacobi, block_p 0;
-   * grad_rowptr NULL = off), as in pg_cocg_opts: GMRES runs on A B with
-   * B = D^-1 + G diag(G^T A G)^-1 G^T (right preconditioning). */
+  /* gradient correction (diagonal Jacobi, block_p 0; grad_rowptr NULL =
+   * off), as in pg_cocg_opts: GMRES runs on A B with
+   * B = D^-1 + G diag(G^T A G)^-1 G^T (right preconditioning; in precision
+   * 1 the correction of the Arnoldi steps runs on the complex64 basis). */
   int64_t grad_cols;
   const int64_t* grad_rowptr;
   const int32_t* grad_col;
@@ -513,7 +514,7 @@ typedef struct pg_cocg_opts {
    * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 8x the
    * inner iterations of the first refinement step (at least 1,000) */
   double inner_rtol;
-  /* gradient correction (pg_cocg: precision 0, 2 or 3; pg_gmres: precision 0;
+  /* gradient correction (pg_cocg: precision 0, 2 or 3; pg_gmres: 0 or 1;
    * diagonal Jacobi, block_p 0; grad_rowptr NULL = off): G, n rows by grad_cols columns, and
    * its transpose from pg_gradient_map.  The preconditioner becomes
    *   B = D^-1 + G diag(G^T A G)^-1 G^T
@@ -586,7 +587,10 @@ int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, const double* v
  * the one it would reach alone; every launch serves all systems.  With
  * opts->block_p > 0 each system gets entity block-Jacobi scaling and
  * seg_entities (host [3 * n_seg]) gives its (edges, faces, elements);
- * otherwise seg_entities may be NULL.  b, x complex128 [n * nrhs] (RHS
+ * otherwise seg_entities may be NULL.  The gradient correction of
+ * pg_cocg_opts applies with diagonal scaling; G is then block-diagonal over
+ * the systems (system j's map with its rows shifted by seg_rows[j] and its
+ * columns by the columns of the systems before it).  b, x complex128 [n * nrhs] (RHS
  * fastest), nrhs right-hand sides per system.  relres and its (host,
  * [n_seg * nrhs], system-major, either may be NULL) receive each system's
  * final true relative residual and iteration count; result.iterations is the

@@ -69,6 +69,17 @@ __device__ int seg_live(const CgState* st, int j) {
   return live;
 }
 
+// 1 if some right-hand side of system j was updated in this iteration
+template <int K>
+__device__ int seg_due(const CgState* st, int j) {
+  __shared__ int due;
+  if (threadIdx.x == 0) due = 0;
+  __syncthreads();
+  if (threadIdx.x < K && st[j * K + threadIdx.x].beta_iter == 1) atomicOr(&due, 1);
+  __syncthreads();
+  return due;
+}
+
 template <int K>
 __device__ void seg_alpha_final(const double2* partial, const Seg& g, CgState* st, CgCtl* ctl) {
   for (int t = threadIdx.x >> 5; t < g.S * K; t += kThreads / 32) {
@@ -91,7 +102,8 @@ __device__ void seg_alpha_final(const double2* partial, const Seg& g, CgState* s
   if (threadIdx.x == 0) ctl->counter = 0;
 }
 
-template <int K>
+// GRAD (gradient correction): rho and beta are left to k_sg_prolong
+template <int K, bool GRAD = false>
 __device__ void seg_beta_final(const double2* prho, const double2* pw, const Seg& g, CgState* st, CgCtl* ctl,
                                double delta) {
   __shared__ int any, stop;
@@ -101,7 +113,8 @@ __device__ void seg_beta_final(const double2* prho, const double2* pw, const Seg
   }
   __syncthreads();
   for (int t = threadIdx.x >> 5; t < g.S * K; t += kThreads / 32) {
-    const double2 rho = seg_pair_sum<K>(prho, g, t);
+    double2 rho = make_double2(0.0, 0.0);
+    if constexpr (!GRAD) rho = seg_pair_sum<K>(prho, g, t);
     const double2 w = seg_pair_sum<K>(pw, g, t);
     if ((threadIdx.x & 31) == 0) {
       CgState& S = st[t];
@@ -110,14 +123,16 @@ __device__ void seg_beta_final(const double2* prho, const double2* pw, const Seg
         S.its += 1;
         S.res = sqrt(w.x);
         if (!isfinite(S.res)) ctl->nonfinite = 1;
-        if (S.rho.x == 0.0 && S.rho.y == 0.0) {
-          S.breakdown = 1;
-          S.active = 0;
-          S.beta = make_double2(0.0, 0.0);
-        } else {
-          S.beta = ddiv(rho, S.rho);
+        if constexpr (!GRAD) {
+          if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+            S.breakdown = 1;
+            S.active = 0;
+            S.beta = make_double2(0.0, 0.0);
+          } else {
+            S.beta = ddiv(rho, S.rho);
+          }
+          S.rho = rho;
         }
-        S.rho = rho;
         if (S.res <= S.target || !isfinite(S.res)) S.active = 0;
         else if (S.res <= delta * S.res0 || S.res > 1e3 * S.res0) atomicOr(&stop, 1);
       } else {
@@ -302,12 +317,15 @@ __global__ void __launch_bounds__(kThreads) k_sg_spmm_grp(const int64_t* __restr
   if (arrive_last(&ctl->counter)) seg_alpha_final<K>(partial, g, st, ctl);
 }
 
-// y += alpha p ; r -= alpha q with each system's alpha; partial rho and w
-template <int K>
+// y += alpha p ; r -= alpha q with each system's alpha; partial rho and w.
+// GRAD: also u = S^-1 r (FP32); rho and beta are left to k_sg_prolong.
+template <int K, bool GRAD = false>
 __global__ void __launch_bounds__(kThreads) k_sg_update(float4* __restrict__ y, float4* __restrict__ r,
                                                         const float4* __restrict__ pv, const float4* __restrict__ q,
                                                         const float* __restrict__ wd, Seg g, CgState* st,
-                                                        double2* prho, double2* pw, CgCtl* ctl, double delta) {
+                                                        double2* prho, double2* pw, CgCtl* ctl, double delta,
+                                                        float2* __restrict__ u = nullptr,
+                                                        const float2* __restrict__ Sinv = nullptr) {
   if (!ctl->any_active) return;
   const SegPos sp = seg_pos(g);
   __shared__ float4 al[kMaxK];
@@ -329,13 +347,91 @@ __global__ void __launch_bounds__(kThreads) k_sg_update(float4* __restrict__ y, 
       re = df_norm(re);
       y[e] = ye;
       r[e] = re;
-      cdf_mac(rho, re, re);
+      if constexpr (GRAD) {
+        u[e] = cmul(Sinv[e / K], make_float2(re.x, re.z));
+      } else {
+        cdf_mac(rho, re, re);
+      }
       ww += (re.x * re.x + re.z * re.z) * wd[e / K];
     }
   __shared__ float4 smf[(kThreads / 32) * kMaxK];
-  block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  if constexpr (!GRAD) block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   block_reduce_f<K>(ww, reinterpret_cast<float*>(smf), pw + (int64_t)blockIdx.x * K);
-  if (arrive_last(&ctl->counter)) seg_beta_final<K>(prho, pw, g, st, ctl, delta);
+  if (arrive_last(&ctl->counter)) seg_beta_final<K, GRAD>(prho, pw, g, st, ctl, delta);
+}
+
+// Gradient correction, several systems: z = r + S^-1 (G t) over each
+// block's own system rows (G is block-diagonal over the systems), partial
+// rho = r^T z per block; in an iteration the last block sets every system's
+// beta = rho / rho_old and rho for the RHS updated in it (beta_iter == 1).
+// At a cycle start (start = 1) p = z when set_p.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sg_prolong(const int64_t* __restrict__ gp,
+                                                         const int32_t* __restrict__ gc,
+                                                         const double* __restrict__ gv,
+                                                         const float2* __restrict__ Sinv,
+                                                         const float2* __restrict__ t,
+                                                         const float4* __restrict__ r, Seg g,
+                                                         float4* __restrict__ z, float4* __restrict__ pv, int set_p,
+                                                         double2* prho, CgState* st, CgCtl* ctl, int start) {
+  if (!start && !ctl->pending) return;
+  const SegPos sp = seg_pos(g);
+  // systems with no RHS updated in this iteration skip their rows (a
+  // converged system keeps one block)
+  const int due = start ? 1 : seg_due<K>(st, sp.j);
+  __shared__ float4 smf[(kThreads / 32) * kMaxK];
+  const int64_t base = sp.r0 * K, total = (sp.r1 - sp.r0) * K;
+  const int64_t chunk = ((total + sp.nbj - 1) / sp.nbj + K - 1) / K * K;
+  const int64_t lo = base + (int64_t)sp.lb * chunk, hi = due ? min(base + total, lo + chunk) : lo;
+  float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+    const int64_t row = e / K;
+    const int rhs = (int)(e % K);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
+      const float gf = __double2float_rn(gv[j]);
+      const float2 v = t[(int64_t)gc[j] * K + rhs];
+      acc.x = fmaf(gf, v.x, acc.x);
+      acc.y = fmaf(gf, v.y, acc.y);
+    }
+    const float2 cr = cmul(Sinv[row], acc);
+    const float4 re = r[e];
+    float4 ze = re;
+    df_add(ze.x, ze.y, cr.x, 0.f);
+    df_add(ze.z, ze.w, cr.y, 0.f);
+    ze = df_norm(ze);
+    z[e] = ze;
+    if (set_p) pv[e] = ze;
+    cdf_mac(rho, re, ze);
+  }
+  block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
+  if (!start && arrive_last(&ctl->counter)) {
+    for (int tt = threadIdx.x >> 5; tt < g.S * K; tt += kThreads / 32) {
+      const double2 rr = seg_pair_sum<K>(prho, g, tt);
+      if ((threadIdx.x & 31) == 0) {
+        CgState& S = st[tt];
+        if (S.beta_iter == 1) {
+          if (S.rho.x == 0.0 && S.rho.y == 0.0) {
+            S.breakdown = 1;
+            S.active = 0;
+            S.beta = make_double2(0.0, 0.0);
+          } else {
+            S.beta = ddiv(rr, S.rho);
+          }
+          S.rho = rr;
+        } else {
+          S.beta = make_double2(0.0, 0.0);
+        }
+      }
+    }
+    if (threadIdx.x == 0) ctl->counter = 0;
+  }
+}
+
+template <int K>
+__global__ void k_sg_u_start(const double2* __restrict__ r64, int64_t n, float2* __restrict__ u) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * K; e += (int64_t)gridDim.x * blockDim.x)
+    u[e] = make_float2((float)r64[e].x, (float)r64[e].y);
 }
 
 // p = r + beta p with each system's beta
@@ -531,13 +627,14 @@ void seg_rebalance(const int64_t* rows, int S, int k, const std::vector<char>& a
 
 struct SegPlan {
   int64_t n, nnz;
+  int64_t gn = 0;           // gradient correction: columns of the block-diagonal G (0: off)
   int k, S, nb;
   int p;                    // block-Jacobi order (0: diagonal)
   std::vector<BjInfo> bj;   // per system, c0 = its first row
   std::vector<int64_t> soff;  // per system offset of its factors (S + 1 entries)
 };
 
-size_t sg_layout(const SegPlan& P, size_t* off /* 18 */) {
+size_t sg_layout(const SegPlan& P, size_t* off /* 24 */) {
   size_t o = 0;
   auto put = [&](int idx, size_t bytes) { off[idx] = o; o += pg_align256(bytes); };
   const size_t pairs = (size_t)P.S * P.k;
@@ -559,6 +656,12 @@ size_t sg_layout(const SegPlan& P, size_t* off /* 18 */) {
   put(15, sizeof(int) * (P.S + 1));              // system blocks
   put(16, P.p ? sizeof(double2) * P.soff[P.S] : 0);      // block-Jacobi factors
   put(17, P.p ? sizeof(double2) * P.n * P.k : 0);        // S r64
+  // gradient correction (FP32 products): S^-1, invD, t, z (FP64 scratch at setup), u
+  put(18, P.gn ? sizeof(float2) * P.n : 0);
+  put(19, P.gn ? sizeof(float2) * P.gn : 0);
+  put(20, P.gn ? sizeof(float2) * P.gn * P.k : 0);
+  put(21, P.gn ? std::max(sizeof(float4) * P.n * P.k, sizeof(double2) * (size_t)std::max(P.n, P.gn)) : 0);
+  put(22, P.gn ? sizeof(float2) * P.n * P.k : 0);
   return o;
 }
 
@@ -593,7 +696,7 @@ int seg_plan(int64_t n, int64_t nnz, int k, const int64_t* rows, int S, const in
 int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, const int32_t* col, const double2* A,
                  const double2* b, double2* x, const pg_cocg_opts* o, pg_gmres_result* res, double* relres_out,
                  int64_t* its_out, char* ws, cudaStream_t s) {
-  size_t off[18];
+  size_t off[24];
   sg_layout(P, off);
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* Sd = reinterpret_cast<double2*>(ws + off[1]);
@@ -624,6 +727,13 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   double2* r64b = reinterpret_cast<double2*>(ws + off[17]);
   const int k = P.k, G = P.nb;
   const bool bj = P.p > 0;
+  const bool grad = P.gn > 0;   // diagonal scaling only (checked by pg_cocg_segments)
+  float2* gSinv = reinterpret_cast<float2*>(ws + off[18]);
+  float2* ginvD = reinterpret_cast<float2*>(ws + off[19]);
+  float2* gt = reinterpret_cast<float2*>(ws + off[20]);
+  float4* gz = reinterpret_cast<float4*>(ws + off[21]);
+  float2* gu = reinterpret_cast<float2*>(ws + off[22]);
+  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   std::vector<int> hblk = seg_blocks(hrows, P.S, k), cur_blk;
   std::vector<char> sys_active(P.S, 1);
   PG_CUDA_TRY(cudaMemcpyAsync(drows, hrows, sizeof(int64_t) * (P.S + 1), cudaMemcpyHostToDevice, s));
@@ -663,6 +773,14 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   } else {
     k_cg_scaling<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, Sd, wd, dstatus);
     k_df_scale_matrix<<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, Sd, At, wdf, wd);
+    if (grad) {
+      double2* tmp = reinterpret_cast<double2*>(gz);   // FP64 scratch until the first z
+      k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(Sd, P.n, tmp);
+      k_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(tmp, P.n, gSinv);
+      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                       P.gn, tmp);
+      k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, ginvD);
+    }
   }
   PG_LAUNCH_CHECK();
   std::vector<double> bnorm(pairs), rn(pairs), tgt(pairs), sc(pairs), sc_prev(pairs, 1.0), scal(4 * (size_t)pairs);
@@ -739,6 +857,16 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   const double delta = 1e-3;
   auto one_iteration = [&](cudaStream_t ss) {
     launch_prod(variant, ss);
+    if (grad) {
+      PG_KSWITCH(k, (k_sg_update<K, true><<<G, kThreads, 0, ss>>>(y, r, pv, q, wdf, g, st, part, part2, ctl, delta, gu,
+                                                                  gSinv),
+                     k_grad_restrict32<K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                        ginvD, gu, P.gn, gt, ctl, 0),
+                     k_sg_prolong<K><<<G, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, gSinv, gt, r,
+                                                             g, gz, pv, 0, part, st, ctl, 0),
+                     k_sg_pupdate<K><<<G, kThreads, 0, ss>>>(pv, gz, g, st, ctl)));
+      return;
+    }
     PG_KSWITCH(k, (k_sg_update<K><<<G, kThreads, 0, ss>>>(y, r, pv, q, wdf, g, st, part, part2, ctl, delta),
                    k_sg_pupdate<K><<<G, kThreads, 0, ss>>>(pv, r, g, st, ctl)));
   };
@@ -850,8 +978,21 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
         PG_KSWITCH(k, (k_bj_apply<K><<<pg_blocks(B.n * K, 256), 256, 0, s>>>(Sblk + P.soff[j], B, r64 + hrows[j] * K,
                                                                              r64b + hrows[j] * K)));
       }
-    PG_KSWITCH(k, (k_sg_start<K><<<G, kThreads, 0, s>>>(bj ? r64b : r64, Sd, g, r, y, pv, first ? 1 : 0, part),
-                   k_sg_cycle_init<K><<<1, kThreads, 0, s>>>(part, g, st, rnorm, target, want, ctl, first ? 1 : 0)));
+    if (grad) {
+      // r = S r64, then z = r + S^-1 G invD G^T S^-1 r (S^-1 r = r64), rho = r^T z, p = z on the first cycle
+      PG_KSWITCH(k, (k_sg_start<K><<<G, kThreads, 0, s>>>(r64, Sd, g, r, y, pv, 0, part),
+                     k_sg_u_start<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, P.n, gu),
+                     k_grad_restrict32<K><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
+                                                                       ginvD, gu, P.gn, gt, ctl, 1),
+                     k_sg_prolong<K><<<G, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, gSinv, gt, r, g,
+                                                            gz, pv, first ? 1 : 0, part, st, ctl, 1),
+                     k_sg_cycle_init<K><<<1, kThreads, 0, s>>>(part, g, st, rnorm, target, want, ctl,
+                                                               first ? 1 : 0)));
+    } else {
+      PG_KSWITCH(k, (k_sg_start<K><<<G, kThreads, 0, s>>>(bj ? r64b : r64, Sd, g, r, y, pv, first ? 1 : 0, part),
+                     k_sg_cycle_init<K><<<1, kThreads, 0, s>>>(part, g, st, rnorm, target, want, ctl,
+                                                               first ? 1 : 0)));
+    }
     if (first) {
       // PG_SPMV_VARIANT forces a candidate; else the fastest on these operands
       const char* fv = getenv("PG_SPMV_VARIANT");
@@ -940,7 +1081,8 @@ extern "C" size_t pg_cocg_segments_workspace_bytes(int64_t n, int64_t nnz, int n
   if (!opts || n < 1 || !valid_k(nrhs)) return 0;
   SegPlan P;
   if (seg_plan(n, nnz, nrhs, seg_rows, n_seg, seg_entities, opts->block_p, P) != PG_OK) return 0;
-  size_t off[18];
+  P.gn = opts->grad_rowptr && opts->grad_cols > 0 ? opts->grad_cols : 0;
+  size_t off[24];
   return sg_layout(P, off) + 256;
 }
 
@@ -959,6 +1101,14 @@ extern "C" int pg_cocg_segments(const int64_t* rowptr, const int32_t* col, const
                  "system's (edges, faces, elements) matching its rows");
     return PG_ERR_ARG;
   }
+  if (opts->grad_rowptr && (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row ||
+                            !opts->gradt_val || opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) ||
+                            opts->block_p > 0)) {
+    pg_set_error("pg_cocg_segments: gradient correction needs all six G arrays (block-diagonal over the systems), "
+                 "grad_cols >= 1 and diagonal Jacobi (block_p 0)");
+    return PG_ERR_ARG;
+  }
+  P.gn = opts->grad_rowptr && opts->grad_cols > 0 ? opts->grad_cols : 0;
   const size_t need = pg_cocg_segments_workspace_bytes(n, nnz, nrhs, seg_rows, n_seg, seg_entities, opts);
   if (!workspace || workspace_bytes < need) {
     pg_set_error("pg_cocg_segments: workspace too small");

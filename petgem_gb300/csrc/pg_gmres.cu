@@ -390,7 +390,7 @@ size_t ws_layout(const Plan& P, size_t* off /* 24 */) {
   // gradient correction: invD, t, u = T v (Arnoldi precision), d = diag A, ones
   put(16, P.gn ? sizeof(double2) * P.gn : 0);
   put(17, P.gn ? sizeof(double2) * P.gn * P.k : 0);
-  put(18, P.gn ? P.csize * P.n * P.k : 0);
+  put(18, P.gn ? sizeof(double2) * P.n * P.k : 0);   // Arnoldi precision in the steps, FP64 in the update
   put(19, P.gn ? sizeof(double2) * P.n : 0);
   put(20, P.gn ? sizeof(double2) * P.n : 0);
   return o;
@@ -486,7 +486,7 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
   const bool bj = P.bj.p > 0;
   double2* Sblk = reinterpret_cast<double2*>(ws + off[14]);
   double2* Minv = reinterpret_cast<double2*>(ws + off[15]);
-  const bool grad = P.gn > 0;   // diagonal Jacobi and complex128 only (checked by pg_gmres)
+  const bool grad = P.gn > 0;   // diagonal Jacobi only (checked by pg_gmres)
   double2* invD = reinterpret_cast<double2*>(ws + off[16]);
   double2* gt = reinterpret_cast<double2*>(ws + off[17]);
   C* gu = reinterpret_cast<C*>(ws + off[18]);
@@ -763,9 +763,9 @@ extern "C" int pg_gmres(const int64_t* rowptr, const int32_t* col, const double*
   }
   if (opts->grad_rowptr) {
     if (!opts->grad_col || !opts->grad_val || !opts->gradt_rowptr || !opts->gradt_row || !opts->gradt_val ||
-        opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0 || opts->precision != 0) {
-      pg_set_error("pg_gmres: gradient correction needs all six G arrays, grad_cols >= 1, precision 0 and diagonal "
-                   "Jacobi (block_p 0)");
+        opts->grad_cols < 1 || opts->grad_cols >= (int64_t(1) << 31) || opts->block_p > 0) {
+      pg_set_error("pg_gmres: gradient correction needs all six G arrays, grad_cols >= 1 and diagonal Jacobi "
+                   "(block_p 0)");
       return PG_ERR_ARG;
     }
   }

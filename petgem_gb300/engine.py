@@ -381,7 +381,8 @@ class DeviceMesh:
         precond="block": entity block-Jacobi (each edge / face / volume's
         diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal;
         "grad": diagonal Jacobi plus the gradient correction
-        D^-1 + G diag(G^T A G)^-1 G^T (COCG in fp64 or df64, GMRES in fp64;
+        D^-1 + G diag(G^T A G)^-1 G^T (COCG in fp64, df64 or ir32, GMRES in
+        fp64 or mixed;
         p <= 3; gradient_map; pec=False for systems without PEC rows, e.g.
         MT, which want fp64: their true residual has an FP64 floor)."""
         if precond not in ("block", "jacobi", "grad"):
@@ -733,7 +734,32 @@ def concat_systems(systems):
             np.asarray(rows, dtype=np.int64))
 
 
-def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_fail=True, check_every=50):
+def concat_gradients(gradients, rows):
+    """Block-diagonal GradientMap of several systems' maps: system j's rows
+    shifted by rows[j] and its columns by the columns before it."""
+    rps, cols, vals, trps, trows, tvals = [], [], [], [], [], []
+    nz, c0 = 0, 0
+    for j, g in enumerate(gradients):
+        n_j = int(g.rowptr.numel()) - 1
+        if n_j != int(rows[j + 1] - rows[j]):
+            raise ValueError(f"gradient map {j}: its rows do not match system {j}")
+        e = g.nnz
+        rps.append(g.rowptr[:-1] + nz)
+        trps.append(g.t_rowptr[:-1] + nz)
+        cols.append(g.col[:e] + c0)
+        vals.append(g.val[:e])
+        trows.append(g.t_row[:e] + int(rows[j]))
+        tvals.append(g.t_val[:e])
+        nz += e
+        c0 += g.n_cols
+    dev = gradients[0].rowptr.device
+    end = torch.tensor([nz], dtype=torch.int64, device=dev)
+    return GradientMap(c0, torch.cat(rps + [end]), torch.cat(cols).to(torch.int32), torch.cat(vals),
+                       torch.cat(trps + [end]), torch.cat(trows).to(torch.int32), torch.cat(tvals))
+
+
+def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_fail=True, check_every=50,
+                       gradients=None):
     """Several independent systems in one double-float COCG (pg_cocg_segments).
 
     systems: [(rowptr int64 [n_j+1], col int32, vals complex128, b complex128
@@ -741,8 +767,10 @@ def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_
     system keeps its own scalars and convergence test (true residual <= rtol
     ||b_j|| per column); every kernel launch and graph replay serves all of
     them.  blocks: None (diagonal Jacobi) or (p, [(n_edges, n_faces,
-    n_elements) per system]) for entity block-Jacobi.  Returns ([x_j], info)
-    with info.relres_per_rhs and info.its_per_rhs per (system, rhs)."""
+    n_elements) per system]) for entity block-Jacobi.  gradients: None or
+    one GradientMap per system (DeviceMesh.gradient_map) for the gradient
+    correction (diagonal scaling).  Returns ([x_j], info) with
+    info.relres_per_rhs and info.its_per_rhs per (system, rhs)."""
     if not systems:
         raise ValueError("no systems")
     for j, (rp, c, v, bj) in enumerate(systems):
@@ -764,6 +792,12 @@ def solve_csr_segments(systems, blocks=None, rtol=1e-8, max_it=100000, raise_on_
     if blocks is not None:
         o.block_p = int(blocks[0])
         ents = np.ascontiguousarray(np.asarray(blocks[1], dtype=np.int64).reshape(S, 3))
+    gmap = None
+    if gradients is not None:
+        if blocks is not None or len(gradients) != S:
+            raise ValueError("gradients: one map per system, with diagonal scaling (blocks=None)")
+        gmap = concat_gradients(gradients, rows)
+        _set_gradient(o, gmap)
     ents_p = ctypes.c_void_p(ents.ctypes.data) if ents is not None else ctypes.c_void_p(0)
     rows_p = ctypes.c_void_p(rows.ctypes.data)
     nbytes = _lib.query("pg_cocg_segments_workspace_bytes", N, nnz, k, rows_p, S, ents_p, ctypes.byref(o))

@@ -37,14 +37,16 @@ def _true_relres(m, A, x, b):
     return (torch.linalg.norm(r, dim=0) / torch.linalg.norm(b, dim=0)).tolist()
 
 
-@pytest.mark.parametrize("k,precond", [(1, "jacobi"), (1, "block"), (4, "block")])
+@pytest.mark.parametrize("k,precond", [(1, "jacobi"), (1, "block"), (4, "block"), (1, "grad"), (4, "grad")])
 def test_segments_match_separate_solves(k, precond):
     from petgem_gb300.engine import solve_csr_segments
     sizes = [5, 3, 4]
     systems = [_system(n, seed=j + 1, k=k) for j, n in enumerate(sizes)]
     rtol = 1e-10
     blocks = (2, [(m.nE, m.nF, m.T) for m, _, _ in systems]) if precond == "block" else None
-    xs, info = solve_csr_segments([(m.rowptr, m.col, A, b) for m, A, b in systems], blocks=blocks, rtol=rtol)
+    grads = [m.gradient_map() for m, _, _ in systems] if precond == "grad" else None
+    xs, info = solve_csr_segments([(m.rowptr, m.col, A, b) for m, A, b in systems], blocks=blocks, rtol=rtol,
+                                  gradients=grads)
     assert info.status == 0
     assert len(info.relres_per_rhs) == len(sizes) and all(len(r) == k for r in info.relres_per_rhs)
     for j, (m, A, b) in enumerate(systems):
