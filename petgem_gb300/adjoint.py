@@ -30,7 +30,8 @@ class ReceiverMisfit:
     d_obs: complex [R, 3] observed E at the receivers (rows of receivers that
     fall outside the mesh are ignored, as petgem drops such receivers)."""
 
-    def __init__(self, mesh, source, receivers, d_obs, rtol=1e-10, ksp="cocg", precision="fp64", max_it=100000):
+    def __init__(self, mesh, source, receivers, d_obs, rtol=1e-10, ksp="cocg", precision="fp64", max_it=100000,
+                 precond="block"):
         self.mesh = mesh
         self.source = dict(source)
         self.freq = float(source["frequency"])
@@ -41,7 +42,7 @@ class ReceiverMisfit:
         self.src_elem = mesh.locate_source(self.source)
         if int(self.src_elem.item()) < 0:
             raise ValueError("source outside the mesh")
-        self.opts = dict(rtol=rtol, ksp=ksp, precision=precision, max_it=max_it)
+        self.opts = dict(rtol=rtol, ksp=ksp, precision=precision, max_it=max_it, precond=precond)
         self.last_info = []
 
     def _sigma(self, m):
