@@ -596,6 +596,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     xg, rgr = timed("cocg", "fp64", b, args.max_it, precond="grad")
     Xgb, rgb = timed("cocg", "fp64", B.contiguous(), args.max_it, precond="grad")
     xgm, rgm = timed("gmres", "fp64", b, args.max_it, precond="grad")
+    xgmm, rgmm = timed("gmres", "mixed", b, args.max_it, precond="grad")
     xgd, rgd = timed("cocg", "df64", b, args.max_it, precond="grad")
     Xgdb, rgdb = timed("cocg", "df64", B.contiguous(), args.max_it, precond="grad")
     xdf, rdf = timed("cocg", "df64", b, args.max_it)
@@ -660,7 +661,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     for x, r in ((x64, r64), (xdf, rdf), (xmx, rmx), (Xdb[:, 0].contiguous(), rdb), (Xf[:, j1].contiguous(), rmf),
                  (xir, rir), (None if Xib is None else Xib[:, 0].contiguous(), rib), (xg, rgr),
                  (Xgb[:, 0].contiguous(), rgb), (xgm, rgm), (xgd, rgd), (Xgdb[:, 0].contiguous(), rgdb),
-                 (Xfg[:, j1].contiguous(), rmfg), (xgi, rgi),
+                 (Xfg[:, j1].contiguous(), rmfg), (xgi, rgi), (xgmm, rgmm),
                  (None if Xgib is None else Xgib[:, 0].contiguous(), rgib)):
         if x is None:
             continue
@@ -671,6 +672,7 @@ def run_solves(args, torch, mesh, model, vals, b):
     out["fp64_grad"] = rgr
     out["fp64_grad_batched"] = rgb
     out["gmres30_fp64_grad"] = rgm
+    out["gmres30_mixed_grad"] = rgmm
     out["df64_grad"] = rgd
     out["ir32_grad"] = rgi
     out["ir32_grad_batched"] = rgib
