@@ -173,22 +173,32 @@ __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restr
   const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
   const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
   float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
-    const int64_t row = e / K;
-    const int rhs = (int)(e % K);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
+  // two items per step (e and e + kThreads), so each thread has two
+  // independent load chains in flight; the items are summed into rho in
+  // increasing e, as a one-item loop would
+  auto finish = [&](int64_t e, float2 acc, float4& re, float4& ze) {
+    const float2 cr = cmul(Sinv[PC ? e : e / K], acc);
+    re = r[e];
+    ze = re;
+    df_add(ze.x, ze.y, cr.x, 0.f);
+    df_add(ze.z, ze.w, cr.y, 0.f);
+    ze = df_norm(ze);
+  };
+  auto gsum = [&](int64_t j, int64_t end, int rhs, float2& acc) {
+    if (j < end) {
       const float g = __double2float_rn(gv[j]);
       const float2 v = t[(int64_t)gc[j] * K + rhs];
       acc.x = fmaf(g, v.x, acc.x);
       acc.y = fmaf(g, v.y, acc.y);
     }
-    const float2 cr = cmul(Sinv[PC ? e : row], acc);
-    const float4 re = r[e];
-    float4 ze = re;
-    df_add(ze.x, ze.y, cr.x, 0.f);
-    df_add(ze.z, ze.w, cr.y, 0.f);
-    ze = df_norm(ze);
+  };
+  auto item = [&](int64_t e, float4& re, float4& ze) {
+    const int64_t row = e / K;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) gsum(j, gp[row + 1], (int)(e % K), acc);
+    finish(e, acc, re, ze);
+  };
+  auto store = [&](int64_t e, float4 ze) {
     z[e] = ze;
     if (set_p) {
       pv[e] = ze;
@@ -198,7 +208,31 @@ __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restr
         ps[e] = df_norm(w);
       }
     }
-    cdf_mac(rho, re, ze);
+  };
+  int64_t e = lo + threadIdx.x;
+  for (; e + kThreads < hi; e += 2 * kThreads) {
+    // both rows' entries in one loop: two gather chains per step
+    const int64_t eb = e + kThreads, rowa = e / K, rowb = eb / K;
+    const int64_t ja0 = gp[rowa], jae = gp[rowa + 1], jb0 = gp[rowb], jbe = gp[rowb + 1];
+    const int64_t steps = max(jae - ja0, jbe - jb0);
+    float2 acca = make_float2(0.f, 0.f), accb = make_float2(0.f, 0.f);
+    for (int64_t s = 0; s < steps; ++s) {
+      gsum(ja0 + s, jae, (int)(e % K), acca);
+      gsum(jb0 + s, jbe, (int)(eb % K), accb);
+    }
+    float4 ra, za, rb, zb;
+    finish(e, acca, ra, za);
+    finish(eb, accb, rb, zb);
+    store(e, za);
+    store(e + kThreads, zb);
+    cdf_mac(rho, ra, za);
+    cdf_mac(rho, rb, zb);
+  }
+  if (e < hi) {
+    float4 ra, za;
+    item(e, ra, za);
+    store(e, za);
+    cdf_mac(rho, ra, za);
   }
   block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   if (!start && arrive_last(&ctl->counter)) {
