@@ -52,3 +52,26 @@ def test_concat_gradients_rejects_mismatched_rows():
     _, b = _map(12, 5, 0.3, 2)
     with pytest.raises(ValueError):
         concat_gradients([a, b], np.array([0, 10, 21]))
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_gradient_map_sizes_match_oracle(p):
+    """pg_gradient_map_sizes (host-only C-ABI query): the column count of the
+    oracle's map and an upper bound of its stored entries; orders outside
+    1..3 are rejected."""
+    import ctypes
+    from oracle import gradient, system
+    from petgem_gb300 import _lib, synthetic
+    nodes, tets = synthetic.kuhn_box(3)
+    mm = system.mesh_maps(nodes, tets, p)
+    nE, nF = int(mm["elemsE"].max()) + 1, int(mm["elemsF"].max()) + 1
+    G, _ = gradient.gradient_map(tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"],
+                                 len(nodes), p)
+    nc, me = ctypes.c_int64(), ctypes.c_int64()
+    lib = _lib.load()
+    assert lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), p, ctypes.byref(nc), ctypes.byref(me)) == 0
+    assert nc.value == G.shape[1]
+    assert G.nnz <= me.value
+    assert lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), 4, ctypes.byref(nc), ctypes.byref(me)) == -1
+    assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, p) > 0
+    assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, 0) == 0
