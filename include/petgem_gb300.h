@@ -511,8 +511,9 @@ typedef struct pg_cocg_opts {
   int block_p;
   int64_t block_edges, block_faces, block_volumes;
   /* precision 3: relative residual reduction each complex64 inner solve aims
-   * for (0 or outside (0, 1): 1e-2); an inner solve stops after at most 8x the
-   * inner iterations of the first refinement step (at least 1,000) */
+   * for (0 or outside (0, 1), the default: 1e-2, or 1e-4 with the gradient
+   * correction); an inner solve stops after at most 8x the inner iterations
+   * of the first refinement step (at least 1,000) */
   double inner_rtol;
   /* gradient correction (pg_cocg: precision 0, 2 or 3; pg_gmres: 0 or 1;
    * diagonal Jacobi, block_p 0; grad_rowptr NULL = off): G, n rows by grad_cols columns, and

@@ -648,7 +648,7 @@ extern "C" void pg_cocg_default_opts(pg_cocg_opts* o) {
   o->rtol = 1e-8;
   o->precision = 0;
   o->check_every = 50;
-  o->inner_rtol = 1e-2;
+  o->inner_rtol = 0.0;   // the solver's default: 1e-2, or 1e-4 with the gradient correction
 }
 
 extern "C" size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts) {

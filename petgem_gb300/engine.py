@@ -376,7 +376,7 @@ class DeviceMesh:
         return vals, b
 
     def solve(self, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True, ksp="gmres", check_every=50, precond="block", inner_rtol=1e-2, pec=True):
+              raise_on_fail=True, ksp="gmres", check_every=50, precond="block", inner_rtol=None, pec=True):
         """Solve A x = b for this mesh's CSR pattern (see solve_csr).
         precond="block": entity block-Jacobi (each edge / face / volume's
         diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal;
@@ -607,7 +607,7 @@ def _new_x(name, b, x0):
 
 
 def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000, precision="fp64", reorth=False,
-              raise_on_fail=True, ksp="gmres", check_every=50, blocks=None, inner_rtol=1e-2, gradient=None):
+              raise_on_fail=True, ksp="gmres", check_every=50, blocks=None, inner_rtol=None, gradient=None):
     """Solve A x = b for a CSR matrix on the GPU (rowptr int64 [N+1], col
     int32 [nnz], vals complex128 [nnz]); b complex128 [N] or [N, k]
     (k in 1,2,4,8,16,32).  The KSPSolve of petgem/solver.py:584-594.
@@ -619,7 +619,8 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     refinement), "df64" (COCG only: double-float arithmetic on the FP32 pipes, FP64-class accuracy)
     or "ir32" (COCG only: FP64 iterative refinement of the true residual around complex64 inner
     solves, each restarted from the FP64 residual and run until its residual has dropped by
-    inner_rtol; max_it counts inner iterations, info.restarts the refinement steps).
+    inner_rtol, default 1e-2, or 1e-4 with the gradient correction; max_it counts inner iterations,
+    info.restarts the refinement steps).
     Convergence: true residual ||b - A x|| <= rtol ||b|| in FP64.
     blocks=(p, n_edges, n_faces, n_elements): entity block-Jacobi on a pattern
     built by DeviceMesh (rows of one entity share their columns): COCG runs on
@@ -660,7 +661,8 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
         o = _lib.CocgOpts()
         lib.pg_cocg_default_opts(ctypes.byref(o))
         o.max_it, o.rtol, o.precision, o.check_every = int(max_it), float(rtol), prec, int(check_every)
-        o.inner_rtol = float(inner_rtol)
+        if inner_rtol is not None:
+            o.inner_rtol = float(inner_rtol)   # else the solver's default (1e-2; 1e-4 with gradient)
         if blocks is not None:
             o.block_p, o.block_edges, o.block_faces, o.block_volumes = (int(v) for v in blocks)
         if gradient is not None:
