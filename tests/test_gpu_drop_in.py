@@ -61,8 +61,14 @@ def test_single_element_hvfem_functions():
         assert a.tolist() == eo[e].tolist() and b.tolist() == fo[e].tolist()
 
 
+# petgem options files may name hypre's AMS; it runs as Jacobi plus the
+# discrete-gradient correction
+PC_OPTS = {"default": [], "hypre": ["-pc_type", "hypre", "-pc_hypre_type", "ams"]}
+
+
+@pytest.mark.parametrize("pc", ["default", "hypre"])
 @pytest.mark.parametrize("p", [1, 2])
-def test_params_pipeline_vs_oracle(tmp_path, p):
+def test_params_pipeline_vs_oracle(tmp_path, p, pc):
     from petgem_gb300 import gmsh
     from petgem_gb300.pipeline import run_kernel
     pts, tets, phys = load_test_mesh()
@@ -94,7 +100,8 @@ output:
   directory: {tmp_path / 'out'}
   directory_scratch: {tmp_path / 'tmp'}
 """)
-    setup, solver, post = run_kernel(str(params), ["-ksp_type", "cocg", "-ksp_rtol", "1e-11", "-ksp_max_it", "100000"])
+    setup, solver, post = run_kernel(str(params), ["-ksp_type", "cocg", "-ksp_rtol", "1e-11", "-ksp_max_it", "100000"]
+                                     + PC_OPTS[pc])
     assert solver.info[0].relres <= 1e-11
     # oracle: assembly, PEC, direct solve, fields
     eE, eN = topology.compute_edges(tets)
@@ -146,7 +153,8 @@ def test_petgem_petsc_test_system_solved_by_gpu_gmres():
     assert np.linalg.norm(xg - xd) <= 1e-6 * np.linalg.norm(xd)
 
 
-def test_params_pipeline_mt_vs_oracle(tmp_path):
+@pytest.mark.parametrize("pc", ["default", "hypre"])
+def test_params_pipeline_mt_vs_oracle(tmp_path, pc):
     """MT mode through the params file: boundary excitation for both
     polarisations, one batched solve, receiver fields and impedances against
     the oracle (petgem's formulation restated, direct solve).  The 1e6-node
@@ -184,7 +192,8 @@ output:
   directory: {tmp_path / 'out'}
   directory_scratch: {tmp_path / 'tmp'}
 """)
-    setup, solver, post = run_kernel(str(params), ["-ksp_type", "cocg", "-ksp_rtol", "1e-11", "-ksp_max_it", "100000"])
+    setup, solver, post = run_kernel(str(params), ["-ksp_type", "cocg", "-ksp_rtol", "1e-11", "-ksp_max_it", "100000"]
+                                     + PC_OPTS[pc])
     assert all(i.status == 0 for i in solver.info)
     from petgem_gb300 import vtk
     _, _, vfields = vtk.read(post.vtk_file)
