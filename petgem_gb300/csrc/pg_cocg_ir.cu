@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(kThreads) k_ir_update(float2* __restrict__ y, 
                                                         const float* __restrict__ wd, int64_t n, CgState* st,
                                                         double2* prho, double2* pw, CgCtl* ctl,
                                                         float2* __restrict__ u = nullptr,
-                                                        const float2* __restrict__ Sinv = nullptr) {
+                                                        const float2* __restrict__ Sinv = nullptr,
+                                                        double spike = 1e30) {
   if (!ctl->any_active) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ float2 al[kMaxK];
@@ -258,9 +259,11 @@ __global__ void __launch_bounds__(kThreads) k_ir_update(float2* __restrict__ y, 
   }
   if constexpr (!GRAD) block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   block_reduce_c32<K>(make_float2(ww, 0.f), smf, pw + (int64_t)blockIdx.x * K);
-  // no early end on residual spikes: an inner solve only needs a 100x drop,
-  // far above what a spike costs an FP32 recurrence (eps32 x the spike)
-  if (arrive_last(&ctl->counter)) cg_beta_final<K, GRAD>(prho, pw, gridDim.x, st, ctl, 0, 0.0, smem, 1e30);
+  // no early end on ordinary residual spikes: an inner solve only needs a
+  // 100x drop, far above what a spike costs an FP32 recurrence (eps32 x the
+  // spike); with the gradient correction an estimate 1e8x its start means the
+  // inner solve diverges, and the refinement step ends there
+  if (arrive_last(&ctl->counter)) cg_beta_final<K, GRAD>(prho, pw, gridDim.x, st, ctl, 0, 0.0, smem, spike);
 }
 
 // Gradient correction in the complex64 inner solve (diagonal scaling):
@@ -630,7 +633,7 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       PG_KSWITCH(k, (launch_ir_spmm<K>(variant, spmv_grid, ss, rowptr, col, At, P.n, pv, q, part, st, ctl)));
     if (grad) {
       PG_KSWITCH(k, (k_ir_update<K, true><<<nbu, kThreads, 0, ss>>>(y, r, pv, q, wdf, P.n, st, part, part2, ctl, gu,
-                                                                    gSinv),
+                                                                    gSinv, 1e8),
                      k_grad_restrict32<K><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                                         ginvD, gu, P.gn, gt, ctl, 0),
                      k_irg_prolong<K><<<nbu, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, gSinv, gt,
@@ -688,11 +691,15 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
     PG_LAUNCH_CHECK();
     PG_CUDA_TRY(cudaMemcpyAsync(rn.data(), rnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
     PG_CUDA_TRY(cudaStreamSynchronize(s));
-    bool all = true, progress = false;
+    bool all = true, progress = false, diverged = false;
     for (int i = 0; i < k; ++i) {
       if (monitor)
         fprintf(stderr, "pg_cocg(ir32): refinement %lld inner its %lld rhs %d true ||r||/||b|| = %.6e\n",
                 (long long)outer, (long long)its, i, bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0);
+      // a refinement step that raised the residual 100x: the complex64 inner
+      // solves diverge (e.g. a nearly non-conducting region whose gradient
+      // correction spans more dynamic range than FP32 carries)
+      if (!first && rn[i] > 1e2 * best[i]) diverged = true;
       if (!isfinite(rn[i])) {
         pg_set_error("pg_cocg: non-finite residual");
         status = PG_ERR_NONFINITE;
@@ -713,6 +720,12 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       if (rn[i] < best[i]) best[i] = rn[i];
     }
     if (status || all) break;
+    if (diverged) {
+      pg_set_error("pg_cocg(ir32): a refinement step raised the true residual 100x (complex64 inner solves diverge; "
+                   "use precision 0 or 2 for this system)");
+      status = PG_ERR_BREAKDOWN;
+      break;
+    }
     if (its >= max_it) {
       status = PG_ERR_NOT_CONVERGED;
       break;

@@ -387,6 +387,11 @@ class DeviceMesh:
         MT, which want fp64: their true residual has an FP64 floor)."""
         if precond not in ("block", "jacobi", "grad"):
             raise ValueError(f"unknown preconditioner {precond!r} (block, jacobi, grad)")
+        if precond == "grad" and not pec and precision != "fp64":
+            # without PEC rows the air's gradient components make the true
+            # residual noisy at the FP64 floor; only the FP64 recurrence, which
+            # never restarts from it, stays stable there
+            raise ValueError("precond='grad' with pec=False (MT systems) runs in precision='fp64'")
         blocks = (self.p, self.nE, self.nF, self.T) if precond == "block" else None
         gradient = self.gradient_map(pec) if precond == "grad" else None
         return solve_csr(self.rowptr, self.col, vals, b, x0=x0, rtol=rtol, restart=restart, max_it=max_it,
