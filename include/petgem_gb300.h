@@ -547,16 +547,20 @@ typedef struct pg_cocg_opts {
  * f64; the entry arrays hold at most max_entries (pg_gradient_map_sizes) and
  * g_rowptr[n] = gt_rowptr[n_cols] entries are stored.  Deterministic;
  * synchronises (PG_ERR_UNSUPPORTED if a coefficient falls outside its row's
- * entity structure, i.e. the basis and the map disagree). */
-int pg_gradient_map_sizes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems, int p,
+ * entity structure, i.e. the basis and the map disagree).  vector_p1 != 0
+ * (p 2..3; nodes f64 [n_nodes * 3] needed) appends the vector P1 fields
+ * lambda_v e_d, 3 columns per vertex (column n_grad + 3 v + d): the
+ * auxiliary space of the vector-nodal correction, whose Jacobi step the
+ * solvers apply together with the gradient's. */
+int pg_gradient_map_sizes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems, int p, int vector_p1,
                           int64_t* n_cols /* host */, int64_t* max_entries /* host */);
 size_t pg_gradient_map_workspace_bytes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems,
-                                       int64_t n_tuples, int p);
-int pg_gradient_map(const int32_t* elemsN, const int32_t* elemsE, const int32_t* elemsF, const int32_t* dofs,
-                    const int32_t* tuple_of_elem, const int32_t* codes, int64_t n_tuples, int64_t n_elems,
-                    int64_t n_nodes, int64_t n_edges, int64_t n_faces, int p, const uint8_t* pec_flags,
-                    int64_t* g_rowptr, int32_t* g_col, double* g_val, int64_t* gt_rowptr, int32_t* gt_row,
-                    double* gt_val, void* workspace, size_t workspace_bytes, void* stream);
+                                       int64_t n_tuples, int p, int vector_p1);
+int pg_gradient_map(const double* nodes, const int32_t* elemsN, const int32_t* elemsE, const int32_t* elemsF,
+                    const int32_t* dofs, const int32_t* tuple_of_elem, const int32_t* codes, int64_t n_tuples,
+                    int64_t n_elems, int64_t n_nodes, int64_t n_edges, int64_t n_faces, int p, int vector_p1,
+                    const uint8_t* pec_flags, int64_t* g_rowptr, int32_t* g_col, double* g_val, int64_t* gt_rowptr,
+                    int32_t* gt_row, double* gt_val, void* workspace, size_t workspace_bytes, void* stream);
 
 void pg_cocg_default_opts(pg_cocg_opts* opts);
 size_t pg_cocg_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts);

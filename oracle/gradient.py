@@ -14,8 +14,12 @@ petgem/hvfem.py:223-316 for K).
 Column order: mesh vertices; then (p >= 2) lambda_a lambda_b per edge; then
 (p = 3) lambda_a lambda_b (lambda_b - lambda_a) per edge, (a, b) oriented by
 the element's edge flag like petgem's edge functions (hvfem.py:881-951), and
-lambda_a lambda_b lambda_c per face.  A row is taken from the lowest-index
-element that holds its DOF.  Columns with an entry in a PEC row are dropped.
+lambda_a lambda_b lambda_c per face.  With vector=True (p >= 2) the vector P1
+fields lambda_v e_d follow, 3 columns per vertex: they are also exactly
+representable for p >= 2, by the reference projection of lambda_v e_k
+combined with the element's Jacobian (covariant pull-back).  A row is taken
+from the lowest-index element that holds its DOF.  Columns with an entry in a
+PEC row are dropped.
 """
 import functools
 
@@ -70,9 +74,31 @@ def local_coefficients(p, eo, fo):
     return C, res
 
 
-def gradient_map(tets, elemsE, elemsF, eo, fo, dofs, n_dofs, n_nodes, p, pec=None):
+@functools.lru_cache(maxsize=4096)
+def local_vector_coefficients(p, eo, fo):
+    """C (nd, 12): lambda_v e_k = sum_i C[i, 3 v + k] N_i on the reference
+    element (p >= 2), cut like local_coefficients; and the largest residual."""
+    pts, wts = basis.tet_rule(2 * p + 2)
+    N, _ = basis.shape3d(pts, p, eo, fo)
+    x, y, z = pts[:, 0], pts[:, 1], pts[:, 2]
+    lam = (1.0 - x - y - z, x, y, z)
+    F = np.zeros((3, 12, len(wts)))
+    for v in range(4):
+        for k in range(3):
+            F[k, 3 * v + k] = lam[v]
+    M = np.einsum("dip,djp,p->ij", N, N, wts)
+    R = np.einsum("dip,dqp,p->iq", N, F, wts)
+    C = np.linalg.solve(M, R)
+    res = float(np.abs(np.einsum("dip,iq->dqp", N, C) - F).max())
+    mx = np.abs(C).max(axis=0, keepdims=True)
+    C = np.where(np.abs(C) <= 1e-8 * mx, 0.0, C)
+    return C, res
+
+
+def gradient_map(tets, elemsE, elemsF, eo, fo, dofs, n_dofs, n_nodes, p, pec=None, vector=False, nodes=None):
     """G as scipy CSR (n_dofs x n_cols, float64) and the largest local
-    representation residual over the orientation tuples used."""
+    representation residual over the orientation tuples used.  vector=True
+    (p >= 2, nodes given) appends the vector P1 columns."""
     tets = np.asarray(tets, dtype=np.int64)
     elemsE = np.asarray(elemsE, dtype=np.int64)
     elemsF = np.asarray(elemsF, dtype=np.int64)
@@ -107,6 +133,23 @@ def gradient_map(tets, elemsE, elemsF, eo, fo, dofs, n_dofs, n_nodes, p, pec=Non
     r = np.repeat(rows, W)
     c = cols.reshape(-1)
     v = vals.reshape(-1)
+    if vector:
+        if p < 2 or nodes is None:
+            raise ValueError("vector columns need p >= 2 and the nodes")
+        tv = np.empty((len(uniq), nd, 12))
+        for k, u in uniq.items():
+            Cv, res = local_vector_coefficients(p, k[:6], k[6:])
+            tv[u] = Cv
+            worst = max(worst, res)
+        X = np.asarray(nodes, dtype=np.float64)[tets[el]]            # (n_rows, 4, 3)
+        J = np.transpose(X[:, 1:, :] - X[:, :1, :], (0, 2, 1))       # J[d, k] = x_{k+1,d} - x_{0,d}
+        cref = tv[tuple_of[el], i, :].reshape(-1, 4, 3)               # (n_rows, v, k)
+        cphys = np.einsum("rvk,rdk->rvd", cref, J).reshape(-1, 12)    # (n_rows, 3 v + d)
+        vcols = n_cols + 3 * np.repeat(tets[el], 3, axis=1) + np.tile(np.arange(3), 4)[None, :]
+        r = np.concatenate([r, np.repeat(rows, 12)])
+        c = np.concatenate([c, vcols.reshape(-1)])
+        v = np.concatenate([v, cphys.reshape(-1)])
+        n_cols += 3 * n_nodes
     keep = v != 0.0
     G = sp.csr_matrix((v[keep], (r[keep], c[keep])), shape=(n_dofs, n_cols))
     if pec is not None and len(pec):

@@ -114,10 +114,10 @@ SIGNATURES = {
     "pg_gmres_default_opts": (None, [_PO]),
     "pg_gmres_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PO]),
     "pg_gmres": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PO, _PR, _P, _P, _SZ, _P]),
-    "pg_gradient_map_sizes": (_INT, [_I64, _I64, _I64, _I64, _INT, _P, _P]),
-    "pg_gradient_map_workspace_bytes": (_SZ, [_I64, _I64, _I64, _I64, _I64, _INT]),
-    "pg_gradient_map": (_INT, [_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64, _INT, _P, _P, _P, _P, _P, _P,
-                               _P, _P, _SZ, _P]),
+    "pg_gradient_map_sizes": (_INT, [_I64, _I64, _I64, _I64, _INT, _INT, _P, _P]),
+    "pg_gradient_map_workspace_bytes": (_SZ, [_I64, _I64, _I64, _I64, _I64, _INT, _INT]),
+    "pg_gradient_map": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64, _INT, _INT, _P, _P, _P, _P,
+                               _P, _P, _P, _P, _SZ, _P]),
     "pg_cocg_default_opts": (None, [_PC]),
     "pg_cocg_workspace_bytes": (_SZ, [_I64, _I64, _INT, _PC]),
     "pg_cocg": (_INT, [_P, _P, _P, _I64, _I64, _P, _P, _INT, _PC, _PR, _P, _P, _SZ, _P]),

@@ -20,6 +20,15 @@
 // Global columns: the mesh's vertices, then one column per edge (p >= 2),
 // then (p = 3) a second column per edge and one per face.
 //
+// With vector_p1 (p >= 2) the map also carries the vector P1 fields
+// lambda_v e_d (3 columns per vertex, after the gradient columns): the
+// auxiliary space of the vector-nodal correction, whose Jacobi step
+// (diag(Pi^T A Pi)) adds to the gradient's in the same B.  They lie in the
+// order-p Nedelec space for p >= 2 as well; in reference coordinates the
+// field of physical direction d is sum_k J[d][k] lambda_v e_k (covariant
+// pull-back), so the reference projection of lambda_v e_k (12 more local
+// functions per tuple) is combined with the owner element's Jacobian.
+//
 // grad(phi) lies in the order-p first-kind Nedelec space, so its local
 // coefficients are the exact L2 projection M^-1 (N, grad phi) on the reference
 // element, and under the covariant map they hold on every element with the
@@ -42,8 +51,13 @@ constexpr int kGradThreads = 128;
 constexpr int kGradChunk = 16;
 
 __host__ __device__ inline int grad_w(int p) { return p == 1 ? 4 : (p == 2 ? 10 : 20); }
-__host__ __device__ inline int grad_edge_len(int p) { return p + 1; }
-__host__ __device__ inline int grad_face_len(int p) { return p == 1 ? 0 : 3 + 3 * (p - 1) + (p == 3 ? 1 : 0); }
+// local functions of the tables: the gradients, then (vector) 12 lambda_v e_k
+__host__ __device__ inline int grad_wt(int p, int vec) { return grad_w(p) + (vec ? 12 : 0); }
+__host__ __device__ inline int grad_edge_len(int p, int vec = 0) { return p + 1 + (vec ? 6 : 0); }
+__host__ __device__ inline int grad_face_len(int p, int vec = 0) {
+  return p == 1 ? 0 : 3 + 3 * (p - 1) + (p == 3 ? 1 : 0) + (vec ? 9 : 0);
+}
+__host__ __device__ inline int grad_vol_len(int p, int vec = 0) { return grad_w(p) + (vec ? 12 : 0); }
 
 // the 3 local edges of each local face (edges as pg_basis orders them)
 __device__ __constant__ int PG_FACE_EDGES[4][3] = {{0, 1, 2}, {0, 3, 4}, {1, 4, 5}, {2, 3, 5}};
@@ -86,15 +100,27 @@ __device__ inline void h1_grad(int q, const double lam[4], const int eo[6], doub
   }
 }
 
-// One CTA per orientation tuple: M = (N_i, N_j) and R = (N_i, grad phi_q) on
-// the reference element (collapsed Gauss-Legendre rule, p+2 points per
-// direction, exact for the degree-2p integrands), then M C = R by Cholesky.
-// out[u][i * W + q] = C[i][q]; entries at or below 1e-8 of their column's
-// largest are set to 0: for p <= 3 the coefficients are either >= 0.1 or
-// rounding below 1e-11 (an exact zero), so the cut is platform-independent.
-__global__ void __launch_bounds__(kGradThreads) k_grad_tables(const int32_t* codes, int p, double* out) {
+// local function q of the tables: the gradient of H1 function q (q < Wg),
+// else lambda_v e_k with v = (q - Wg) / 3, k = (q - Wg) % 3
+__device__ inline void aux_fn(int q, int Wg, const double lam[4], const int eo[6], double g[3]) {
+  if (q < Wg) {
+    h1_grad(q, lam, eo, g);
+    return;
+  }
+  const int v = (q - Wg) / 3, k = (q - Wg) % 3;
+  for (int d = 0; d < 3; ++d) g[d] = d == k ? lam[v] : 0.0;
+}
+
+// One CTA per orientation tuple: M = (N_i, N_j) and R = (N_i, f_q) on the
+// reference element for the local functions f_q of aux_fn (collapsed
+// Gauss-Legendre rule, p+2 points per direction, exact for the degree-2p
+// integrands), then M C = R by Cholesky.  out[u][i * W + q] = C[i][q] (W =
+// grad_wt); entries at or below 1e-8 of their column's largest are set to 0:
+// for p <= 3 the coefficients are either >= 0.1 of it or rounding below
+// 1e-11, so the cut is platform-independent.
+__global__ void __launch_bounds__(kGradThreads) k_grad_tables(const int32_t* codes, int p, int vec, double* out) {
   extern __shared__ double sm[];
-  const int nd = pg_nd_elem(p), W = grad_w(p);
+  const int nd = pg_nd_elem(p), W = grad_wt(p, vec), Wg = grad_w(p);
   double* M = sm;                           // nd * nd, then R = nd * W
   double* R = M + nd * nd;
   double* Nb = R + nd * W;                  // chunk * 3 * nd
@@ -125,7 +151,7 @@ __global__ void __launch_bounds__(kGradThreads) k_grad_tables(const int32_t* cod
       const double lam[4] = {1.0 - x - y - z, x, y, z};
       for (int q = 0; q < W; ++q) {
         double gq[3];
-        h1_grad(q, lam, eo, gq);
+        aux_fn(q, Wg, lam, eo, gq);
         for (int d = 0; d < 3; ++d) Gb[(size_t)c * 3 * W + d * W + q] = gq[d];
       }
     }
@@ -191,9 +217,9 @@ __global__ void k_grad_owner(const int32_t* elemsE, const int32_t* elemsF, int64
 }
 
 // first slot of DOF row r in the structural (uncompacted) layout
-__device__ inline int64_t grad_srow(int64_t r, int64_t nE, int64_t nF, int p) {
+__device__ inline int64_t grad_srow(int64_t r, int64_t nE, int64_t nF, int p, int vec) {
   const int64_t nEr = nE * p, nFr = nF * p * (p - 1);
-  const int64_t le = grad_edge_len(p), lf = grad_face_len(p), lv = grad_w(p);
+  const int64_t le = grad_edge_len(p, vec), lf = grad_face_len(p, vec), lv = grad_vol_len(p, vec);
   if (r <= nEr) return r * le;
   if (r <= nEr + nFr) return nEr * le + (r - nEr) * lf;
   return nEr * le + nFr * lf + (r - nEr - nFr) * lv;
@@ -207,37 +233,42 @@ __device__ inline int32_t grad_gid(int q, int64_t el, const int32_t* elemsN, con
   return (int32_t)(nN + 2 * nE + elemsF[el * 4 + q - 16]);
 }
 
-// The owner element writes each DOF row's structural entries.  status bit 1:
-// a coefficient outside the row's structure was not zero (the basis and the
-// map disagree).
-__global__ void k_grad_fill(const int32_t* elemsN, const int32_t* elemsE, const int32_t* elemsF, const int32_t* dofs,
-                            const int32_t* tuple_of_elem, const double* tables, int64_t T, int64_t nN, int64_t nE,
-                            int64_t nF, int p, const int32_t* eown, const int32_t* fown, int32_t* scol, double* sval,
-                            int* status) {
-  const int nd = pg_nd_elem(p), W = grad_w(p);
+// The owner element writes each DOF row's structural entries: the gradient
+// columns, then (vec) the vector P1 columns of the entity's vertices, whose
+// physical coefficient for direction d is sum_k J[d][k] C[i][Wg + 3 v + k]
+// (J of the owner element; x = x0 + J xi).  status bit 1: a coefficient
+// outside the row's structure was not zero (the basis and the map disagree).
+__global__ void k_grad_fill(const double* nodes, const int32_t* elemsN, const int32_t* elemsE, const int32_t* elemsF,
+                            const int32_t* dofs, const int32_t* tuple_of_elem, const double* tables, int64_t T,
+                            int64_t nN, int64_t nE, int64_t nF, int p, int vec, int64_t colsG, const int32_t* eown,
+                            const int32_t* fown, int32_t* scol, double* sval, int* status) {
+  const int nd = pg_nd_elem(p), Wg = grad_w(p), W = grad_wt(p, vec);
   const int ne = 6 * p, nf = 4 * p * (p - 1);
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < T * nd;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t el = idx / nd;
     const int i = (int)(idx % nd);
-    int kind, ent, nq;
+    int kind, ent, nq, nvert;
     if (i < ne) {
       kind = 0;
       ent = i / p;
       if (eown[elemsE[el * 6 + ent]] != el) continue;
       nq = grad_edge_len(p);
+      nvert = 2;
     } else if (i < ne + nf) {
       kind = 1;
       ent = (i - ne) / (p * (p - 1));
       if (fown[elemsF[el * 4 + ent]] != el) continue;
       nq = grad_face_len(p);
+      nvert = 3;
     } else {
       kind = 2;
       ent = 0;
-      nq = W;
+      nq = Wg;
+      nvert = 4;
     }
     const double* tab = tables + (size_t)tuple_of_elem[el] * nd * W + (size_t)i * W;
-    const int64_t base = grad_srow(dofs[el * nd + i], nE, nF, p);
+    const int64_t base = grad_srow(dofs[el * nd + i], nE, nF, p, vec);
     unsigned used = 0;
     for (int s = 0; s < nq; ++s) {
       const int q = kind == 0 ? edge_q(ent, s) : (kind == 1 ? face_q(ent, s) : s);
@@ -245,28 +276,46 @@ __global__ void k_grad_fill(const int32_t* elemsN, const int32_t* elemsE, const 
       scol[base + s] = grad_gid(q, el, elemsN, elemsE, elemsF, nN, nE);
       sval[base + s] = tab[q];
     }
+    if (vec) {
+      double J[3][3];
+      const double* x0 = nodes + 3 * (int64_t)elemsN[el * 4];
+      for (int k = 0; k < 3; ++k) {
+        const double* xk = nodes + 3 * (int64_t)elemsN[el * 4 + k + 1];
+        for (int d = 0; d < 3; ++d) J[d][k] = xk[d] - x0[d];
+      }
+      for (int vl = 0; vl < nvert; ++vl) {
+        const int v = kind == 0 ? PG_EDGE_VERTS[ent][vl] : (kind == 1 ? PG_FACE_VERTS[ent][vl] : vl);
+        const double* c = tab + Wg + 3 * v;
+        for (int k = 0; k < 3; ++k) used |= 1u << (Wg + 3 * v + k);
+        for (int d = 0; d < 3; ++d) {
+          const int64_t slot = base + nq + 3 * vl + d;
+          scol[slot] = (int32_t)(colsG + 3 * (int64_t)elemsN[el * 4 + v] + d);
+          sval[slot] = J[d][0] * c[0] + J[d][1] * c[1] + J[d][2] * c[2];
+        }
+      }
+    }
     for (int q = 0; q < W; ++q)
       if (!((used >> q) & 1u) && tab[q] != 0.0) atomicOr(status, 1);
   }
 }
 
 // columns with an entry in a PEC row are dropped
-__global__ void k_grad_exclude(const uint8_t* pec, int64_t n, int64_t nE, int64_t nF, int p, const int32_t* scol,
-                               const double* sval, uint8_t* excl) {
+__global__ void k_grad_exclude(const uint8_t* pec, int64_t n, int64_t nE, int64_t nF, int p, int vec,
+                               const int32_t* scol, const double* sval, uint8_t* excl) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     if (!pec[r]) continue;
-    const int64_t lo = grad_srow(r, nE, nF, p), hi = grad_srow(r + 1, nE, nF, p);
+    const int64_t lo = grad_srow(r, nE, nF, p, vec), hi = grad_srow(r + 1, nE, nF, p, vec);
     for (int64_t k = lo; k < hi; ++k)
       if (sval[k] != 0.0) excl[scol[k]] = 1;
   }
 }
 
-__global__ void k_grad_rowcount(int64_t n, int64_t nE, int64_t nF, int p, const int32_t* scol, const double* sval,
-                                const uint8_t* excl, int64_t* cnt) {
+__global__ void k_grad_rowcount(int64_t n, int64_t nE, int64_t nF, int p, int vec, const int32_t* scol,
+                                const double* sval, const uint8_t* excl, int64_t* cnt) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r <= n; r += (int64_t)gridDim.x * blockDim.x) {
     int64_t c = 0;
     if (r < n) {
-      const int64_t lo = grad_srow(r, nE, nF, p), hi = grad_srow(r + 1, nE, nF, p);
+      const int64_t lo = grad_srow(r, nE, nF, p, vec), hi = grad_srow(r + 1, nE, nF, p, vec);
       for (int64_t k = lo; k < hi; ++k) c += (sval[k] != 0.0 && !excl[scol[k]]) ? 1 : 0;
     }
     cnt[r] = c;
@@ -274,10 +323,11 @@ __global__ void k_grad_rowcount(int64_t n, int64_t nE, int64_t nF, int p, const 
 }
 
 // compacted rows of G; column counts for the transpose
-__global__ void k_grad_compact(int64_t n, int64_t nE, int64_t nF, int p, const int32_t* scol, const double* sval,
-                               const uint8_t* excl, const int64_t* grp, int32_t* gc, double* gv, int64_t* colcnt) {
+__global__ void k_grad_compact(int64_t n, int64_t nE, int64_t nF, int p, int vec, const int32_t* scol,
+                               const double* sval, const uint8_t* excl, const int64_t* grp, int32_t* gc, double* gv,
+                               int64_t* colcnt) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t lo = grad_srow(r, nE, nF, p), hi = grad_srow(r + 1, nE, nF, p);
+    const int64_t lo = grad_srow(r, nE, nF, p, vec), hi = grad_srow(r + 1, nE, nF, p, vec);
     int64_t o = grp[r];
     for (int64_t k = lo; k < hi; ++k)
       if (sval[k] != 0.0 && !excl[scol[k]]) {
@@ -321,16 +371,18 @@ __global__ void k_grad_tsort(int64_t nc, const int64_t* gtp, int32_t* gtr, doubl
 }
 
 struct GradSizes {
-  int64_t n, cols, max_entries;
+  int64_t n, cols, cols_grad, max_entries;
   size_t tables, eown, fown, scol, sval, excl, rowcnt, colcnt, cursor, status, scan, total;
 };
 
-bool grad_sizes(int64_t nN, int64_t nE, int64_t nF, int64_t T, int64_t n_tuples, int p, GradSizes* g) {
-  if (p < 1 || p > 3 || nN < 4 || nE < 6 || nF < 4 || T < 1 || n_tuples < 1) return false;
-  const int W = grad_w(p), nd = pg_nd_elem(p);
+bool grad_sizes(int64_t nN, int64_t nE, int64_t nF, int64_t T, int64_t n_tuples, int p, int vec, GradSizes* g) {
+  if (p < 1 || p > 3 || nN < 4 || nE < 6 || nF < 4 || T < 1 || n_tuples < 1 || (vec && p < 2)) return false;
+  const int W = grad_wt(p, vec), nd = pg_nd_elem(p);
   g->n = nE * p + nF * p * (p - 1) + T * pg_nd_vol(p);
-  g->cols = nN + (p >= 2 ? nE : 0) + (p == 3 ? nE + nF : 0);
-  g->max_entries = nE * p * grad_edge_len(p) + nF * p * (p - 1) * grad_face_len(p) + T * pg_nd_vol(p) * W;
+  g->cols_grad = nN + (p >= 2 ? nE : 0) + (p == 3 ? nE + nF : 0);
+  g->cols = g->cols_grad + (vec ? 3 * nN : 0);
+  g->max_entries = nE * p * grad_edge_len(p, vec) + nF * p * (p - 1) * grad_face_len(p, vec) +
+                   T * pg_nd_vol(p) * grad_vol_len(p, vec);
   if (g->n >= (int64_t(1) << 31) || g->cols >= (int64_t(1) << 31) || T >= (int64_t(1) << 31)) return false;
   size_t o = 0;
   auto put = [&](size_t* slot, size_t bytes) { *slot = o; o += pg_align256(bytes); };
@@ -353,10 +405,10 @@ bool grad_sizes(int64_t nN, int64_t nE, int64_t nF, int64_t T, int64_t n_tuples,
 }  // namespace
 
 extern "C" int pg_gradient_map_sizes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems, int p,
-                                     int64_t* n_cols, int64_t* max_entries) {
+                                     int vector_p1, int64_t* n_cols, int64_t* max_entries) {
   GradSizes g;
-  if (!grad_sizes(n_nodes, n_edges, n_faces, n_elems, 1, p, &g)) {
-    pg_set_error("pg_gradient_map_sizes: order must be 1..3 and the mesh non-empty");
+  if (!grad_sizes(n_nodes, n_edges, n_faces, n_elems, 1, p, vector_p1, &g)) {
+    pg_set_error("pg_gradient_map_sizes: order must be 1..3 (2..3 with vector_p1) and the mesh non-empty");
     return PG_ERR_ARG;
   }
   if (n_cols) *n_cols = g.cols;
@@ -365,24 +417,27 @@ extern "C" int pg_gradient_map_sizes(int64_t n_nodes, int64_t n_edges, int64_t n
 }
 
 extern "C" size_t pg_gradient_map_workspace_bytes(int64_t n_nodes, int64_t n_edges, int64_t n_faces, int64_t n_elems,
-                                                  int64_t n_tuples, int p) {
+                                                  int64_t n_tuples, int p, int vector_p1) {
   GradSizes g;
-  if (!grad_sizes(n_nodes, n_edges, n_faces, n_elems, n_tuples, p, &g)) return 0;
+  if (!grad_sizes(n_nodes, n_edges, n_faces, n_elems, n_tuples, p, vector_p1, &g)) return 0;
   return g.total;
 }
 
-extern "C" int pg_gradient_map(const int32_t* elemsN, const int32_t* elemsE, const int32_t* elemsF,
-                               const int32_t* dofs, const int32_t* tuple_of_elem, const int32_t* codes,
-                               int64_t n_tuples, int64_t n_elems, int64_t n_nodes, int64_t n_edges, int64_t n_faces,
-                               int p, const uint8_t* pec_flags, int64_t* g_rowptr, int32_t* g_col, double* g_val,
-                               int64_t* gt_rowptr, int32_t* gt_row, double* gt_val, void* workspace,
-                               size_t workspace_bytes, void* stream) {
+extern "C" int pg_gradient_map(const double* nodes, const int32_t* elemsN, const int32_t* elemsE,
+                               const int32_t* elemsF, const int32_t* dofs, const int32_t* tuple_of_elem,
+                               const int32_t* codes, int64_t n_tuples, int64_t n_elems, int64_t n_nodes,
+                               int64_t n_edges, int64_t n_faces, int p, int vector_p1, const uint8_t* pec_flags,
+                               int64_t* g_rowptr, int32_t* g_col, double* g_val, int64_t* gt_rowptr, int32_t* gt_row,
+                               double* gt_val, void* workspace, size_t workspace_bytes, void* stream) {
   GradSizes g;
-  if (!grad_sizes(n_nodes, n_edges, n_faces, n_elems, n_tuples, p, &g) || !elemsN || !elemsE || !elemsF || !dofs ||
-      !tuple_of_elem || !codes || !g_rowptr || !g_col || !g_val || !gt_rowptr || !gt_row || !gt_val) {
-    pg_set_error("pg_gradient_map: bad argument (order 1..3, non-empty mesh, every output given)");
+  if (!grad_sizes(n_nodes, n_edges, n_faces, n_elems, n_tuples, p, vector_p1, &g) || !elemsN || !elemsE ||
+      !elemsF || !dofs || !tuple_of_elem || !codes || !g_rowptr || !g_col || !g_val || !gt_rowptr || !gt_row ||
+      !gt_val || (vector_p1 && !nodes)) {
+    pg_set_error("pg_gradient_map: bad argument (order 1..3, 2..3 with vector_p1 and nodes, non-empty mesh, every "
+                 "output given)");
     return PG_ERR_ARG;
   }
+  const int vec = vector_p1 ? 1 : 0;
   if (!workspace || workspace_bytes < g.total) {
     pg_set_error("pg_gradient_map: workspace too small");
     return PG_ERR_WORKSPACE;
@@ -402,11 +457,11 @@ extern "C" int pg_gradient_map(const int32_t* elemsN, const int32_t* elemsE, con
   void* scan_ws = ws + g.scan;
   const int64_t sn = g.n + 1 > g.cols + 1 ? g.n + 1 : g.cols + 1;
   const size_t scan_bytes = pg::scan_workspace_bytes(sn);
-  const int nd = pg_nd_elem(p), W = grad_w(p);
+  const int nd = pg_nd_elem(p), W = grad_wt(p, vec);
 
   const size_t smem = sizeof(double) * ((size_t)nd * nd + (size_t)nd * W + (size_t)kGradChunk * (6 * nd + 3 * W + 1));
   PG_CUDA_TRY(cudaFuncSetAttribute(k_grad_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_grad_tables<<<(unsigned)n_tuples, kGradThreads, smem, s>>>(codes, p, tables);
+  k_grad_tables<<<(unsigned)n_tuples, kGradThreads, smem, s>>>(codes, p, vec, tables);
   PG_CUDA_TRY(cudaMemsetAsync(eown, 0x7f, sizeof(int32_t) * n_edges, s));
   PG_CUDA_TRY(cudaMemsetAsync(fown, 0x7f, sizeof(int32_t) * n_faces, s));
   PG_CUDA_TRY(cudaMemsetAsync(scol, 0, sizeof(int32_t) * g.max_entries, s));
@@ -416,16 +471,16 @@ extern "C" int pg_gradient_map(const int32_t* elemsN, const int32_t* elemsE, con
   PG_CUDA_TRY(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * g.cols, s));
   PG_CUDA_TRY(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
   k_grad_owner<<<pg_blocks(n_elems, 256), 256, 0, s>>>(elemsE, elemsF, n_elems, eown, fown);
-  k_grad_fill<<<pg_blocks(n_elems * nd, 256), 256, 0, s>>>(elemsN, elemsE, elemsF, dofs, tuple_of_elem, tables,
-                                                          n_elems, n_nodes, n_edges, n_faces, p, eown, fown, scol,
-                                                          sval, dstatus);
+  k_grad_fill<<<pg_blocks(n_elems * nd, 256), 256, 0, s>>>(nodes, elemsN, elemsE, elemsF, dofs, tuple_of_elem, tables,
+                                                          n_elems, n_nodes, n_edges, n_faces, p, vec, g.cols_grad,
+                                                          eown, fown, scol, sval, dstatus);
   if (pec_flags)
-    k_grad_exclude<<<pg_blocks(g.n, 256), 256, 0, s>>>(pec_flags, g.n, n_edges, n_faces, p, scol, sval, excl);
-  k_grad_rowcount<<<pg_blocks(g.n + 1, 256), 256, 0, s>>>(g.n, n_edges, n_faces, p, scol, sval, excl, rowcnt);
+    k_grad_exclude<<<pg_blocks(g.n, 256), 256, 0, s>>>(pec_flags, g.n, n_edges, n_faces, p, vec, scol, sval, excl);
+  k_grad_rowcount<<<pg_blocks(g.n + 1, 256), 256, 0, s>>>(g.n, n_edges, n_faces, p, vec, scol, sval, excl, rowcnt);
   PG_LAUNCH_CHECK();
   int st = pg::scan_exclusive_i64(rowcnt, g_rowptr, g.n + 1, nullptr, scan_ws, scan_bytes, s);
   if (st) return st;
-  k_grad_compact<<<pg_blocks(g.n, 256), 256, 0, s>>>(g.n, n_edges, n_faces, p, scol, sval, excl, g_rowptr, g_col,
+  k_grad_compact<<<pg_blocks(g.n, 256), 256, 0, s>>>(g.n, n_edges, n_faces, p, vec, scol, sval, excl, g_rowptr, g_col,
                                                      g_val, colcnt);
   PG_LAUNCH_CHECK();
   st = pg::scan_exclusive_i64(colcnt, gt_rowptr, g.cols + 1, nullptr, scan_ws, scan_bytes, s);

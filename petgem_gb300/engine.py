@@ -239,18 +239,22 @@ class DeviceMesh:
             self._pec_mask = f
         return self._pec_mask
 
-    def gradient_map(self, pec=True):
-        """The mesh's discrete gradient G and its transpose (pg_gradient_map;
-        built once per variant, p <= 3): the gradient correction of
-        ``solve(precond="grad")``.  pec=True drops the columns of H1 functions
-        that touch a PEC DOF (CSEM systems, PEC applied); pec=False keeps
-        every column (MT systems, whose boundary DOFs stay unknowns)."""
+    def gradient_map(self, pec=True, vector=None):
+        """The mesh's auxiliary map (pg_gradient_map; built once per variant,
+        p <= 3): the discrete gradient G of the order-p H1 space and, with
+        vector (default: p >= 2), the vector P1 fields after it; the
+        correction of ``solve(precond="grad")`` applies a Jacobi step on every
+        column.  pec=True drops the columns that touch a PEC DOF (CSEM
+        systems, PEC applied); pec=False keeps every column (MT systems, whose
+        boundary DOFs stay unknowns)."""
+        vec = (self.p >= 2) if vector is None else bool(vector)
         cache = self.__dict__.setdefault("_grad", {})
-        if bool(pec) not in cache:
+        key = (bool(pec), vec)
+        if key not in cache:
             dev = self.device
             nc, me = ctypes.c_int64(), ctypes.c_int64()
-            _lib.call("pg_gradient_map_sizes", self.n_nodes, self.nE, self.nF, self.T, self.p, ctypes.byref(nc),
-                      ctypes.byref(me))
+            _lib.call("pg_gradient_map_sizes", self.n_nodes, self.nE, self.nF, self.T, self.p, int(vec),
+                      ctypes.byref(nc), ctypes.byref(me))
             nc, me = int(nc.value), int(me.value)
             g = GradientMap(nc, torch.empty(self.N + 1, dtype=torch.int64, device=dev),
                             torch.empty(me, dtype=torch.int32, device=dev),
@@ -259,13 +263,13 @@ class DeviceMesh:
                             torch.empty(me, dtype=torch.int32, device=dev),
                             torch.empty(me, dtype=torch.float64, device=dev))
             ws = _ws(_lib.query("pg_gradient_map_workspace_bytes", self.n_nodes, self.nE, self.nF, self.T,
-                                self.n_tuples, self.p), dev)
-            _lib.call("pg_gradient_map", _p(self.elemsN), _p(self.elemsE), _p(self.elemsF), _p(self.dofs),
-                      _p(self.tuple_of_elem), _p(self.codes), self.n_tuples, self.T, self.n_nodes, self.nE, self.nF,
-                      self.p, _p(self.pec_mask()) if pec else None, _p(g.rowptr), _p(g.col), _p(g.val),
-                      _p(g.t_rowptr), _p(g.t_row), _p(g.t_val), _p(ws), ws.numel(), _s())
-            cache[bool(pec)] = g
-        return cache[bool(pec)]
+                                self.n_tuples, self.p, int(vec)), dev)
+            _lib.call("pg_gradient_map", _p(self.nodes), _p(self.elemsN), _p(self.elemsE), _p(self.elemsF),
+                      _p(self.dofs), _p(self.tuple_of_elem), _p(self.codes), self.n_tuples, self.T, self.n_nodes,
+                      self.nE, self.nF, self.p, int(vec), _p(self.pec_mask()) if pec else None, _p(g.rowptr),
+                      _p(g.col), _p(g.val), _p(g.t_rowptr), _p(g.t_row), _p(g.t_val), _p(ws), ws.numel(), _s())
+            cache[key] = g
+        return cache[key]
 
     def records(self):
         """Assembly records (once per mesh): output / transpose position,

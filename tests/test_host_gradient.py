@@ -69,9 +69,15 @@ def test_gradient_map_sizes_match_oracle(p):
                                  len(nodes), p)
     nc, me = ctypes.c_int64(), ctypes.c_int64()
     lib = _lib.load()
-    assert lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), p, ctypes.byref(nc), ctypes.byref(me)) == 0
+    assert lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), p, 0, ctypes.byref(nc), ctypes.byref(me)) == 0
     assert nc.value == G.shape[1]
     assert G.nnz <= me.value
-    assert lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), 4, ctypes.byref(nc), ctypes.byref(me)) == -1
-    assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, p) > 0
-    assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, 0) == 0
+    assert lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), 4, 0, ctypes.byref(nc), ctypes.byref(me)) == -1
+    assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, p, 0) > 0
+    assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, 0, 0) == 0
+    # with the vector P1 columns (p >= 2): 3 more per vertex
+    vst = lib.pg_gradient_map_sizes(len(nodes), nE, nF, len(tets), p, 1, ctypes.byref(nc), ctypes.byref(me))
+    if p == 1:
+        assert vst == -1
+    else:
+        assert vst == 0 and nc.value == G.shape[1] + 3 * len(nodes)

@@ -56,3 +56,32 @@ def test_gradient_pec_columns_dropped(p):
     touched = np.unique(G0[mm["bnd"]].indices)
     assert kept.sum() == G0.shape[1] - len(touched)
     assert kept[:64].sum() == 8   # interior vertices of the 3^3 box
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_vector_p1_columns_exact_and_consistent(p):
+    """The vector P1 columns (lambda_v e_d) are exactly representable for
+    p >= 2 and every element around a DOF gives the same coefficients: the
+    map taken from the lowest-index elements equals the one taken from the
+    highest-index ones, and Pi times the nodal values of a linear vector
+    field reproduces that field's interpolation (checked by the mass-weighted
+    residual against the oracle's own elemental mass matrices)."""
+    nodes, tets = _box()
+    mm = system.mesh_maps(nodes, tets, p)
+    args = (tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"], len(nodes), p)
+    G, res = gradient.gradient_map(*args, vector=True, nodes=nodes)
+    assert res < 1e-12
+    n_grad = G.shape[1] - 3 * len(nodes)
+    # reversed element order: rows from the highest-index elements
+    rev = np.arange(len(tets))[::-1]
+    Gr, _ = gradient.gradient_map(tets[rev], mm["elemsE"][rev], mm["elemsF"][rev], mm["eo"][rev], mm["fo"][rev],
+                                  mm["dofs"][rev], mm["N"], len(nodes), p, vector=True, nodes=nodes)
+    assert abs(G - Gr).max() <= 1e-9 * abs(G).max()
+    # a constant field e_x: sum_v lambda_v = 1, so Pi applied to (1, 0, 0) at every vertex is e_x
+    ex = np.zeros(G.shape[1])
+    ex[n_grad + 0::3] = 1.0
+    u = G @ ex
+    # e_x = grad(x): the gradient columns represent it through the vertex hats' x coordinates
+    gx = np.zeros(G.shape[1])
+    gx[:len(nodes)] = nodes[:, 0]
+    assert abs(u - G @ gx).max() <= 1e-9 * abs(u).max()
