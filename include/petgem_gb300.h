@@ -575,8 +575,9 @@ int pg_cocg(const int64_t* rowptr, const int32_t* col, const double* vals, int64
  * omega_0 > 0 (col_scale: host array [nrhs]).  The matrix is read once per
  * iteration for all columns; each column has its own Jacobi scaling.  b, x
  * complex128 [n * nrhs] (RHS fastest).  The gradient correction of
- * pg_cocg_opts applies (diag(G^T A_j G) = s_j diag(G^T A0 G), since
- * G^T K G = 0); block_p is ignored.  Other arguments as pg_cocg. */
+ * pg_cocg_opts applies, with each column's own diagonal
+ * diag(G^T A_j G) = Re d + i s_j Im d, d = diag(G^T A0 G); block_p is
+ * ignored.  Other arguments as pg_cocg. */
 size_t pg_cocg_multifreq_workspace_bytes(int64_t n, int64_t nnz, int nrhs, const pg_cocg_opts* opts /* may be NULL */);
 int pg_cocg_multifreq(const int64_t* rowptr, const int32_t* col, const double* vals, int64_t n, int64_t nnz,
                       const double* b, double* x, int nrhs, const double* col_scale, const pg_cocg_opts* opts,

@@ -180,8 +180,10 @@ __global__ void k_to_f32(const double2* __restrict__ a, int64_t n, float2* __res
     out[e] = make_float2((float)a[e].x, (float)a[e].y);
 }
 
-// PC (several frequencies): column j's diag(G^T A_j G) is s_j diag(G^T A_0 G)
-// (G^T K G = 0), so t carries the column's 1 / s_j (cinv).
+// PC (several frequencies): A_j = Re A0 + i s_j Im A0 and G is real, so
+// column j's diag(G^T A_j G) is Re d + i s_j Im d with d = diag(G^T A0 G)
+// (invD holds d; cscale the s_j).  Re d vanishes on gradient columns
+// (G^T K G = 0) but not on vector P1 columns.
 template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __restrict__ gtp,
                                                            const int32_t* __restrict__ gtr,
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __r
                                                            const float2* __restrict__ invD,
                                                            const float2* __restrict__ u, int64_t gn,
                                                            float2* __restrict__ t, const CgCtl* ctl, int start,
-                                                           const float* __restrict__ cinv = nullptr) {
+                                                           const float* __restrict__ cscale = nullptr) {
   if (!start && !ctl->pending) return;
   const int64_t total = gn * K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
@@ -202,8 +204,24 @@ __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __r
       acc.x = fmaf(g, v.x, acc.x);
       acc.y = fmaf(g, v.y, acc.y);
     }
-    float2 w = cmul(invD[c], acc);
-    if (PC) w = make_float2(w.x * cinv[rhs], w.y * cinv[rhs]);
+    float2 w;
+    if (PC) {
+      // invD holds the diagonal d of G^T A0 G; column rhs divides by
+      // Re d + i s_j Im d (scaled by the larger part against underflow)
+      const float2 d = invD[c];
+      float dx = d.x, dy = cscale[rhs] * d.y;
+      const float m = fmaxf(fabsf(dx), fabsf(dy));
+      if (m > 0.f) {
+        dx /= m;
+        dy /= m;
+        const float den = m * fmaf(dx, dx, dy * dy);
+        w = make_float2(fmaf(acc.x, dx, acc.y * dy) / den, fmaf(acc.y, dx, -acc.x * dy) / den);
+      } else {
+        w = make_float2(0.f, 0.f);
+      }
+    } else {
+      w = cmul(invD[c], acc);
+    }
     t[e] = w;
   }
 }

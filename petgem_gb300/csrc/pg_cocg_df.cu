@@ -816,7 +816,7 @@ size_t df_layout(const Plan& P, size_t* off /* 28 */, bool mf) {
   put(22, P.gn ? sizeof(float2) * P.gn * P.k : 0);
   put(23, P.gn ? std::max(sizeof(float4) * P.n * P.k, sizeof(double2) * (size_t)P.gn) : 0);
   put(24, P.gn ? sizeof(float2) * P.n * P.k : 0);
-  put(25, P.gn && mf ? sizeof(float) * P.k : 0);   // 1 / s_j per column
+  put(25, P.gn && mf ? sizeof(float) * P.k : 0);   // s_j per column
   return o;
 }
 
@@ -839,7 +839,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   float2* gt = reinterpret_cast<float2*>(ws + off[22]);
   float4* gz = reinterpret_cast<float4*>(ws + off[23]);
   float2* gu = reinterpret_cast<float2*>(ws + off[24]);
-  float* gcinv = reinterpret_cast<float*>(ws + off[25]);
+  float* gscale = reinterpret_cast<float*>(ws + off[25]);
   const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
@@ -892,12 +892,15 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       double2* tmp = reinterpret_cast<double2*>(gz);   // FP64 scratch until the first z
       k_grad_sinv<<<pg_blocks(P.n * k, 256), 256, 0, s>>>(S, P.n * k, tmp);
       k_to_f32<<<pg_blocks(P.n * k, 256), 256, 0, s>>>(tmp, P.n * k, Sinv);
+      // diag(G^T A_j G) = Re d + i s_j Im d with d = diag(G^T A0 G): exact for
+      // every column (the vector P1 columns have Re d != 0); the restriction
+      // divides per column
       k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
-                                                       P.gn, tmp);
+                                                       P.gn, tmp, 1);
       k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, invD);
       std::vector<float> ci(k);
-      for (int i = 0; i < k; ++i) ci[i] = (float)(1.0 / col_scale[i]);
-      PG_CUDA_TRY(cudaMemcpyAsync(gcinv, ci.data(), sizeof(float) * k, cudaMemcpyHostToDevice, s));
+      for (int i = 0; i < k; ++i) ci[i] = (float)col_scale[i];
+      PG_CUDA_TRY(cudaMemcpyAsync(gscale, ci.data(), sizeof(float) * k, cudaMemcpyHostToDevice, s));
       PG_CUDA_TRY(cudaStreamSynchronize(s));   // ci must outlive the copy
     }
     // the host copy of the scales must outlive the asynchronous copy
@@ -972,7 +975,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                                                                           0, delta, gu, Sinv),
                      k_grad_restrict32<K, true><<<gblocks, kThreads, 0, ss>>>(o->gradt_rowptr, o->gradt_row,
                                                                            o->gradt_val, invD, gu, P.gn, gt, ctl, 0,
-                                                                           gcinv),
+                                                                           gscale),
                      k_dfg_prolong<K, true><<<nbu, kThreads, 0, ss>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv,
                                                                       gt, r, P.n, gz, pv, 0, part, st, ctl, 0),
                      k_df_pupdate<K, true><<<pg_blocks(P.n * K, kThreads), kThreads, 0, ss>>>(pv, gz, P.n, st, ctl,
@@ -1100,7 +1103,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
                      k_dfg_u_start<K><<<pg_blocks(P.n * K, 256), 256, 0, s>>>(r64, P.n, gu),
                      k_grad_restrict32<K, true><<<gblocks, kThreads, 0, s>>>(o->gradt_rowptr, o->gradt_row,
                                                                           o->gradt_val, invD, gu, P.gn, gt, ctl, 1,
-                                                                          gcinv),
+                                                                          gscale),
                      k_dfg_prolong<K, true><<<nb, kThreads, 0, s>>>(o->grad_rowptr, o->grad_col, o->grad_val, Sinv,
                                                                      gt, r, P.n, gz, pv, first ? 1 : 0, part, st, ctl,
                                                                      1, ps, Sdf)));

@@ -696,10 +696,12 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       if (monitor)
         fprintf(stderr, "pg_cocg(ir32): refinement %lld inner its %lld rhs %d true ||r||/||b|| = %.6e\n",
                 (long long)outer, (long long)its, i, bnorm[i] > 0 ? rn[i] / bnorm[i] : 0.0);
-      // a refinement step that raised the residual 100x: the complex64 inner
-      // solves diverge (e.g. a nearly non-conducting region whose gradient
-      // correction spans more dynamic range than FP32 carries)
-      if (!first && rn[i] > 1e2 * best[i]) diverged = true;
+      // with the gradient correction, a refinement step that raised the
+      // residual 100x means the complex64 inner solves diverge (e.g. a nearly
+      // non-conducting region whose correction spans more dynamic range than
+      // FP32 carries); without it a step that overshoots is recovered by the
+      // next one, and the stagnation rule below ends a solve that does not
+      if (grad && !first && rn[i] > 1e2 * best[i]) diverged = true;
       if (!isfinite(rn[i])) {
         pg_set_error("pg_cocg: non-finite residual");
         status = PG_ERR_NONFINITE;

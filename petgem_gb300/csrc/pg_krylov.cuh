@@ -258,11 +258,11 @@ bool valid_k(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || 
 
 // Gradient correction shared by COCG and GMRES: G (real, DOF rows x H1
 // columns, from pg_gradient_map) and its transpose (rows ascending).
-// invD[phi] = 1 / (G^T A G)_{phi phi} (0 for an empty or vanishing column).
-// (A G_phi)_r = sum_k A_rk G_{k phi}; G_{k phi} is looked up by binary search
-// in the transpose row of phi.
+// invD[phi] = 1 / (G^T A G)_{phi phi} (0 for an empty or vanishing column;
+// raw != 0 stores the diagonal itself).  (A G_phi)_r = sum_k A_rk G_{k phi};
+// G_{k phi} is looked up by binary search in the transpose row of phi.
 __global__ void k_grad_diag(const int64_t* rowptr, const int32_t* col, const double2* A, const int64_t* gtp,
-                            const int32_t* gtr, const double* gtv, int64_t gn, double2* invD) {
+                            const int32_t* gtr, const double* gtv, int64_t gn, double2* invD, int raw = 0) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < gn; c += (int64_t)gridDim.x * blockDim.x) {
     const int64_t lo = gtp[c], hi = gtp[c + 1];
     double2 d = make_double2(0.0, 0.0);
@@ -285,7 +285,8 @@ __global__ void k_grad_diag(const int64_t* rowptr, const int32_t* col, const dou
       d.x = fma(gtv[j], acc.x, d.x);
       d.y = fma(gtv[j], acc.y, d.y);
     }
-    invD[c] = (d.x == 0.0 && d.y == 0.0) ? make_double2(0.0, 0.0) : ddiv(make_double2(1.0, 0.0), d);
+    if (raw) invD[c] = d;
+    else invD[c] = (d.x == 0.0 && d.y == 0.0) ? make_double2(0.0, 0.0) : ddiv(make_double2(1.0, 0.0), d);
   }
 }
 
