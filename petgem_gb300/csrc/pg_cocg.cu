@@ -442,7 +442,7 @@ int run_cocg(const Plan& P, const int64_t* rowptr, const int32_t* col, const dou
     k_cg_scale_matrix<CM><<<pg_blocks(P.n, 256), 256, 0, s>>>(rowptr, col, A, P.n, S, At);
     if (grad) {
       k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n, Sinv);
-      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+      k_grad_diag<<<pg_blocks(P.gn * 32, 256), 256, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                        P.gn, invD);
     }
   }

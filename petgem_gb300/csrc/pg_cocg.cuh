@@ -180,6 +180,56 @@ __global__ void k_to_f32(const double2* __restrict__ a, int64_t n, float2* __res
     out[e] = make_float2((float)a[e].x, (float)a[e].y);
 }
 
+// acc += sum_j g_j v[c_j * K + rhs] over [j0, j1) of a map row (FP32 products
+// of the FP64 map values), accumulated in entry order; four entries' index
+// and value loads are issued before their four gathers, so a thread keeps
+// four independent gathers in flight instead of one dependent chain.
+template <int K>
+__device__ __forceinline__ void grad_gather4(const int32_t* __restrict__ gc, const double* __restrict__ gv,
+                                             const float2* __restrict__ v, int64_t j, int rhs, float2& acc) {
+  int32_t c[4];
+  float g[4];
+  float2 w[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    c[i] = gc[j + i];
+    g[i] = __double2float_rn(gv[j + i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) w[i] = v[(int64_t)c[i] * K + rhs];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    acc.x = fmaf(g[i], w[i].x, acc.x);
+    acc.y = fmaf(g[i], w[i].y, acc.y);
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void grad_gather1(const int32_t* __restrict__ gc, const double* __restrict__ gv,
+                                             const float2* __restrict__ v, int64_t j, int rhs, float2& acc) {
+  const float g = __double2float_rn(gv[j]);
+  const float2 w = v[(int64_t)gc[j] * K + rhs];
+  acc.x = fmaf(g, w.x, acc.x);
+  acc.y = fmaf(g, w.y, acc.y);
+}
+
+template <int K>
+__device__ __forceinline__ void grad_row_acc(const int32_t* __restrict__ gc, const double* __restrict__ gv,
+                                             const float2* __restrict__ v, int64_t j0, int64_t j1, int rhs,
+                                             float2& acc) {
+  int64_t j = j0;
+  for (; j + 4 <= j1; j += 4) grad_gather4<K>(gc, gv, v, j, rhs, acc);
+  for (; j < j1; ++j) grad_gather1<K>(gc, gv, v, j, rhs, acc);
+}
+
+template <int K>
+__device__ __forceinline__ float2 grad_row_sum(const int32_t* __restrict__ gc, const double* __restrict__ gv,
+                                               const float2* __restrict__ v, int64_t j0, int64_t j1, int rhs) {
+  float2 acc = make_float2(0.f, 0.f);
+  grad_row_acc<K>(gc, gv, v, j0, j1, rhs, acc);
+  return acc;
+}
+
 // PC (several frequencies): A_j = Re A0 + i s_j Im A0 and G is real, so
 // column j's diag(G^T A_j G) is Re d + i s_j Im d with d = diag(G^T A0 G)
 // (invD holds d; cscale the s_j).  Re d vanishes on gradient columns
@@ -197,13 +247,7 @@ __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __r
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = e / K;
     const int rhs = (int)(e % K);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
-      const float g = __double2float_rn(gtv[j]);
-      const float2 v = u[(int64_t)gtr[j] * K + rhs];
-      acc.x = fmaf(g, v.x, acc.x);
-      acc.y = fmaf(g, v.y, acc.y);
-    }
+    const float2 acc = grad_row_sum<K>(gtr, gtv, u, gtp[c], gtp[c + 1], rhs);
     float2 w;
     if (PC) {
       // invD holds the diagonal d of G^T A0 G; column rhs divides by
@@ -247,14 +291,7 @@ __global__ void __launch_bounds__(kThreads) k_grad_restrict(const int64_t* __res
   const int64_t total = gn * K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = e / K;
-    const int rhs = (int)(e % K);
-    double2 acc = make_double2(0.0, 0.0);
-    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
-      const double g = gtv[j];
-      const double2 v = u[(int64_t)gtr[j] * K + rhs];
-      acc.x = fma(g, v.x, acc.x);
-      acc.y = fma(g, v.y, acc.y);
-    }
+    const double2 acc = grad_row_sum64<K>(gtr, gtv, u, gtp[c], gtp[c + 1], (int)(e % K));
     t[e] = cmul(invD[c], acc);
   }
 }
@@ -281,14 +318,7 @@ __global__ void __launch_bounds__(kThreads) k_grad_prolong(const int64_t* __rest
   double2 rho = make_double2(0.0, 0.0);
   for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
     const int64_t row = e / K;
-    const int rhs = (int)(e % K);
-    double2 acc = make_double2(0.0, 0.0);
-    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
-      const double g = gv[j];
-      const double2 v = t[(int64_t)gc[j] * K + rhs];
-      acc.x = fma(g, v.x, acc.x);
-      acc.y = fma(g, v.y, acc.y);
-    }
+    const double2 acc = grad_row_sum64<K>(gc, gv, t, gp[row], gp[row + 1], (int)(e % K));
     const double2 re = r[e];
     const double2 ze = dadd(re, cmul(Sinv[row], acc));
     z[e] = ze;

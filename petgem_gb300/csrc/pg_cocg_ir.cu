@@ -288,14 +288,7 @@ __global__ void __launch_bounds__(kThreads) k_irg_prolong(const int64_t* __restr
   float2 rho = make_float2(0.f, 0.f);
   for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
     const int64_t row = e / K;
-    const int rhs = (int)(e % K);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
-      const float g = __double2float_rn(gv[j]);
-      const float2 v = t[(int64_t)gc[j] * K + rhs];
-      acc.x = fmaf(g, v.x, acc.x);
-      acc.y = fmaf(g, v.y, acc.y);
-    }
+    const float2 acc = grad_row_sum<K>(gc, gv, t, gp[row], gp[row + 1], (int)(e % K));
     const float2 re = r[e];
     const float2 ze = cfma(Sinv[row], acc, re);
     z[e] = ze;
@@ -593,7 +586,7 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
       double2* tmp = reinterpret_cast<double2*>(ws + off[15]);   // FP64 scratch (n * k >= n, gn entries)
       k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(S, P.n, tmp);
       k_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(tmp, P.n, gSinv);
-      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+      k_grad_diag<<<pg_blocks(P.gn * 32, 256), 256, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                        P.gn, tmp);
       k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, ginvD);
     }

@@ -386,14 +386,7 @@ __global__ void __launch_bounds__(kThreads) k_sg_prolong(const int64_t* __restri
   float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
     const int64_t row = e / K;
-    const int rhs = (int)(e % K);
-    float2 acc = make_float2(0.f, 0.f);
-    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
-      const float gf = __double2float_rn(gv[j]);
-      const float2 v = t[(int64_t)gc[j] * K + rhs];
-      acc.x = fmaf(gf, v.x, acc.x);
-      acc.y = fmaf(gf, v.y, acc.y);
-    }
+    const float2 acc = grad_row_sum<K>(gc, gv, t, gp[row], gp[row + 1], (int)(e % K));
     const float2 cr = cmul(Sinv[row], acc);
     const float4 re = r[e];
     float4 ze = re;
@@ -777,7 +770,7 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
       double2* tmp = reinterpret_cast<double2*>(gz);   // FP64 scratch until the first z
       k_grad_sinv<<<pg_blocks(P.n, 256), 256, 0, s>>>(Sd, P.n, tmp);
       k_to_f32<<<pg_blocks(P.n, 256), 256, 0, s>>>(tmp, P.n, gSinv);
-      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+      k_grad_diag<<<pg_blocks(P.gn * 32, 256), 256, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                        P.gn, tmp);
       k_to_f32<<<pg_blocks(P.gn, 256), 256, 0, s>>>(tmp, P.gn, ginvD);
     }

@@ -318,14 +318,7 @@ __global__ void __launch_bounds__(kThreads) k_gm_restrict(const int64_t* __restr
   const int64_t total = gn * K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = e / K;
-    const int rhs = (int)(e % K);
-    double2 acc = make_double2(0.0, 0.0);
-    for (int64_t j = gtp[c]; j < gtp[c + 1]; ++j) {
-      const double g = gtv[j];
-      const double2 x = to_d(v[(int64_t)gtr[j] * K + rhs]);
-      acc.x = fma(g, x.x, acc.x);
-      acc.y = fma(g, x.y, acc.y);
-    }
+    const double2 acc = grad_row_sum64<K>(gtr, gtv, v, gtp[c], gtp[c + 1], (int)(e % K));
     t[e] = cmul(invD[c], acc);
   }
 }
@@ -342,14 +335,7 @@ __global__ void __launch_bounds__(kThreads) k_gm_prolong(const int64_t* __restri
   const int64_t total = n * K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = e / K;
-    const int rhs = (int)(e % K);
-    double2 acc = make_double2(0.0, 0.0);
-    for (int64_t j = gp[row]; j < gp[row + 1]; ++j) {
-      const double g = gv[j];
-      const double2 x = t[(int64_t)gc[j] * K + rhs];
-      acc.x = fma(g, x.x, acc.x);
-      acc.y = fma(g, x.y, acc.y);
-    }
+    const double2 acc = grad_row_sum64<K>(gc, gv, t, gp[row], gp[row + 1], (int)(e % K));
     u[e] = cfrom<C>(dadd(to_d(v[e]), cmul(d[row], acc)));
   }
 }
@@ -516,7 +502,7 @@ int run_gmres(const Plan& P, const int64_t* rowptr, const int32_t* col, const do
     if (grad) {
       k_recip<<<pg_blocks(P.n, 256), 256, 0, s>>>(dinv, P.n, dA);
       k_fill_one<<<pg_blocks(P.n, 256), 256, 0, s>>>(ones, P.n);
-      k_grad_diag<<<pg_blocks(P.gn, 128), 128, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
+      k_grad_diag<<<pg_blocks(P.gn * 32, 256), 256, 0, s>>>(rowptr, col, A, o->gradt_rowptr, o->gradt_row, o->gradt_val,
                                                        P.gn, invD);
     }
   }

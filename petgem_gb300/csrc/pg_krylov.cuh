@@ -70,6 +70,41 @@ template <> __device__ __forceinline__ float2 cfrom<float2>(double2 v) { return 
 template <> __device__ __forceinline__ double2 cfrom<double2>(double2 v) { return v; }
 __device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
 __device__ __forceinline__ double2 to_d(double2 v) { return v; }
+
+// acc = sum_j g_j v[c_j * K + rhs] over [j0, j1) of a row of the auxiliary
+// map (or of its transpose), in FP64 and in entry order; four entries'
+// index and value loads are issued before their four gathers, so a thread
+// keeps four independent gathers in flight instead of one dependent chain.
+template <int K, typename V>
+__device__ __forceinline__ double2 grad_row_sum64(const int32_t* __restrict__ gc, const double* __restrict__ gv,
+                                                  const V* __restrict__ v, int64_t j0, int64_t j1, int rhs) {
+  double2 acc = make_double2(0.0, 0.0);
+  int64_t j = j0;
+  for (; j + 4 <= j1; j += 4) {
+    int32_t c[4];
+    double g[4];
+    double2 w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      c[i] = gc[j + i];
+      g[i] = gv[j + i];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = to_d(v[(int64_t)c[i] * K + rhs]);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      acc.x = fma(g[i], w[i].x, acc.x);
+      acc.y = fma(g[i], w[i].y, acc.y);
+    }
+  }
+  for (; j < j1; ++j) {
+    const double2 w = to_d(v[(int64_t)gc[j] * K + rhs]);
+    acc.x = fma(gv[j], w.x, acc.x);
+    acc.y = fma(gv[j], w.y, acc.y);
+  }
+  return acc;
+}
+
 __device__ __forceinline__ double2 dadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 dsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 dscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
@@ -260,16 +295,24 @@ bool valid_k(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || 
 // columns, from pg_gradient_map) and its transpose (rows ascending).
 // invD[phi] = 1 / (G^T A G)_{phi phi} (0 for an empty or vanishing column;
 // raw != 0 stores the diagonal itself).  (A G_phi)_r = sum_k A_rk G_{k phi};
-// G_{k phi} is looked up by binary search in the transpose row of phi.
+// G_{k phi} is looked up by binary search in the transpose row of phi.  One
+// warp per column (launch 32 threads per column): the warp walks the
+// column's rows r in order, lane l takes the stored entries l, l + 32, ... of
+// row r of A (coalesced loads), each lane keeps its own partial sum, and the
+// lanes' sums are combined in a fixed tree, so the result does not depend on
+// scheduling.
 __global__ void k_grad_diag(const int64_t* rowptr, const int32_t* col, const double2* A, const int64_t* gtp,
                             const int32_t* gtr, const double* gtv, int64_t gn, double2* invD, int raw = 0) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < gn; c += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = w0; c < gn; c += nw) {
     const int64_t lo = gtp[c], hi = gtp[c + 1];
     double2 d = make_double2(0.0, 0.0);
     for (int64_t j = lo; j < hi; ++j) {
       const int64_t r = gtr[j];
-      double2 acc = make_double2(0.0, 0.0);
-      for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const double gj = gtv[j];
+      for (int64_t k = rowptr[r] + lane; k < rowptr[r + 1]; k += 32) {
         const int32_t s = col[k];
         int64_t a = lo, b = hi;
         while (a < b) {
@@ -278,13 +321,18 @@ __global__ void k_grad_diag(const int64_t* rowptr, const int32_t* col, const dou
           else b = m;
         }
         if (a < hi && gtr[a] == s) {
-          acc.x = fma(A[k].x, gtv[a], acc.x);
-          acc.y = fma(A[k].y, gtv[a], acc.y);
+          const double w = gj * gtv[a];
+          d.x = fma(A[k].x, w, d.x);
+          d.y = fma(A[k].y, w, d.y);
         }
       }
-      d.x = fma(gtv[j], acc.x, d.x);
-      d.y = fma(gtv[j], acc.y, d.y);
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      d.x += __shfl_down_sync(0xffffffffu, d.x, off);
+      d.y += __shfl_down_sync(0xffffffffu, d.y, off);
+    }
+    if (lane != 0) continue;
     if (raw) invD[c] = d;
     else invD[c] = (d.x == 0.0 && d.y == 0.0) ? make_double2(0.0, 0.0) : ddiv(make_double2(1.0, 0.0), d);
   }
