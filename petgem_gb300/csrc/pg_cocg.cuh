@@ -233,7 +233,12 @@ __device__ __forceinline__ float2 grad_row_sum(const int32_t* __restrict__ gc, c
 // PC (several frequencies): A_j = Re A0 + i s_j Im A0 and G is real, so
 // column j's diag(G^T A_j G) is Re d + i s_j Im d with d = diag(G^T A0 G)
 // (invD holds d; cscale the s_j).  Re d vanishes on gradient columns
-// (G^T K G = 0) but not on vector P1 columns.
+// (G^T K G = 0) but not on vector P1 columns.  K >= 4: a thread takes one
+// column and 4 RHS (kGradQ), loading each gathered u row slice as two 16-byte
+// vectors and the entry's index and value once for the 4; every RHS is
+// still summed in entry order.  Launch ceil(gn * K / kGradQ(K)) threads.
+__host__ __device__ constexpr int kGradQ(int k) { return k >= 4 ? 4 : 1; }
+
 template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __restrict__ gtp,
                                                            const int32_t* __restrict__ gtr,
@@ -243,12 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __r
                                                            float2* __restrict__ t, const CgCtl* ctl, int start,
                                                            const float* __restrict__ cscale = nullptr) {
   if (!start && !ctl->pending) return;
-  const int64_t total = gn * K;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = e / K;
-    const int rhs = (int)(e % K);
-    const float2 acc = grad_row_sum<K>(gtr, gtv, u, gtp[c], gtp[c + 1], rhs);
-    float2 w;
+  auto scaled = [&](int64_t c, int rhs, float2 acc) {
     if (PC) {
       // invD holds the diagonal d of G^T A0 G; column rhs divides by
       // Re d + i s_j Im d (scaled by the larger part against underflow)
@@ -259,14 +259,48 @@ __global__ void __launch_bounds__(kThreads) k_grad_restrict32(const int64_t* __r
         dx /= m;
         dy /= m;
         const float den = m * fmaf(dx, dx, dy * dy);
-        w = make_float2(fmaf(acc.x, dx, acc.y * dy) / den, fmaf(acc.y, dx, -acc.x * dy) / den);
-      } else {
-        w = make_float2(0.f, 0.f);
+        return make_float2(fmaf(acc.x, dx, acc.y * dy) / den, fmaf(acc.y, dx, -acc.x * dy) / den);
       }
-    } else {
-      w = cmul(invD[c], acc);
+      return make_float2(0.f, 0.f);
     }
-    t[e] = w;
+    return cmul(invD[c], acc);
+  };
+  constexpr int Q = kGradQ(K), KQ = K / Q;
+  const int64_t total = gn * KQ;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / KQ;
+    if constexpr (Q == 1) {
+      const int rhs = (int)(e % KQ);
+      t[e] = scaled(c, rhs, grad_row_sum<K>(gtr, gtv, u, gtp[c], gtp[c + 1], rhs));
+    } else {
+      // RHS r0 .. r0 + 3: u rows and t are 8-byte complex values with K a
+      // multiple of 4, so each slice starts on a 32-byte boundary
+      const int r0 = (int)(e % KQ) * Q;
+      float2 acc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
+      const int64_t j1 = gtp[c + 1];
+#pragma unroll 2
+      for (int64_t j = gtp[c]; j < j1; ++j) {
+        const float g = __double2float_rn(gtv[j]);
+        const float4* up = reinterpret_cast<const float4*>(u + (int64_t)gtr[j] * K + r0);
+        const float4 a = up[0], b = up[1];
+        acc[0].x = fmaf(g, a.x, acc[0].x);
+        acc[0].y = fmaf(g, a.y, acc[0].y);
+        acc[1].x = fmaf(g, a.z, acc[1].x);
+        acc[1].y = fmaf(g, a.w, acc[1].y);
+        acc[2].x = fmaf(g, b.x, acc[2].x);
+        acc[2].y = fmaf(g, b.y, acc[2].y);
+        acc[3].x = fmaf(g, b.z, acc[3].x);
+        acc[3].y = fmaf(g, b.w, acc[3].y);
+      }
+      float2 w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q] = scaled(c, r0 + q, acc[q]);
+      float4* tp = reinterpret_cast<float4*>(t + c * K + r0);
+      tp[0] = make_float4(w[0].x, w[0].y, w[1].x, w[1].y);
+      tp[1] = make_float4(w[2].x, w[2].y, w[3].x, w[3].y);
+    }
   }
 }
 

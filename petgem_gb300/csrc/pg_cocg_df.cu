@@ -845,7 +845,7 @@ int run_cocg_df(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   float4* gz = reinterpret_cast<float4*>(ws + off[23]);
   float2* gu = reinterpret_cast<float2*>(ws + off[24]);
   float* gscale = reinterpret_cast<float*>(ws + off[25]);
-  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
+  const unsigned gblocks = pg_blocks(P.gn * P.k / kGradQ(P.k), kThreads);   // k_grad_restrict32 only
   float4* At = reinterpret_cast<float4*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);

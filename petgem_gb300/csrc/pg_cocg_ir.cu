@@ -530,7 +530,7 @@ int run_cocg_ir(const Plan& P, const int64_t* rowptr, const int32_t* col, const 
   float2* gt = reinterpret_cast<float2*>(ws + off[18]);
   float2* gz = reinterpret_cast<float2*>(ws + off[19]);
   float2* gu = reinterpret_cast<float2*>(ws + off[20]);
-  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
+  const unsigned gblocks = pg_blocks(P.gn * P.k / kGradQ(P.k), kThreads);   // k_grad_restrict32 only
   float2* At = reinterpret_cast<float2*>(ws + off[0]);
   double2* S = reinterpret_cast<double2*>(ws + off[1]);
   double* wd = reinterpret_cast<double*>(ws + off[2]);

@@ -726,7 +726,7 @@ int run_cocg_seg(const SegPlan& P, const int64_t* hrows, const int64_t* rowptr, 
   float2* gt = reinterpret_cast<float2*>(ws + off[20]);
   float4* gz = reinterpret_cast<float4*>(ws + off[21]);
   float2* gu = reinterpret_cast<float2*>(ws + off[22]);
-  const unsigned gblocks = pg_blocks(P.gn * P.k, kThreads);
+  const unsigned gblocks = pg_blocks(P.gn * P.k / kGradQ(P.k), kThreads);   // k_grad_restrict32 only
   std::vector<int> hblk = seg_blocks(hrows, P.S, k), cur_blk;
   std::vector<char> sys_active(P.S, 1);
   PG_CUDA_TRY(cudaMemcpyAsync(drows, hrows, sizeof(int64_t) * (P.S + 1), cudaMemcpyHostToDevice, s));
