@@ -474,6 +474,32 @@ __device__ void block_reduce_df(float4 v, float4* smf, double2* out) {
   __syncthreads();
 }
 
+// The same when a thread holds 4 RHS, r0 .. r0 + 3 with r0 = 4 (lane % (K /
+// 4)) (K >= 4): lanes with the same r0 are combined, then the warps in order.
+template <int K>
+__device__ void block_reduce_df_q4(const float4 (&rho)[4], float4* smf, double2* out) {
+  constexpr int KQ = K / 4;
+  float4 v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = rho[q];
+#pragma unroll
+    for (int off = 16; off >= KQ; off >>= 1) cdf_add(v[q], shfl_xor4(v[q], off));
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < KQ) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) smf[warp * K + lane * 4 + q] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    float4 t = smf[threadIdx.x];
+    for (int w = 1; w < kThreads / 32; ++w) cdf_add(t, smf[w * K + threadIdx.x]);
+    out[threadIdx.x] = cdf_to(t);
+  }
+  __syncthreads();
+}
+
 template <int K>
 __device__ void block_reduce_f(float v, float* smf, double2* out) {
 #pragma unroll

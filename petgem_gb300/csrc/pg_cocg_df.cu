@@ -154,7 +154,9 @@ __global__ void k_dfg_u_start(const double2* __restrict__ r64, int64_t n, float2
 // z = r + S^-1 (G t), partial rho = r^T z (double-float); in an iteration the
 // last block sets beta = rho / rho_old and rho for the RHS updated in it
 // (beta_iter == 1); at a cycle start p = z when set_p.  PC (several
-// frequencies): S^-1 per element, and ps = S o p is set with p.
+// frequencies): S^-1 per element, and ps = S o p is set with p.  K >= 4: a
+// thread takes one row and 4 RHS (two 16-byte gathers of t per entry, the
+// entry's index and value loaded once for the 4).
 template <int K, bool PC = false>
 __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restrict__ gp,
                                                           const int32_t* __restrict__ gc,
@@ -169,13 +171,6 @@ __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restr
   if (!start && !ctl->pending) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ float4 smf[(kThreads / 32) * kMaxK];
-  const int64_t total = n * K;
-  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
-  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
-  float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
-  // two items per step (e and e + kThreads), so each thread has two
-  // independent load chains in flight; the items are summed into rho in
-  // increasing e, as a one-item loop would
   auto finish = [&](int64_t e, float2 acc, float4& re, float4& ze) {
     const float2 cr = cmul(Sinv[PC ? e : e / K], acc);
     re = r[e];
@@ -199,47 +194,95 @@ __global__ void __launch_bounds__(kThreads) k_dfg_prolong(const int64_t* __restr
       }
     }
   };
-  int64_t e = lo + threadIdx.x;
-  for (; e + kThreads < hi; e += 2 * kThreads) {
-    // both rows' entries in one loop (each row summed in entry order); one
-    // RHS: four entries of each row per step, eight gathers in flight (with
-    // 16 RHS the unrolled form measured 9 % slower: the 16 lanes of a row
-    // already share its index loads)
-    const int64_t eb = e + kThreads, rowa = e / K, rowb = eb / K;
-    const int64_t ja0 = gp[rowa], jae = gp[rowa + 1], jb0 = gp[rowb], jbe = gp[rowb + 1];
-    const int rha = (int)(e % K), rhb = (int)(eb % K);
-    float2 acca = make_float2(0.f, 0.f), accb = make_float2(0.f, 0.f);
-    if constexpr (K == 1) {
-      const int64_t nmin = min(jae - ja0, jbe - jb0);
-      int64_t s = 0;
-      for (; s + 4 <= nmin; s += 4) {
-        grad_gather4<K>(gc, gv, t, ja0 + s, rha, acca);
-        grad_gather4<K>(gc, gv, t, jb0 + s, rhb, accb);
+  if constexpr (kGradQ(K) == 4) {
+    // (row, quad) items; a block's range starts on a row, so a thread's
+    // quad is lane % KQ throughout
+    constexpr int KQ = K / 4;
+    const int64_t totq = n * KQ;
+    const int64_t chq = ((totq + gridDim.x - 1) / gridDim.x + KQ - 1) / KQ * KQ;
+    const int64_t lq = (int64_t)blockIdx.x * chq, hq = min(totq, lq + chq);
+    float4 rq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rq[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t f = lq + threadIdx.x; f < hq; f += kThreads) {
+      const int64_t row = f / KQ;
+      const int r0 = (int)(f % KQ) * 4;
+      float2 acc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
+      const int64_t j1 = gp[row + 1];
+#pragma unroll 2
+      for (int64_t j = gp[row]; j < j1; ++j) {
+        const float g = __double2float_rn(gv[j]);
+        const float4* tp = reinterpret_cast<const float4*>(t + (int64_t)gc[j] * K + r0);
+        const float4 a = tp[0], b = tp[1];
+        acc[0].x = fmaf(g, a.x, acc[0].x);
+        acc[0].y = fmaf(g, a.y, acc[0].y);
+        acc[1].x = fmaf(g, a.z, acc[1].x);
+        acc[1].y = fmaf(g, a.w, acc[1].y);
+        acc[2].x = fmaf(g, b.x, acc[2].x);
+        acc[2].y = fmaf(g, b.y, acc[2].y);
+        acc[3].x = fmaf(g, b.z, acc[3].x);
+        acc[3].y = fmaf(g, b.w, acc[3].y);
       }
-      grad_row_acc<K>(gc, gv, t, ja0 + s, jae, rha, acca);
-      grad_row_acc<K>(gc, gv, t, jb0 + s, jbe, rhb, accb);
-    } else {
-      const int64_t steps = max(jae - ja0, jbe - jb0);
-      for (int64_t s = 0; s < steps; ++s) {
-        if (ja0 + s < jae) grad_gather1<K>(gc, gv, t, ja0 + s, rha, acca);
-        if (jb0 + s < jbe) grad_gather1<K>(gc, gv, t, jb0 + s, rhb, accb);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int64_t e = row * K + r0 + q;
+        float4 re, ze;
+        finish(e, acc[q], re, ze);
+        store(e, ze);
+        cdf_mac(rq[q], re, ze);
       }
     }
-    float4 ra, za, rb, zb;
-    finish(e, acca, ra, za);
-    finish(eb, accb, rb, zb);
-    store(e, za);
-    store(e + kThreads, zb);
-    cdf_mac(rho, ra, za);
-    cdf_mac(rho, rb, zb);
+    block_reduce_df_q4<K>(rq, smf, prho + (int64_t)blockIdx.x * K);
+  } else {
+    const int64_t total = n * K;
+    const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+    const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+    float4 rho = make_float4(0.f, 0.f, 0.f, 0.f);
+    // two items per step (e and e + kThreads), so each thread has two
+    // independent load chains in flight; the items are summed into rho in
+    // increasing e, as a one-item loop would
+    int64_t e = lo + threadIdx.x;
+    for (; e + kThreads < hi; e += 2 * kThreads) {
+      // both rows' entries in one loop (each row summed in entry order); one
+      // RHS: four entries of each row per step, eight gathers in flight
+      const int64_t eb = e + kThreads, rowa = e / K, rowb = eb / K;
+      const int64_t ja0 = gp[rowa], jae = gp[rowa + 1], jb0 = gp[rowb], jbe = gp[rowb + 1];
+      const int rha = (int)(e % K), rhb = (int)(eb % K);
+      float2 acca = make_float2(0.f, 0.f), accb = make_float2(0.f, 0.f);
+      if constexpr (K == 1) {
+        const int64_t nmin = min(jae - ja0, jbe - jb0);
+        int64_t s = 0;
+        for (; s + 4 <= nmin; s += 4) {
+          grad_gather4<K>(gc, gv, t, ja0 + s, rha, acca);
+          grad_gather4<K>(gc, gv, t, jb0 + s, rhb, accb);
+        }
+        grad_row_acc<K>(gc, gv, t, ja0 + s, jae, rha, acca);
+        grad_row_acc<K>(gc, gv, t, jb0 + s, jbe, rhb, accb);
+      } else {
+        const int64_t steps = max(jae - ja0, jbe - jb0);
+        for (int64_t s = 0; s < steps; ++s) {
+          if (ja0 + s < jae) grad_gather1<K>(gc, gv, t, ja0 + s, rha, acca);
+          if (jb0 + s < jbe) grad_gather1<K>(gc, gv, t, jb0 + s, rhb, accb);
+        }
+      }
+      float4 ra, za, rb, zb;
+      finish(e, acca, ra, za);
+      finish(eb, accb, rb, zb);
+      store(e, za);
+      store(e + kThreads, zb);
+      cdf_mac(rho, ra, za);
+      cdf_mac(rho, rb, zb);
+    }
+    if (e < hi) {
+      float4 ra, za;
+      item(e, ra, za);
+      store(e, za);
+      cdf_mac(rho, ra, za);
+    }
+    block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   }
-  if (e < hi) {
-    float4 ra, za;
-    item(e, ra, za);
-    store(e, za);
-    cdf_mac(rho, ra, za);
-  }
-  block_reduce_df<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   if (!start && arrive_last(&ctl->counter)) {
     const double2 rr = sum_partials<K>(prho, gridDim.x, threadIdx.x < K ? threadIdx.x : 0, smem);
     if (threadIdx.x < K) {
