@@ -85,3 +85,36 @@ def test_vector_p1_columns_exact_and_consistent(p):
     gx = np.zeros(G.shape[1])
     gx[:len(nodes)] = nodes[:, 0]
     assert abs(u - G @ gx).max() <= 1e-9 * abs(u).max()
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_auxiliary_diagonal_across_frequencies(p):
+    """The several-frequency solver keeps one diagonal d = diag(Bᵀ A0 B) of
+    the auxiliary map B = [G Π] and divides each column by Re d + i s_j Im d:
+    with A_j = Re A0 + i s_j Im A0 and B real that is diag(Bᵀ A_j B) exactly.
+    The plain rescale s_j d holds on the gradient columns only (K G = 0, so
+    Re d vanishes there) and not on the vector P1 columns."""
+    nodes, tets = _box()
+    mm = system.mesh_maps(nodes, tets, p)
+    M, K = system.element_matrices(nodes[tets], mm["eo"], mm["fo"], np.ones((len(tets), 2)), p, processes=1)
+    Kg, Mg = _global(K, mm["dofs"], mm["N"]), _global(M, mm["dofs"], mm["N"])
+    Bfull, _ = gradient.gradient_map(tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"],
+                                     len(nodes), p, pec=mm["bnd"], vector=True, nodes=nodes)
+    # the columns PEC left (vector columns come after the gradient columns)
+    used = np.flatnonzero(np.diff(Bfull.tocsc().indptr) > 0)
+    is_vec = used >= Bfull.shape[1] - 3 * len(nodes)
+    assert is_vec.any() and (~is_vec).any()
+    B = Bfull.tocsc()[:, used]
+    # a frequency at which curl-curl and mass terms are of one size (where the
+    # rescale's error matters)
+    c = 0.7 * abs(Kg).max() / abs(Mg).max()
+    A0 = (Kg - 1j * c * Mg).tocsr()
+    d0 = np.asarray((B.T @ (A0 @ B)).diagonal())
+    for s in (0.25, 0.5, 2.0):
+        Aj = (Kg - 1j * c * s * Mg).tocsr()
+        dj = np.asarray((B.T @ (Aj @ B)).diagonal())
+        split = d0.real + 1j * s * d0.imag
+        assert abs(dj - split).max() <= 1e-12 * abs(dj).max()
+        scaled = s * d0
+        assert abs(dj - scaled)[~is_vec].max() <= 1e-10 * abs(dj).max()
+        assert abs(dj - scaled)[is_vec].max() >= 1e-2 * abs(dj[is_vec]).max()
