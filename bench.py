@@ -714,7 +714,8 @@ def profile_solves(args, torch, mesh, vals, b):
                                      ("cocg_mixed_batched", "cocg", "mixed", B, "block"),
                                      ("gmres_mixed", "gmres", "mixed", b, "block"), ("gmres_fp64", "gmres", "fp64", b, "block"),
                                      ("cocg_fp64_grad", "cocg", "fp64", b, "grad"),
-                                     ("cocg_df64_grad_batched", "cocg", "df64", B, "grad")):
+                                     ("cocg_df64_grad_batched", "cocg", "df64", B, "grad"),
+                                     ("cocg_ir32_grad_batched", "cocg", "ir32", B, "grad")):
         if args.profile_only and name not in args.profile_only.split(","):
             continue
         torch.cuda.synchronize()

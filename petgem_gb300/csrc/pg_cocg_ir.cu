@@ -47,6 +47,38 @@ __device__ void block_reduce_c32(float2 v, float2* smf, double2* out) {
   __syncthreads();
 }
 
+// The same when a thread holds 4 RHS, r0 .. r0 + 3 with r0 = 4 (lane % (K /
+// 4)) (K >= 4): lanes with the same r0 are combined, then the warps in order.
+template <int K>
+__device__ void block_reduce_c32_q4(const float2 (&rho)[4], float2* smf, double2* out) {
+  constexpr int KQ = K / 4;
+  float2 v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    v[q] = rho[q];
+#pragma unroll
+    for (int off = 16; off >= KQ; off >>= 1) {
+      v[q].x += __shfl_xor_sync(0xffffffffu, v[q].x, off);
+      v[q].y += __shfl_xor_sync(0xffffffffu, v[q].y, off);
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < KQ) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) smf[warp * K + lane * 4 + q] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double sx = 0.0, sy = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) {
+      sx += (double)smf[w * K + threadIdx.x].x;
+      sy += (double)smf[w * K + threadIdx.x].y;
+    }
+    out[threadIdx.x] = make_double2(sx, sy);
+  }
+  __syncthreads();
+}
+
 __device__ __forceinline__ float2 c32_bilin_add(float2 acc, float2 a, float2 b) {   // acc + a*b
   return cfma(a, b, acc);
 }
@@ -269,7 +301,10 @@ __global__ void __launch_bounds__(kThreads) k_ir_update(float2* __restrict__ y, 
 // Gradient correction in the complex64 inner solve (diagonal scaling):
 // z = r + S^-1 (G t) in FP32, partial rho = r^T z; inside an iteration the
 // last block sets beta = rho / rho_old and rho for the RHS updated in it
-// (beta_iter == 1).  At an inner start (start = 1) p = z.
+// (beta_iter == 1).  At an inner start (start = 1) p = z.  K >= 4: a thread
+// takes one row and 4 RHS (two 16-byte gathers of t per entry, the entry's
+// index and value loaded once for the 4; z as before, rho's partial sums in
+// another fixed order).
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_irg_prolong(const int64_t* __restrict__ gp,
                                                           const int32_t* __restrict__ gc,
@@ -282,20 +317,77 @@ __global__ void __launch_bounds__(kThreads) k_irg_prolong(const int64_t* __restr
   if (!start && !ctl->pending) return;
   __shared__ double2 smem[2 * (kThreads / 32) * kMaxK];
   __shared__ float2 smf[(kThreads / 32) * kMaxK];
-  const int64_t total = n * K;
-  const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
-  const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
-  float2 rho = make_float2(0.f, 0.f);
-  for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
-    const int64_t row = e / K;
-    const float2 acc = grad_row_sum<K>(gc, gv, t, gp[row], gp[row + 1], (int)(e % K));
-    const float2 re = r[e];
-    const float2 ze = cfma(Sinv[row], acc, re);
-    z[e] = ze;
-    if (start) pv[e] = ze;
-    rho = cfma(re, ze, rho);
+  if constexpr (kGradQ(K) == 4) {
+    // (row, quad) items; a block's range starts on a row, so a thread's
+    // quad is lane % KQ throughout; r, z, p and t slices start on 32 bytes
+    constexpr int KQ = K / 4;
+    const int64_t totq = n * KQ;
+    const int64_t chq = ((totq + gridDim.x - 1) / gridDim.x + KQ - 1) / KQ * KQ;
+    const int64_t lq = (int64_t)blockIdx.x * chq, hq = min(totq, lq + chq);
+    float2 rq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rq[q] = make_float2(0.f, 0.f);
+    for (int64_t f = lq + threadIdx.x; f < hq; f += kThreads) {
+      const int64_t row = f / KQ;
+      const int r0 = (int)(f % KQ) * 4;
+      float2 acc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
+      const int64_t j1 = gp[row + 1];
+#pragma unroll 2
+      for (int64_t j = gp[row]; j < j1; ++j) {
+        const float g = __double2float_rn(gv[j]);
+        const float4* tp = reinterpret_cast<const float4*>(t + (int64_t)gc[j] * K + r0);
+        const float4 a = tp[0], b = tp[1];
+        acc[0].x = fmaf(g, a.x, acc[0].x);
+        acc[0].y = fmaf(g, a.y, acc[0].y);
+        acc[1].x = fmaf(g, a.z, acc[1].x);
+        acc[1].y = fmaf(g, a.w, acc[1].y);
+        acc[2].x = fmaf(g, b.x, acc[2].x);
+        acc[2].y = fmaf(g, b.y, acc[2].y);
+        acc[3].x = fmaf(g, b.z, acc[3].x);
+        acc[3].y = fmaf(g, b.w, acc[3].y);
+      }
+      const int64_t e0 = row * K + r0;
+      const float2 sv = Sinv[row];
+      const float4* rp = reinterpret_cast<const float4*>(r + e0);
+      const float4 ra = rp[0], rb = rp[1];
+      const float2 re[4] = {make_float2(ra.x, ra.y), make_float2(ra.z, ra.w), make_float2(rb.x, rb.y),
+                            make_float2(rb.z, rb.w)};
+      float2 ze[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ze[q] = cfma(sv, acc[q], re[q]);
+        rq[q] = cfma(re[q], ze[q], rq[q]);
+      }
+      const float4 za = make_float4(ze[0].x, ze[0].y, ze[1].x, ze[1].y);
+      const float4 zb = make_float4(ze[2].x, ze[2].y, ze[3].x, ze[3].y);
+      float4* zp = reinterpret_cast<float4*>(z + e0);
+      zp[0] = za;
+      zp[1] = zb;
+      if (start) {
+        float4* pp = reinterpret_cast<float4*>(pv + e0);
+        pp[0] = za;
+        pp[1] = zb;
+      }
+    }
+    block_reduce_c32_q4<K>(rq, smf, prho + (int64_t)blockIdx.x * K);
+  } else {
+    const int64_t total = n * K;
+    const int64_t chunk = ((total + gridDim.x - 1) / gridDim.x + K - 1) / K * K;
+    const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(total, lo + chunk);
+    float2 rho = make_float2(0.f, 0.f);
+    for (int64_t e = lo + threadIdx.x; e < hi; e += kThreads) {
+      const int64_t row = e / K;
+      const float2 acc = grad_row_sum<K>(gc, gv, t, gp[row], gp[row + 1], (int)(e % K));
+      const float2 re = r[e];
+      const float2 ze = cfma(Sinv[row], acc, re);
+      z[e] = ze;
+      if (start) pv[e] = ze;
+      rho = cfma(re, ze, rho);
+    }
+    block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   }
-  block_reduce_c32<K>(rho, smf, prho + (int64_t)blockIdx.x * K);
   if (!start && arrive_last(&ctl->counter)) {
     const double2 rr = sum_partials<K>(prho, gridDim.x, threadIdx.x < K ? threadIdx.x : 0, smem);
     if (threadIdx.x < K) {
