@@ -454,7 +454,8 @@ typedef struct pg_gmres_opts {
   int64_t block_edges, block_faces, block_volumes;
   /* gradient correction (diagonal Jacobi, block_p 0; grad_rowptr NULL =
    * off), as in pg_cocg_opts: GMRES runs on A B with
-   * B = D^-1 + G diag(G^T A G)^-1 G^T (right preconditioning; in precision
+   * B = D^-1 + G diag(G^T A G)^-1 G^T, G the map of pg_gradient_map (with
+   * or without its vector P1 columns; right preconditioning; in precision
    * 1 the correction of the Arnoldi steps runs on the complex64 basis). */
   int64_t grad_cols;
   const int64_t* grad_rowptr;
@@ -521,8 +522,9 @@ typedef struct pg_cocg_opts {
    *   B = D^-1 + G diag(G^T A G)^-1 G^T
    * (D = diag A; diag(G^T A G) is formed from A when the solve starts), which
    * adds a Jacobi step on the gradient fields that the edge Jacobi step
-   * cannot reduce; no petgem counterpart (petgem/solver.py:584-594 leaves
-   * the preconditioner to PETSc). */
+   * cannot reduce, and (when the map carries its vector P1 columns) one on
+   * the vector-nodal fields; no petgem counterpart (petgem/solver.py:584-594
+   * leaves the preconditioner to PETSc). */
   int64_t grad_cols;
   const int64_t* grad_rowptr;
   const int32_t* grad_col;
