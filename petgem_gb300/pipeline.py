@@ -153,7 +153,8 @@ class Solver:
         # bjacobi: one block per edge / face / element; sor (petgem's default,
         # a sequential sweep) and none run with the entity blocks as well;
         # hypre's AMS (auxiliary-space Maxwell) is served by its one-level
-        # relative, Jacobi plus the discrete-gradient correction
+        # relative, Jacobi plus one Jacobi step on the discrete gradients and
+        # (nord >= 2) on the vector P1 fields
         precond = {"jacobi": "jacobi", "hypre": "grad"}.get(pc, "block")
         if precond == "grad" and self.mesh.p > 3:
             raise ValueError("-pc_type hypre: the gradient correction is built for nord <= 3")
