@@ -81,3 +81,8 @@ def test_gradient_map_sizes_match_oracle(p):
         assert vst == -1
     else:
         assert vst == 0 and nc.value == G.shape[1] + 3 * len(nodes)
+        Gv, _ = gradient.gradient_map(tets, mm["elemsE"], mm["elemsF"], mm["eo"], mm["fo"], mm["dofs"], mm["N"],
+                                      len(nodes), p, vector=True, nodes=nodes)
+        assert Gv.shape[1] == nc.value and Gv.nnz <= me.value
+        assert lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, p, 1) > \
+            lib.pg_gradient_map_workspace_bytes(len(nodes), nE, nF, len(tets), 3, p, 0)
