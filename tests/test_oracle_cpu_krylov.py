@@ -1,5 +1,6 @@
-"""The CPU baseline solver (compiled C + OpenMP COCG, measurement
-infrastructure) solves the reference's assembled system (golden A, b, PEC)."""
+"""The CPU baseline solvers (compiled C + OpenMP COCG and petgem's restarted
+GMRES(m) + Jacobi, measurement infrastructure) solve the reference's
+assembled system (golden A, b, PEC)."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
