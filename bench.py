@@ -587,8 +587,9 @@ def run_solves(args, torch, mesh, model, vals, b):
         raise RuntimeError("a batched source was not located in the mesh (zero right-hand side)")
     x64, r64 = timed("cocg", "fp64", b, args.max_it)
     _, r64j = timed("cocg", "fp64", b, args.max_it, precond="jacobi")
-    # Jacobi plus the gradient correction D^-1 + G diag(G^T A G)^-1 G^T (the
-    # discrete gradient map is built once per mesh and timed on its own)
+    # Jacobi plus the auxiliary-space correction D^-1 + B diag(B^T A B)^-1 B^T
+    # (B = [G P], the discrete gradient and the vector P1 fields; the map is
+    # built once per mesh and timed on its own)
     torch.cuda.synchronize()
     t = time.time()
     gmap = mesh.gradient_map()
@@ -691,9 +692,10 @@ def run_solves(args, torch, mesh, model, vals, b):
     if rib.get("converged"):
         out["speedup_ir32_batched_vs_fp64_per_rhs"] = round(r64["ms_per_rhs"] / max(rib["ms_per_rhs"], 1e-9), 2)
     out["gmres30_mixed_300its"] = rg
-    out["note_grad"] = ("grad = diagonal Jacobi plus the gradient correction D^-1 + G diag(G^T A G)^-1 G^T "
-                        "(G: the discrete gradient of the quadratic H1 space, built on the device from the mesh); "
-                        "gmres30_fp64_grad is petgem's KSP, GMRES(30), right-preconditioned with it")
+    out["note_grad"] = ("grad = diagonal Jacobi plus the auxiliary-space correction D^-1 + B diag(B^T A B)^-1 B^T "
+                        "(B = [G P]: the discrete gradient of the quadratic H1 space and the vector P1 fields, "
+                        "built on the device from the mesh); gmres30_fp64_grad is petgem's KSP, GMRES(30), "
+                        "right-preconditioned with it")
     out["note"] = ("df64 = double-float (FP64-class, 48-bit mantissa) arithmetic on the FP32 pipes; ir32 = complex64 "
                    "inner COCG solves (matrix, vectors, products in FP32), each restarted from the FP64 true residual, "
                    "inside FP64 iterative refinement (each inner solve to a 100x residual drop, capped); at this "

@@ -384,9 +384,10 @@ class DeviceMesh:
         """Solve A x = b for this mesh's CSR pattern (see solve_csr).
         precond="block": entity block-Jacobi (each edge / face / volume's
         diagonal block factored L D L^T; COCG and GMRES); "jacobi": diagonal;
-        "grad": diagonal Jacobi plus the gradient correction
-        D^-1 + G diag(G^T A G)^-1 G^T (COCG in fp64, df64 or ir32, GMRES in
-        fp64 or mixed;
+        "grad": diagonal Jacobi plus the auxiliary-space correction
+        D^-1 + G diag(G^T A G)^-1 G^T, G = gradient_map() (the discrete
+        gradients and, for p >= 2, the vector P1 fields; COCG in fp64, df64 or
+        ir32, GMRES in fp64 or mixed;
         p <= 3; gradient_map; pec=False for systems without PEC rows, e.g.
         MT, which want fp64: their true residual has an FP64 floor)."""
         if precond not in ("block", "jacobi", "grad"):
@@ -636,9 +637,10 @@ def solve_csr(rowptr, col, vals, b, x0=None, rtol=1e-8, restart=30, max_it=20000
     S A S^T (S = D^-1/2 L^-1 per block), GMRES on A M^-1 (M^-1 = A_aa^-1 per
     block, right preconditioning: PETSc -pc_type bjacobi with one block per
     edge / face / element).
-    gradient: a GradientMap (DeviceMesh.gradient_map) for the gradient
-    correction: the preconditioner D^-1 + G diag(G^T A G)^-1 G^T (diagonal
-    Jacobi; COCG in fp64 or df64, GMRES in fp64 on the right).
+    gradient: a GradientMap (DeviceMesh.gradient_map) for the auxiliary-space
+    correction: the preconditioner D^-1 + G diag(G^T A G)^-1 G^T, G the map
+    with or without its vector P1 columns (diagonal Jacobi; COCG in fp64,
+    df64 or ir32, GMRES in fp64 or mixed on the right).
     """
     _check_csr(f"solve_csr({ksp})", rowptr, col, vals, b)
     if gradient is not None:
