@@ -84,6 +84,29 @@ class Preprocessing:
         Timers()["Preprocessing"].stop()
 
 
+def ksp_settings(opts, nord):
+    """(ksp, precond) for the solver from the PETSc options petgem's
+    KSPSolve reads (petgem/solver.py:584-594): -ksp_type gmres | cocg,
+    -pc_type jacobi | bjacobi | sor | none | hypre (-pc_hypre_type ams).
+    bjacobi: one block per edge / face / element; sor (petgem's default, a
+    sequential sweep) and none run with the entity blocks as well; hypre's
+    AMS (auxiliary-space Maxwell) is served by its one-level relative, Jacobi
+    plus one Jacobi step on the discrete gradients and (nord >= 2) on the
+    vector P1 fields, built for nord <= 3.  Anything else raises ValueError."""
+    ksp = str(opts.get("ksp_type", "gmres"))
+    if ksp not in ("gmres", "cocg"):
+        raise ValueError(f"-ksp_type {ksp}: supported types are gmres and cocg")
+    pc = str(opts.get("pc_type", "jacobi"))
+    if pc not in ("jacobi", "sor", "none", "bjacobi", "hypre"):
+        raise ValueError(f"-pc_type {pc}: supported preconditioners are jacobi, bjacobi and hypre (ams)")
+    if pc == "hypre" and str(opts.get("pc_hypre_type", "ams")) != "ams":
+        raise ValueError("-pc_type hypre: supported -pc_hypre_type is ams")
+    precond = {"jacobi": "jacobi", "hypre": "grad"}.get(pc, "block")
+    if precond == "grad" and int(nord) > 3:
+        raise ValueError("-pc_type hypre: the gradient correction is built for nord <= 3")
+    return ksp, precond
+
+
 class Solver:
     """Assembly and Krylov solve (petgem/solver.py:31-598)."""
 
@@ -142,22 +165,7 @@ class Solver:
             torch.cuda.synchronize()
             Timers()["SetBoundaries"].stop()
         Timers()["Solver"].start()
-        ksp = str(opts.get("ksp_type", "gmres"))
-        if ksp not in ("gmres", "cocg"):
-            raise ValueError(f"-ksp_type {ksp}: supported types are gmres and cocg")
-        pc = str(opts.get("pc_type", "jacobi"))
-        if pc not in ("jacobi", "sor", "none", "bjacobi", "hypre"):
-            raise ValueError(f"-pc_type {pc}: supported preconditioners are jacobi, bjacobi and hypre (ams)")
-        if pc == "hypre" and str(opts.get("pc_hypre_type", "ams")) != "ams":
-            raise ValueError("-pc_type hypre: supported -pc_hypre_type is ams")
-        # bjacobi: one block per edge / face / element; sor (petgem's default,
-        # a sequential sweep) and none run with the entity blocks as well;
-        # hypre's AMS (auxiliary-space Maxwell) is served by its one-level
-        # relative, Jacobi plus one Jacobi step on the discrete gradients and
-        # (nord >= 2) on the vector P1 fields
-        precond = {"jacobi": "jacobi", "hypre": "grad"}.get(pc, "block")
-        if precond == "grad" and self.mesh.p > 3:
-            raise ValueError("-pc_type hypre: the gradient correction is built for nord <= 3")
+        ksp, precond = ksp_settings(opts, self.mesh.p)
         self.info = []
         self.ksp = ksp
         # all polarisations in one batched solve (one SpMM per iteration)
